@@ -1,0 +1,193 @@
+// edmd_device.cuh -- device data layout and exact FP64 event arithmetic of the
+// hard-disk engine.  Every formula follows the reference routine cited beside
+// it operation for operation; the translation unit is compiled with
+// --fmad=false so no multiply-add is contracted, which makes the results
+// bit-identical to the reference built with IEEE flags.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace edmd {
+
+constexpr double NEVER = 100000000000000000000000000.0;  // src/EDMD.h:8
+constexpr int32_t NIL = -1;
+constexpr uint32_t BINF = 0xFFFFFFFFu;                   // "not in the emulated tree"
+constexpr uint64_t TIE_MAX = (1ull << 62) - 1;
+
+// event states
+constexpr uint32_t ST_NONE = 0, ST_QUEUED = 1, ST_OVF = 2;
+// event kinds by slot: [0,N) crossing, [N,2N) collision, 2N screenshot,
+// 2N+1 thermo, 2N+2 growth stop
+constexpr int SP_SCREEN = 0, SP_THERMO = 1, SP_GROW = 2, NSPECIAL = 3;
+
+// kinematic record of one disk: one 64-byte line half, so a candidate read
+// during a prediction costs two 32-byte sectors and brings the list link and
+// the collision counter along with the trajectory.
+struct __align__(64) Disk {
+  double x, y, vx, vy, tl, rad, m;
+  int32_t nxt;     // next disk in the same cell (src/EDMD.h:48 nxt)
+  uint32_t coll;   // collision counter (src/EDMD.h:52 coll)
+};
+
+// one event slot (src/EDMD.h:66-74 node) with its emulated queue key
+struct __align__(32) Ev {
+  double t;
+  uint64_t tie;    // insertion-order class and counter, see schedule()
+  uint32_t b;      // absolute calendar bucket the event enters the tree in
+  int32_t j;       // crossing direction (1..4) or collision partner
+  uint32_t ca;     // collActual: partner's counter at prediction time
+  uint32_t st;     // ST_*
+};
+
+// tournament-tree node: the minimum key of its subtree and the leaf holding it
+struct Node {
+  double t;
+  uint64_t tie;
+  uint32_t b;
+  int32_t idx;
+};
+
+struct Box {
+  double Lx, Ly, hLx, hLy;     // box and halves (boxConstantHelper src/EDMD.c:679)
+  double cxs, cys, cxf, cyf;   // cell sizes and reciprocals
+  double dtP, dtPN;            // calendar bucket width 5/N and width*N
+  int32_t Nxc, Nyc, N, pad;
+};
+
+constexpr int MAXLEV = 8;
+
+// scalar state of one system, kept in global memory between calls
+struct SysState {
+  double t, P;                 // current time, paulTime of the current bucket
+  double collT[4];             // collTermX, Y, XY, YX
+  double lastThermo;           // lastScreen of saveThermo (src/EDMD.c:5261)
+  uint64_t C;                  // insertion counter
+  uint64_t k, next_wrap;       // current absolute bucket, next overflow wrap
+  uint64_t ncol, ncol_total, ncross, nstale, npair, npred, nevents, ntrace;
+  int32_t ovf, grow, nrows, stop_reason;
+  int32_t status, err_a, err_b, pad;
+};
+
+struct SysDev {
+  Box B;
+  double res, Einit, dtime, dtimeTh, tmax;
+  int32_t L, nlev;             // tree leaves (N + NSPECIAL) and levels
+  int32_t lev_off[MAXLEV], lev_cnt[MAXLEV];
+  Disk* d;
+  double* vr;                  // growth rate per disk (src/EDMD.h:44 vr)
+  int32_t *cx, *cy, *prv, *crossX, *crossY;
+  int32_t* head;               // cell heads (cellList, src/EDMD.c:486)
+  Ev* ev;                      // 2N + NSPECIAL slots
+  int32_t *on, *op;            // overflow-bucket links (eventPaul[N])
+  Node* tree;
+  SysState* st;
+  void* trace;                 // edmd_collision records
+  int64_t trace_cap;
+  double* rows;                // thermo rows, 9 doubles each
+  int32_t rows_cap, pad;
+};
+
+// ---------------------------------------------------------------- arithmetic
+
+__device__ __forceinline__ void pbc(const Box& B, double& dx, double& dy) {  // PBC src/EDMD.c:5896
+  if (dx >= B.hLx) dx -= B.Lx;
+  else if (dx < -B.hLx) dx += B.Lx;
+  if (dy >= B.hLy) dy -= B.Ly;
+  else if (dy < -B.hLy) dy += B.Ly;
+}
+__device__ __forceinline__ double pbc_in_x(const Box& B, double d) {  // PBCinsideCellX 5922
+  if (d >= B.hLx) return d - B.Lx;
+  else if (d < -B.hLx) return d + B.Lx;
+  return d;
+}
+__device__ __forceinline__ double pbc_in_y(const Box& B, double d) {  // PBCinsideCellY 5930
+  if (d >= B.hLy) return d - B.Ly;
+  else if (d < -B.hLy) return d + B.Ly;
+  return d;
+}
+__device__ __forceinline__ int pbc_cx(const Box& B, int a) { return a < 0 ? a + B.Nxc : (a >= B.Nxc ? a - B.Nxc : a); }
+__device__ __forceinline__ int pbc_cy(const Box& B, int a) { return a < 0 ? a + B.Nyc : (a >= B.Nyc ? a - B.Nyc : a); }
+
+// freeFlyNormal src/EDMD.c:4954 / freeFlyGrow 4992 (rad advanced separately)
+__device__ __forceinline__ void free_fly(const Box& B, Disk& p, double t) {
+  double dt = t - p.tl;
+  p.tl = t;
+  p.x += dt * p.vx;
+  p.y += dt * p.vy;
+  if (p.x < 0) p.x += B.Lx;
+  else if (p.x >= B.Lx) p.x -= B.Lx;
+  if (p.y < 0) p.y += B.Ly;
+  else if (p.y >= B.Ly) p.y -= B.Ly;
+}
+
+// collisionTimeNormal src/EDMD.c:2661-2723; p1 is current at t.
+// *overlap is set when the pair overlaps by more than 0.01 (2708-2717).
+__device__ __forceinline__ double coll_time_normal(const Box& B, const Disk& p1, const Disk& p2,
+                                                   double t, bool* overlap) {
+  double lat2 = t - p2.tl;
+  double dvx = p2.vx - p1.vx;
+  double dvy = p2.vy - p1.vy;
+  double dx = (p2.x + lat2 * p2.vx) - p1.x;
+  double dy = (p2.y + lat2 * p2.vy) - p1.y;
+  pbc(B, dx, dy);
+  double b = dx * dvx + dy * dvy;
+  if (b > 0) return NEVER;
+  double v2 = dvx * dvx + dvy * dvy;
+  double d2 = dx * dx + dy * dy - 4 * p1.rad * p2.rad;
+  double det = b * b - v2 * d2;
+  if (d2 < -0.01) { *overlap = true; return NEVER; }
+  if (det < 0) return NEVER;
+  return (-b - sqrt(det)) / v2;
+}
+
+// collisionTimeGrow src/EDMD.c:2598-2659 (radii grow at vr)
+__device__ __forceinline__ double coll_time_grow(const Box& B, const Disk& p1, double vr1,
+                                                 const Disk& p2, double vr2, double t,
+                                                 bool* overlap) {
+  double lat2 = t - p2.tl;
+  double dvx = p2.vx - p1.vx;
+  double dvy = p2.vy - p1.vy;
+  double dvr = vr1 + vr2;
+  double dx = (p2.x + lat2 * p2.vx) - p1.x;
+  double dy = (p2.y + lat2 * p2.vy) - p1.y;
+  double dr = sqrt(4 * (p1.rad) * (p2.rad + lat2 * vr2));
+  pbc(B, dx, dy);
+  double b = dx * dvx + dy * dvy - dvr * dr;
+  double v2 = dvx * dvx + dvy * dvy;
+  double d2 = dx * dx + dy * dy;
+  double det = b * b - (v2 - dvr * dvr) * (d2 - dr * dr);
+  if (det < 0) return NEVER;
+  double plus = (-b + sqrt(det)) / (v2 - dvr * dvr);
+  double minus = (-b - sqrt(det)) / (v2 - dvr * dvr);
+  if (((minus > 0) && (plus > 0) && (minus < plus)) || ((minus > 0) && (plus < 0))) return minus;
+  else if (((minus > 0) && (plus > 0.000000001) && (plus < minus)) ||
+           ((minus < 0) && (plus > 0.000000001)))
+    return plus;
+  if (d2 - dr * dr < -0.01) *overlap = true;
+  return NEVER;
+}
+
+// crossingEventNormal src/EDMD.c:2405-2482 (the Grow variant 2343 is the same
+// arithmetic); returns the absolute time and direction code 1..4.
+__device__ __forceinline__ double crossing_time(const Box& B, const Disk& p, int cx, int cy,
+                                                double t, int* dir) {
+  double tx, ty;
+  int xx, yy;
+  if (p.vx < 0) { tx = pbc_in_x(B, cx * B.cxs - p.x) / p.vx; xx = 1; }
+  else { tx = pbc_in_x(B, (1 + cx) * B.cxs - p.x) / p.vx; xx = 2; }
+  if (p.vy < 0) { ty = pbc_in_y(B, cy * B.cys - p.y) / p.vy; yy = 3; }
+  else { ty = pbc_in_y(B, (1 + cy) * B.cys - p.y) / p.vy; yy = 4; }
+  if (tx < ty) { *dir = xx; return t + tx; }
+  *dir = yy;
+  return t + ty;
+}
+
+__device__ __forceinline__ bool key_less(uint32_t b1, double t1, uint64_t k1, int32_t i1,
+                                         uint32_t b2, double t2, uint64_t k2, int32_t i2) {
+  if (b1 != b2) return b1 < b2;
+  if (t1 != t2) return t1 < t2;
+  if (k1 != k2) return k1 < k2;
+  return i1 < i2;
+}
+
+}  // namespace edmd

@@ -1,0 +1,1078 @@
+// edmd_engine.cu -- serial-exact event engine (one warp per system) and the C ABI.
+//
+// Each system is advanced by one warp that pops events in exactly the order of
+// the reference's queue (src/EDMD.c:2144-2327: a calendar of N buckets of
+// width 5/N plus an overflow bucket, feeding an unbalanced BST whose in-order
+// ties go to the later insertion).  That order is emulated by the key
+//     (b, t, tie)
+// b   = absolute calendar bucket in which the event enters the BST,
+// t   = event time,
+// tie = class and counter reproducing the BST insertion order inside a bucket:
+//       class 0  re-added directly into the BST by an overflow wrap (inserted
+//                before the bucket's own list is loaded), ascending counter;
+//       class 1  pushed onto a bucket list (LIFO: loaded last-pushed-first),
+//                descending counter;
+//       class 2  inserted directly because it falls in the current bucket,
+//                ascending counter.
+// The keys live in a 32-ary tournament tree (level 0 = one leaf per disk, the
+// minimum of its crossing and collision events, plus three special events);
+// each tree level is fixed by one coalesced 32-wide load and a warp butterfly.
+// Collision prediction packs the candidates of the 3x3 neighbour cells of the
+// (up to two) disks that changed into the lanes of the warp.
+#include "edmd_device.cuh"
+#include "../../include/edmd_gpu.h"
+
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+using namespace edmd;
+
+#define FULL 0xffffffffu
+
+namespace {
+
+constexpr int MAXC = 8;          // candidates buffered per cell list per lane
+constexpr int WARPS_PER_BLOCK = 4;
+
+struct RunArgs {
+  int64_t max_coll;
+  double t_stop;
+  uint32_t flags;
+  int64_t max_events;
+  int32_t nsys;
+  int32_t* work;                 // persistent work counter
+};
+
+struct WarpSmem {
+  int32_t reg[32 * MAXC];        // per-lane walk buffers
+  int32_t comp[2 * 9 * MAXC];    // packed candidates
+  int16_t ord[2 * 9 * MAXC];     // their scan order
+};
+
+__device__ __forceinline__ Node empty_node(int idx) {
+  Node n; n.t = __longlong_as_double(0x7ff0000000000000ll); n.tie = ~0ull; n.b = BINF; n.idx = idx;
+  return n;
+}
+
+__device__ __forceinline__ bool node_less(const Node& a, const Node& b) {
+  return key_less(a.b, a.t, a.tie, a.idx, b.b, b.t, b.tie, b.idx);
+}
+
+__device__ __forceinline__ void warp_min(Node& n) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    Node m;
+    m.t = __shfl_xor_sync(FULL, n.t, o);
+    m.tie = __shfl_xor_sync(FULL, n.tie, o);
+    m.b = __shfl_xor_sync(FULL, n.b, o);
+    m.idx = __shfl_xor_sync(FULL, n.idx, o);
+    if (node_less(m, n)) n = m;
+  }
+}
+
+__device__ __forceinline__ Node ev_node(const Ev& e, int idx) {
+  Node n; n.t = e.t; n.tie = e.tie; n.b = e.b; n.idx = idx;
+  return n;
+}
+
+// recompute the leaf of `leaf` from its events and fix its path to the root
+__device__ void leaf_update(const SysDev& S, int leaf, int lane) {
+  const int N = S.B.N;
+  Node n = empty_node(leaf);
+  if (leaf < N) {
+    Ev e0 = S.ev[leaf], e1 = S.ev[N + leaf];
+    if (e0.st == ST_QUEUED) n = ev_node(e0, leaf);
+    if (e1.st == ST_QUEUED) { Node m = ev_node(e1, leaf); if (node_less(m, n)) n = m; }
+  } else {
+    Ev e = S.ev[2 * N + (leaf - N)];
+    if (e.st == ST_QUEUED) n = ev_node(e, leaf);
+  }
+  if (lane == 0) S.tree[leaf] = n;
+  __syncwarp();
+  int idx = leaf;
+  for (int h = 1; h < S.nlev; h++) {
+    int par = idx >> 5;
+    int ch = (par << 5) + lane;
+    Node c = ch < S.lev_cnt[h - 1] ? S.tree[S.lev_off[h - 1] + ch] : empty_node(0x7fffffff);
+    warp_min(c);
+    if (lane == 0) S.tree[S.lev_off[h] + par] = c;
+    __syncwarp();
+    idx = par;
+  }
+}
+
+// rebuild every level of the tree (after init or the growth stop)
+__device__ void tree_rebuild(const SysDev& S, int lane) {
+  const int N = S.B.N;
+  for (int l = lane; l < S.L; l += 32) {
+    Node n = empty_node(l);
+    if (l < N) {
+      Ev e0 = S.ev[l], e1 = S.ev[N + l];
+      if (e0.st == ST_QUEUED) n = ev_node(e0, l);
+      if (e1.st == ST_QUEUED) { Node m = ev_node(e1, l); if (node_less(m, n)) n = m; }
+    } else {
+      Ev e = S.ev[2 * N + (l - N)];
+      if (e.st == ST_QUEUED) n = ev_node(e, l);
+    }
+    S.tree[l] = n;
+  }
+  __syncwarp();
+  for (int h = 1; h < S.nlev; h++) {
+    for (int par = 0; par < S.lev_cnt[h]; par++) {
+      int ch = (par << 5) + lane;
+      Node c = ch < S.lev_cnt[h - 1] ? S.tree[S.lev_off[h - 1] + ch] : empty_node(0x7fffffff);
+      warp_min(c);
+      if (lane == 0) S.tree[S.lev_off[h] + par] = c;
+    }
+    __syncwarp();
+  }
+}
+
+// ---------------------------------------------------------------- queue
+
+// addEventToQueue (src/EDMD.c:2144) in key form.  `cls_direct` is 2 for a
+// schedule from an event handler and 0 for the re-add done by a wrap.
+__device__ void schedule(const SysDev& S, SysState& R, int e, double T, int32_t j, uint32_t ca,
+                         uint64_t cls_direct, int lane) {
+  const Box& B = S.B;
+  Ev ev;
+  ev.t = T; ev.j = j; ev.ca = ca;
+  double dt = T - R.P;
+  if (dt < B.dtP) {
+    ev.b = (uint32_t)R.k; ev.tie = (cls_direct << 62) | R.C; ev.st = ST_QUEUED;
+  } else if (dt >= B.dtPN) {
+    ev.b = BINF; ev.tie = R.C; ev.st = ST_OVF;
+    if (lane == 0) {
+      S.on[e] = R.ovf; S.op[e] = NIL;
+      if (R.ovf != NIL) S.op[R.ovf] = e;
+    }
+    R.ovf = e;
+  } else {
+    int d = (int)(dt / B.dtP);
+    ev.b = (uint32_t)(R.k + (uint64_t)d); ev.tie = (1ull << 62) | (TIE_MAX - R.C); ev.st = ST_QUEUED;
+  }
+  R.C++;
+  if (lane == 0) S.ev[e] = ev;
+  __syncwarp();
+}
+
+// removeEventFromQueue (src/EDMD.c:2209) in key form
+__device__ void unqueue(const SysDev& S, SysState& R, int e, int lane) {
+  uint32_t st = S.ev[e].st;
+  if (st == ST_OVF) {
+    int p = S.op[e], n = S.on[e];
+    if (lane == 0) {
+      if (p != NIL) S.on[p] = n;
+      if (n != NIL) S.op[n] = p;
+    }
+    if (p == NIL) R.ovf = n;
+  }
+  if (lane == 0) S.ev[e].st = ST_NONE;
+  __syncwarp();
+}
+
+// the overflow bucket is redistributed when the calendar wraps
+// (addNextPaulEvent src/EDMD.c:2287-2300)
+__device__ void do_wrap(const SysDev& S, SysState& R, int lane) {
+  const int N = S.B.N;
+  int e = R.ovf;
+  R.ovf = NIL;
+  __syncwarp();
+  while (e != NIL) {
+    int n = S.on[e];
+    double T = S.ev[e].t;
+    int32_t j = S.ev[e].j;
+    uint32_t ca = S.ev[e].ca;
+    schedule(S, R, e, T, j, ca, 0ull, lane);
+    __syncwarp();
+    int leaf = e < 2 * N ? (e < N ? e : e - N) : N + (e - 2 * N);
+    leaf_update(S, leaf, lane);
+    e = n;
+  }
+}
+
+// ---------------------------------------------------------------- prediction
+
+struct Pred { double dt; int32_t partner; uint32_t ca; };
+
+__device__ __forceinline__ void grow_fly(const SysDev& S, Disk& p, int i, double t, bool grow) {
+  double dt = t - p.tl;
+  free_fly(S.B, p, t);
+  if (grow) p.rad += dt * S.vr[i];
+}
+
+__device__ __forceinline__ double pair_time(const SysDev& S, const Disk& A, int a, const Disk& P,
+                                            int p, double t, bool grow, bool* ovl) {
+  if (grow) return coll_time_grow(S.B, A, S.vr[a], P, S.vr[p], t, ovl);
+  return coll_time_normal(S.B, A, P, t, ovl);
+}
+
+__device__ __forceinline__ void best_merge(double& bd, int& bo, int& bp, uint32_t& bc,
+                                           double d, int o, int p, uint32_t c) {
+  if (d < bd || (d == bd && o < bo)) { bd = d; bo = o; bp = p; bc = c; }
+}
+
+// collisionEventNormal / Grow (src/EDMD.c:2829 / 3104) for disks a0 and a1
+// (a1 may be -1): scan the 3x3 neighbour cells, dy outer and dx inner, list
+// order, keep the first strict minimum.  Lanes 0..8 own a0's cells and lanes
+// 16..24 own a1's; the candidates are then packed over the whole warp.
+__device__ void predict2(const SysDev& S, SysState& R, int a0, int a1, Pred& r0, Pred& r1,
+                         int lane, WarpSmem* sm, bool* ovl, int* ovl_a, int* ovl_b) {
+  const Box& B = S.B;
+  const bool grow = R.grow != 0;
+  const double dinit = grow ? 10000000 : NEVER;
+  const int g = lane >> 4, q = lane & 15;
+  const int a = g ? a1 : a0;
+  int cnt = 0;
+  int32_t* reg = sm->reg + lane * MAXC;
+  if (a >= 0 && q < 9) {
+    int X = S.cx[a], Y = S.cy[a];
+    int cell = pbc_cy(B, Y + q / 3 - 1) * B.Nxc + pbc_cx(B, X + q % 3 - 1);
+    int p = S.head[cell];
+    while (p != NIL) {
+      if (p != a) { if (cnt < MAXC) reg[cnt] = p; cnt++; }
+      p = S.d[p].nxt;
+    }
+  }
+  bool spill = __any_sync(FULL, cnt > MAXC);
+  Disk A0 = S.d[a0];
+  Disk A1 = a1 >= 0 ? S.d[a1] : A0;
+  double bd0 = dinit, bd1 = dinit;
+  int bo0 = -1, bo1 = -1, bp0 = 0, bp1 = 0;
+  uint32_t bc0 = 0, bc1 = 0;
+  bool lovl = false;
+  int la = -1, lb = -1;
+  int tot;
+  if (!spill) {
+    int incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 16; o <<= 1) {
+      int v = __shfl_up_sync(FULL, incl, o, 16);
+      if (q >= o) incl += v;
+    }
+    int excl = incl - cnt;
+    int tot0 = __shfl_sync(FULL, incl, 15);
+    int tot1 = __shfl_sync(FULL, incl, 31);
+    int base = g ? tot0 : 0;
+    for (int k = 0; k < cnt; k++) {
+      sm->comp[base + excl + k] = reg[k];
+      sm->ord[base + excl + k] = (int16_t)(q * MAXC + k);
+    }
+    __syncwarp();
+    tot = tot0 + tot1;
+    for (int f = lane; f < tot; f += 32) {
+      int p = sm->comp[f];
+      int o = sm->ord[f];
+      Disk P = S.d[p];
+      bool g1 = f >= tot0;
+      bool ov = false;
+      double d = pair_time(S, g1 ? A1 : A0, g1 ? a1 : a0, P, p, R.t, grow, &ov);
+      if (ov) { lovl = true; la = g1 ? a1 : a0; lb = p; }
+      if (g1) best_merge(bd1, bo1, bp1, bc1, d, o, p, P.coll);
+      else best_merge(bd0, bo0, bp0, bc0, d, o, p, P.coll);
+    }
+    __syncwarp();
+  } else {
+    // a cell list longer than MAXC: every lane walks its own list
+    tot = 0;
+    if (a >= 0 && q < 9) {
+      const Disk& AA = g ? A1 : A0;
+      int X = S.cx[a], Y = S.cy[a];
+      int cell = pbc_cy(B, Y + q / 3 - 1) * B.Nxc + pbc_cx(B, X + q % 3 - 1);
+      int p = S.head[cell];
+      int k = 0;
+      while (p != NIL) {
+        Disk P = S.d[p];
+        if (p != a) {
+          bool ov = false;
+          double d = pair_time(S, AA, a, P, p, R.t, grow, &ov);
+          if (ov) { lovl = true; la = a; lb = p; }
+          if (g) best_merge(bd1, bo1, bp1, bc1, d, q * 4096 + k, p, P.coll);
+          else best_merge(bd0, bo0, bp0, bc0, d, q * 4096 + k, p, P.coll);
+          k++;
+        }
+        p = P.nxt;
+      }
+      tot = k;
+    }
+    for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(FULL, tot, o);
+  }
+  // lexicographic (dt, scan order) minimum over the warp
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    double d = __shfl_xor_sync(FULL, bd0, o); int oo = __shfl_xor_sync(FULL, bo0, o);
+    int pp = __shfl_xor_sync(FULL, bp0, o); uint32_t cc = __shfl_xor_sync(FULL, bc0, o);
+    best_merge(bd0, bo0, bp0, bc0, d, oo, pp, cc);
+    d = __shfl_xor_sync(FULL, bd1, o); oo = __shfl_xor_sync(FULL, bo1, o);
+    pp = __shfl_xor_sync(FULL, bp1, o); cc = __shfl_xor_sync(FULL, bc1, o);
+    best_merge(bd1, bo1, bp1, bc1, d, oo, pp, cc);
+  }
+  if (bo0 < 0) bc0 = S.d[0].coll;   // no partner: partner 0 (src/EDMD.c:2830)
+  if (bo1 < 0) bc1 = S.d[0].coll;
+  r0.dt = bd0; r0.partner = bp0; r0.ca = bc0;
+  r1.dt = bd1; r1.partner = bp1; r1.ca = bc1;
+  R.npair += (uint64_t)tot;
+  R.npred += (a1 >= 0) ? 2 : 1;
+  unsigned m = __ballot_sync(FULL, lovl);
+  if (m) {
+    int src = __ffs(m) - 1;
+    *ovl = true;
+    *ovl_a = __shfl_sync(FULL, la, src);
+    *ovl_b = __shfl_sync(FULL, lb, src);
+  }
+}
+
+// ---------------------------------------------------------------- handlers
+
+
+// sequential sum over disks, in index order, identical in all lanes
+template <class F>
+__device__ __forceinline__ void seq_sums(const SysDev& S, int lane, int nval, double* out, F f) {
+  const int N = S.B.N;
+  for (int k = 0; k < nval; k++) out[k] = 0;
+  for (int base = 0; base < N; base += 32) {
+    double v[4] = {0, 0, 0, 0};
+    int i = base + lane;
+    if (i < N) f(i, v);
+    int lim = min(32, N - base);
+    for (int s = 0; s < lim; s++)
+      for (int k = 0; k < nval; k++) out[k] += __shfl_sync(FULL, v[k], s);
+  }
+}
+
+// physicalQ (src/EDMD.c:5968-6013): px, py, E
+__device__ void physical_q(const SysDev& S, int lane, double* E, double* px, double* py) {
+  double o[3];
+  seq_sums(S, lane, 3, o, [&](int i, double* v) {
+    Disk p = S.d[i];
+    v[0] = p.vx * p.m;
+    v[1] = p.vy * p.m;
+    double vx = p.vx;
+    v[2] = 0.5 * p.m * (vx * vx + p.vy * p.vy);
+  });
+  *px = o[0]; *py = o[1]; *E = o[2];
+}
+
+// takeAThermo + saveThermo (src/EDMD.c:4679, 5232-5697) with Nthermo = 1
+__device__ void do_thermo(const SysDev& S, SysState& R, int lane) {
+  const int N = S.B.N;
+  double E, px, py;
+  physical_q(S, lane, &E, &px, &py);
+  double area = S.B.Lx * S.B.Ly;
+  double dT = R.t - R.lastThermo;
+  R.lastThermo = R.t;
+  double e4[4];
+  seq_sums(S, lane, 4, e4, [&](int i, double* v) {
+    Disk p = S.d[i];
+    v[0] = p.m * p.vx * p.vx; v[1] = p.m * p.vy * p.vy;
+    v[2] = p.m * p.vx * p.vy; v[3] = p.m * p.vy * p.vx;
+  });
+  double row[9];
+  row[0] = R.t; row[1] = (double)R.ncol; row[2] = E / N;
+  row[4] = -1 * R.collT[0] / (area * dT) + e4[0] / area;
+  row[5] = -1 * R.collT[1] / (area * dT) + e4[1] / area;
+  row[6] = -1 * R.collT[2] / (area * dT) + e4[2] / area;
+  row[7] = -1 * R.collT[3] / (area * dT) + e4[3] / area;
+  row[3] = (-1 / (dT)) * (R.collT[0] + R.collT[1]) / (2 * area) + E / area;
+  R.collT[0] = R.collT[1] = R.collT[2] = R.collT[3] = 0;
+  double vxa;
+  seq_sums(S, lane, 1, &vxa, [&](int i, double* v) { v[0] = S.d[i].vx; });
+  vxa /= N;
+  double v24[2];
+  seq_sums(S, lane, 2, v24, [&](int i, double* v) {
+    double d = S.d[i].vx - vxa; double d2 = d * d; v[0] = d2; v[1] = d2 * d2;
+  });
+  v24[0] /= N; v24[1] /= N;
+  row[8] = (v24[0] > 0.0) ? v24[1] / (3.0 * v24[0] * v24[0]) - 1.0 : 0.0;
+  if (R.t != 0) {
+    if (R.nrows < S.rows_cap && lane == 0)
+      for (int k = 0; k < 9; k++) S.rows[(int64_t)R.nrows * 9 + k] = row[k];
+    R.nrows++;
+  }
+}
+
+// stopGrow (src/EDMD.c:4740-4800)
+__device__ void do_growstop(const SysDev& S, SysState& R, int lane, WarpSmem* sm,
+                            bool* ovl, int* oa, int* ob) {
+  const int N = S.B.N;
+  for (int i = lane; i < N; i += 32) {
+    Disk p = S.d[i];
+    grow_fly(S, p, i, R.t, true);
+    p.coll = 0;
+    S.d[i] = p;
+    S.crossX[i] = 0; S.crossY[i] = 0;
+  }
+  R.ncol = 0; R.ncross = 0;
+  R.grow = 0;
+  __syncwarp();
+  // normalizePhysicalQ (src/EDMD.c:5723-5764)
+  double E, px, py;
+  physical_q(S, lane, &E, &px, &py);
+  for (int i = lane; i < N; i += 32) {
+    Disk p = S.d[i];
+    p.vx -= px / (N * p.m);
+    p.vy -= py / (N * p.m);
+    S.d[i] = p;
+  }
+  __syncwarp();
+  physical_q(S, lane, &E, &px, &py);
+  for (int i = lane; i < N; i += 32) {
+    Disk p = S.d[i];
+    p.vx /= sqrt(E / N / S.Einit);
+    p.vy /= sqrt(E / N / S.Einit);
+    S.d[i] = p;
+  }
+  __syncwarp();
+  for (int i = 0; i < N; i++) {
+    uint32_t c = S.d[i].coll + 1;
+    if (lane == 0) S.d[i].coll = c;
+    __syncwarp();
+    unqueue(S, R, N + i, lane);
+    Pred r0, r1;
+    predict2(S, R, i, -1, r0, r1, lane, sm, ovl, oa, ob);
+    schedule(S, R, N + i, R.t + r0.dt, r0.partner, r0.ca, 2ull, lane);
+    unqueue(S, R, i, lane);
+    int dir;
+    Disk p = S.d[i];
+    double tc = crossing_time(S.B, p, S.cx[i], S.cy[i], R.t, &dir);
+    schedule(S, R, i, tc, dir, 0, 2ull, lane);
+    __syncwarp();
+  }
+  tree_rebuild(S, lane);
+}
+
+// ---------------------------------------------------------------- run loop
+
+__device__ void run_system(const SysDev& S, const RunArgs& A, int lane, WarpSmem* sm) {
+  const Box& B = S.B;
+  const int N = B.N;
+  SysState R = *S.st;
+  if (R.status != EDMD_OK) return;
+  const int root = S.lev_off[S.nlev - 1];
+  int64_t logged = 0, nev = 0;
+  int stop = 0, status = EDMD_OK;
+  bool ovl = false;
+  int oa = -1, ob = -1;
+  for (;;) {
+    if (!(R.t <= S.tmax)) { stop = EDMD_STOP_TMAX; break; }
+    if (logged >= A.max_coll) { stop = EDMD_STOP_COLL; break; }
+    if (nev >= A.max_events) { status = EDMD_ERR_BUDGET; break; }
+    Node r;
+    int guard = 0;
+    for (;;) {
+      r = S.tree[root];
+      if (r.b == BINF || (uint64_t)r.b >= R.next_wrap) {
+        if (r.b == BINF && R.ovf == NIL) { status = EDMD_ERR_BUDGET; break; }
+        while (R.k < R.next_wrap) { R.P += B.dtP; R.k++; }
+        do_wrap(S, R, lane);
+        R.next_wrap += (uint64_t)N;
+        if (++guard > (1 << 20)) { status = EDMD_ERR_BUDGET; break; }
+        continue;
+      }
+      while (R.k < (uint64_t)r.b) { R.P += B.dtP; R.k++; }
+      break;
+    }
+    if (status != EDMD_OK) break;
+    int leaf = r.idx, e;
+    if (leaf < N) {
+      Ev e0 = S.ev[leaf];
+      e = (e0.st == ST_QUEUED && e0.b == r.b && e0.t == r.t && e0.tie == r.tie) ? leaf : N + leaf;
+    } else {
+      e = 2 * N + (leaf - N);
+    }
+    Ev E = S.ev[e];
+    if (E.t >= A.t_stop) { stop = EDMD_STOP_TIME; break; }
+    R.t = E.t;
+    nev++;
+    R.nevents++;
+    if (lane == 0) S.ev[e].st = ST_NONE;
+    __syncwarp();
+    const bool grow = R.grow != 0;
+    if (e >= N && e < 2 * N) {
+      // ---------------- collision (doTheCollisionNormal 3542 / Grow 3465)
+      const int i = e - N, j = E.j;
+      Disk di = S.d[i];
+      grow_fly(S, di, i, R.t, grow);
+      Disk dj = S.d[j];
+      if (E.ca != dj.coll) {
+        if (lane == 0) S.d[i] = di;
+        __syncwarp();
+        R.nstale++;
+        Pred r0, r1;
+        predict2(S, R, i, -1, r0, r1, lane, sm, &ovl, &oa, &ob);
+        schedule(S, R, N + i, R.t + r0.dt, r0.partner, r0.ca, 2ull, lane);
+        __syncwarp();
+        leaf_update(S, i, lane);
+      } else {
+        const int ci = S.cy[i] * B.Nxc + S.cx[i];
+        const int cj = S.cy[j] * B.Nxc + S.cx[j];
+        if ((A.flags & EDMD_F_TRACE) && S.trace && (int64_t)R.ntrace < S.trace_cap && lane == 0) {
+          edmd_collision* tr = (edmd_collision*)S.trace + R.ntrace;
+          tr->i = i; tr->j = j; tr->cell_i = ci; tr->cell_j = cj; tr->t = R.t;
+        }
+        R.ntrace++;
+        if (!(A.flags & EDMD_F_COUNT_NORMAL) || !grow) logged++;
+        R.ncol++;
+        R.ncol_total++;
+        grow_fly(S, dj, j, R.t, grow);
+        di.coll++;
+        dj.coll++;
+        double dx = dj.x - di.x, dy = dj.y - di.y;
+        double dvx = dj.vx - di.vx, dvy = dj.vy - di.vy;
+        if (!grow) {   // elastic branch src/EDMD.c:3802-3827
+          double invMass = 1 / (di.m + dj.m);
+          pbc(B, dx, dy);
+          double collKernel = invMass * (1 + S.res) * (dx * dvx + dy * dvy);
+          double distSquared = 4 * di.rad * dj.rad;
+          double f = collKernel / distSquared;
+          double ct = di.m * dj.m * f;
+          R.collT[0] += ct * dx * dx;
+          R.collT[1] += ct * dy * dy;
+          R.collT[2] += ct * dx * dy;
+          R.collT[3] += ct * dy * dx;
+          di.vx += f * dj.m * dx;
+          di.vy += f * dj.m * dy;
+          dj.vx -= f * di.m * dx;
+          dj.vy -= f * di.m * dy;
+        } else {       // growth rule src/EDMD.c:3479-3520
+          double delta = 0.1 * 0;
+          double res = 0.75 * 0 + 1;
+          double dvr = S.vr[i] + S.vr[j];
+          pbc(B, dx, dy);
+          double dist = sqrt(dx * dx + dy * dy);
+          double dxr = dx / dist, dyr = dy / dist;
+          double invMass = 1 / (di.m + dj.m);
+          double collKernel = invMass * (1 + res) * (dxr * dvx + dyr * dvy - dvr);
+          di.vx += collKernel * dj.m * dxr - 2 * dj.m * invMass * delta * dxr;
+          di.vy += collKernel * dj.m * dyr - 2 * dj.m * invMass * delta * dyr;
+          dj.vx -= collKernel * di.m * dxr - 2 * di.m * invMass * delta * dxr;
+          dj.vy -= collKernel * di.m * dyr - 2 * di.m * invMass * delta * dyr;
+        }
+        if (lane == 0) { S.d[i] = di; S.d[j] = dj; }
+        __syncwarp();
+        unqueue(S, R, i, lane);
+        unqueue(S, R, j, lane);
+        int diri, dirj;
+        double tci = crossing_time(B, di, S.cx[i], S.cy[i], R.t, &diri);
+        double tcj = crossing_time(B, dj, S.cx[j], S.cy[j], R.t, &dirj);
+        schedule(S, R, i, tci, diri, 0, 2ull, lane);
+        schedule(S, R, j, tcj, dirj, 0, 2ull, lane);
+        unqueue(S, R, N + j, lane);
+        Pred r0, r1;
+        predict2(S, R, i, j, r0, r1, lane, sm, &ovl, &oa, &ob);
+        schedule(S, R, N + i, R.t + r0.dt, r0.partner, r0.ca, 2ull, lane);
+        schedule(S, R, N + j, R.t + r1.dt, r1.partner, r1.ca, 2ull, lane);
+        __syncwarp();
+        leaf_update(S, i, lane);
+        leaf_update(S, j, lane);
+      }
+    } else if (e < N) {
+      // ---------------- cell crossing (doTheCrossing 2501)
+      const int i = e;
+      R.ncross++;
+      Disk di = S.d[i];
+      grow_fly(S, di, i, R.t, grow);
+      int cx = S.cx[i], cy = S.cy[i];
+      if (lane == 0) {
+        int pv = S.prv[i], nx = di.nxt;
+        if (pv == NIL) S.head[cy * B.Nxc + cx] = nx;
+        else S.d[pv].nxt = nx;
+        if (nx != NIL) S.prv[nx] = pv;
+      }
+      int dx = 0, dy = 0;
+      switch (E.j) {
+        case 1: if (cx - 1 == -1) { cx = B.Nxc - 1; dx = -1; } else cx -= 1; break;
+        case 2: if (cx + 1 == B.Nxc) { cx = 0; dx = 1; } else cx += 1; break;
+        case 3: if (cy - 1 == -1) { cy = B.Nyc - 1; dy = -1; } else cy -= 1; break;
+        case 4: if (cy + 1 == B.Nyc) { cy = 0; dy = 1; } else cy += 1; break;
+      }
+      __syncwarp();
+      if (lane == 0) {
+        int c = cy * B.Nxc + cx;
+        int h = S.head[c];
+        S.cx[i] = cx; S.cy[i] = cy;
+        if (dx) S.crossX[i] += dx;
+        if (dy) S.crossY[i] += dy;
+        S.prv[i] = NIL;
+        di.nxt = h;
+        S.d[i] = di;
+        S.head[c] = i;
+        if (h != NIL) S.prv[h] = i;
+      }
+      __syncwarp();
+      int dir;
+      double tc = crossing_time(B, di, cx, cy, R.t, &dir);
+      schedule(S, R, i, tc, dir, 0, 2ull, lane);
+      unqueue(S, R, N + i, lane);
+      __syncwarp();
+      Pred r0, r1;
+      predict2(S, R, i, -1, r0, r1, lane, sm, &ovl, &oa, &ob);
+      schedule(S, R, N + i, R.t + r0.dt, r0.partner, r0.ca, 2ull, lane);
+      __syncwarp();
+      leaf_update(S, i, lane);
+    } else if (e == 2 * N + SP_SCREEN) {
+      // ---------------- screenshot (takeAScreenshot 4657): free-fly everything
+      for (int i = lane; i < N; i += 32) {
+        Disk p = S.d[i];
+        grow_fly(S, p, i, R.t, grow);
+        S.d[i] = p;
+      }
+      __syncwarp();
+      schedule(S, R, e, R.t + S.dtime, 0, 0, 2ull, lane);
+      __syncwarp();
+      leaf_update(S, N + SP_SCREEN, lane);
+      if (A.flags & EDMD_F_STOP_AT_SCREEN) { stop = EDMD_STOP_SCREEN; }
+    } else if (e == 2 * N + SP_THERMO) {
+      do_thermo(S, R, lane);
+      schedule(S, R, e, R.t + S.dtimeTh, 0, 0, 2ull, lane);
+      __syncwarp();
+      leaf_update(S, N + SP_THERMO, lane);
+    } else {
+      do_growstop(S, R, lane, sm, &ovl, &oa, &ob);
+      if (A.flags & EDMD_F_STOP_AT_GROW) stop = EDMD_STOP_GROW;
+    }
+    if (ovl) { status = EDMD_ERR_OVERLAP; break; }
+    if (stop) break;
+  }
+  R.stop_reason = stop;
+  R.status = status;
+  if (ovl) { R.err_a = oa; R.err_b = ob; }
+  if (lane == 0) *S.st = R;
+  __syncwarp();
+}
+
+__global__ void __launch_bounds__(32 * WARPS_PER_BLOCK)
+k_run(const SysDev* __restrict__ sys, RunArgs A) {
+  __shared__ WarpSmem smem[WARPS_PER_BLOCK];
+  const int lane = threadIdx.x & 31;
+  const int w = threadIdx.x >> 5;
+  for (;;) {
+    int s = 0;
+    if (lane == 0) s = atomicAdd(A.work, 1);
+    s = __shfl_sync(FULL, s, 0);
+    if (s >= A.nsys) break;
+    SysDev S = sys[s];
+    run_system(S, A, lane, &smem[w]);
+  }
+}
+
+// ---------------------------------------------------------------- init kernels
+
+// initial predictions of eventListInit (src/EDMD.c:2007-2012): all disks are
+// current at t = 0 and the calendar sits at bucket 0, so every key is known
+// without serialising: the k-th scheduled event has counter k.
+__global__ void k_init_events(const SysDev* __restrict__ sys, int s) {
+  const SysDev S = sys[s];
+  const Box& B = S.B;
+  const int N = B.N;
+  const bool grow = S.st->grow != 0;
+  const int nspec = grow ? 3 : 2;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  auto key = [&](Ev& ev, double T, uint64_t C) {
+    double dt = T - 0.0;
+    if (dt < B.dtP) { ev.b = 0; ev.tie = (2ull << 62) | C; ev.st = ST_QUEUED; }
+    else if (dt >= B.dtPN) { ev.b = BINF; ev.tie = C; ev.st = ST_OVF; }
+    else { int d = (int)(dt / B.dtP); ev.b = (uint32_t)d; ev.tie = (1ull << 62) | (TIE_MAX - C); ev.st = ST_QUEUED; }
+  };
+  if (i < N) {
+    Disk A = S.d[i];
+    int dir;
+    Ev ec; ec.t = crossing_time(B, A, S.cx[i], S.cy[i], 0.0, &dir); ec.j = dir; ec.ca = 0;
+    key(ec, ec.t, (uint64_t)nspec + 2ull * i);
+    S.ev[i] = ec;
+    double bd = grow ? 10000000 : NEVER;
+    int bp = 0;
+    bool ov = false;
+    int X = S.cx[i], Y = S.cy[i];
+    uint64_t np = 0;
+    for (int q = 0; q < 9; q++) {
+      int cell = pbc_cy(B, Y + q / 3 - 1) * B.Nxc + pbc_cx(B, X + q % 3 - 1);
+      for (int p = S.head[cell]; p != NIL; p = S.d[p].nxt) {
+        if (p == i) continue;
+        Disk P = S.d[p];
+        double d = grow ? coll_time_grow(B, A, S.vr[i], P, S.vr[p], 0.0, &ov)
+                        : coll_time_normal(B, A, P, 0.0, &ov);
+        np++;
+        if (bd > d) { bd = d; bp = p; }
+      }
+    }
+    Ev el; el.t = 0.0 + bd; el.j = bp; el.ca = 0;
+    key(el, el.t, (uint64_t)nspec + 2ull * i + 1);
+    S.ev[N + i] = el;
+    atomicAdd((unsigned long long*)&S.st->npair, (unsigned long long)np);
+    if (ov) { S.st->status = EDMD_ERR_OVERLAP; S.st->err_a = i; }
+  } else if (i == N) {
+    // thermo, [growth stop], screenshot in eventListInit order
+    Ev e; e.j = 0; e.ca = 0;
+    e.t = S.st->lastThermo;   // holds first_thermo + 1e-9 on entry
+    key(e, e.t, 0);
+    S.ev[2 * N + SP_THERMO] = e;
+    uint64_t C = 1;
+    Ev g; g.j = 0; g.ca = 0; g.t = S.st->collT[0];  // holds t_growstop on entry
+    if (grow) { key(g, g.t, C); C++; } else { g.st = ST_NONE; g.b = BINF; g.tie = 0; }
+    S.ev[2 * N + SP_GROW] = g;
+    Ev sc; sc.j = 0; sc.ca = 0; sc.t = S.st->collT[1];  // holds first_screen on entry
+    key(sc, sc.t, C);
+    S.ev[2 * N + SP_SCREEN] = sc;
+  }
+}
+
+// link the initial overflow bucket in LIFO order and finish the scalar state
+__global__ void k_init_finish(const SysDev* __restrict__ sys, int s) {
+  const SysDev S = sys[s];
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const int N = S.B.N;
+  const bool grow = S.st->grow != 0;
+  int head = NIL;
+  auto push = [&](int e) {
+    if (S.ev[e].st != ST_OVF) return;
+    S.on[e] = head; S.op[e] = NIL;
+    if (head != NIL) S.op[head] = e;
+    head = e;
+  };
+  push(2 * N + SP_THERMO);
+  if (grow) push(2 * N + SP_GROW);
+  push(2 * N + SP_SCREEN);
+  for (int i = 0; i < N; i++) { push(i); push(N + i); }
+  SysState& R = *S.st;
+  R.ovf = head;
+  R.C = (uint64_t)(grow ? 3 : 2) + 2ull * N;
+  R.npred = (uint64_t)N;
+  R.lastThermo = 0;
+  R.collT[0] = R.collT[1] = 0;
+}
+
+__global__ void k_tree_build(const SysDev* __restrict__ sys, int s) {
+  const SysDev S = sys[s];
+  tree_rebuild(S, threadIdx.x & 31);
+}
+
+__global__ void k_sync(const SysDev* __restrict__ sys, int nsys) {
+  int s = blockIdx.x;
+  if (s >= nsys) return;
+  const SysDev S = sys[s];
+  const double t = S.st->t;
+  const bool grow = S.st->grow != 0;
+  for (int i = threadIdx.x; i < S.B.N; i += blockDim.x) {
+    Disk p = S.d[i];
+    grow_fly(S, p, i, t, grow);
+    S.d[i] = p;
+  }
+}
+
+}  // namespace
+
+// ==================================================================== C ABI
+
+struct edmd_ctx {
+  int nsys = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  std::vector<SysDev> hs;
+  SysDev* ds = nullptr;
+  char* pool = nullptr;
+  int32_t* work = nullptr;
+  std::string err;
+};
+
+static int set_err(edmd_ctx* c, int code, const std::string& m) {
+  if (c) c->err = m;
+  return code;
+}
+#define CK(call)                                                                         \
+  do {                                                                                   \
+    cudaError_t _e = (call);                                                             \
+    if (_e != cudaSuccess) return set_err(ctx, EDMD_ERR_CUDA, std::string(#call ": ") +   \
+                                                                  cudaGetErrorString(_e)); \
+  } while (0)
+
+static size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+extern "C" int edmd_device_info(char* name, int32_t cap, int32_t* sm_count) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) return EDMD_ERR_NODEV;
+  cudaDeviceProp p;
+  if (cudaGetDeviceProperties(&p, 0) != cudaSuccess) return EDMD_ERR_CUDA;
+  if (name && cap > 0) { strncpy(name, p.name, cap - 1); name[cap - 1] = 0; }
+  if (sm_count) *sm_count = p.multiProcessorCount;
+  return EDMD_OK;
+}
+
+extern "C" int edmd_create(int32_t nsys, const edmd_system_desc* desc, const double* x,
+                           const double* y, const double* vx, const double* vy,
+                           const double* rad, const double* m, const double* vr,
+                           int64_t trace_cap, edmd_ctx** out) {
+  if (!out || nsys <= 0 || !desc || !x || !y || !vx || !vy || !rad || !m) return EDMD_ERR_ARG;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return EDMD_ERR_NODEV;
+  edmd_ctx* ctx = new edmd_ctx();
+  ctx->nsys = nsys;
+  ctx->hs.resize(nsys);
+  const int rows_cap = 1024;
+  // ---- layout
+  std::vector<size_t> off(nsys);
+  size_t total = 0;
+  std::vector<std::vector<int>> lev_cnt(nsys);
+  for (int s = 0; s < nsys; s++) {
+    const edmd_system_desc& D = desc[s];
+    if (D.N < 2 || !(D.Lx > 0) || !(D.Ly > 0)) { delete ctx; return EDMD_ERR_ARG; }
+    SysDev& S = ctx->hs[s];
+    memset(&S, 0, sizeof(S));
+    Box& B = S.B;
+    B.N = D.N; B.Lx = D.Lx; B.Ly = D.Ly;
+    B.hLx = D.Lx / 2; B.hLy = D.Ly / 2;                      // boxConstantHelper 679-714
+    B.Nyc = (int)(B.hLy); B.Nxc = (int)(B.hLx);
+    if (B.Nxc < 1 || B.Nyc < 1) { delete ctx; return EDMD_ERR_ARG; }
+    B.cxs = D.Lx / B.Nxc; B.cys = D.Ly / B.Nyc;
+    B.cxf = 1 / B.cxs; B.cyf = 1 / B.cys;
+    B.dtP = 5.0 / (double)D.N;
+    B.dtPN = B.dtP * D.N;
+    S.res = D.res; S.Einit = D.Einit; S.dtime = D.dtime; S.dtimeTh = D.dtime_thermo; S.tmax = D.tmax;
+    S.L = D.N + NSPECIAL;
+    int c = S.L, h = 0;
+    lev_cnt[s].push_back(c);
+    while (c > 1) { c = (c + 31) / 32; lev_cnt[s].push_back(c); }
+    S.nlev = (int)lev_cnt[s].size();
+    if (S.nlev > MAXLEV) { delete ctx; return EDMD_ERR_ARG; }
+    size_t nodes = 0;
+    for (h = 0; h < S.nlev; h++) { S.lev_off[h] = (int)nodes; S.lev_cnt[h] = lev_cnt[s][h]; nodes += lev_cnt[s][h]; }
+    size_t N = D.N, E = 2 * N + NSPECIAL, C = (size_t)B.Nxc * B.Nyc;
+    size_t sz = 0;
+    sz += align_up(sizeof(SysState), 256);
+    sz += align_up(N * sizeof(Disk), 256);
+    sz += align_up(N * 8, 256);            // vr
+    sz += 5 * align_up(N * 4, 256);        // cx cy prv crossX crossY
+    sz += align_up(C * 4, 256);            // head
+    sz += align_up(E * sizeof(Ev), 256);
+    sz += 2 * align_up(E * 4, 256);        // on op
+    sz += align_up(nodes * sizeof(Node), 256);
+    sz += align_up((size_t)trace_cap * sizeof(edmd_collision), 256);
+    sz += align_up((size_t)rows_cap * 9 * 8, 256);
+    off[s] = total;
+    total += sz;
+  }
+  cudaError_t ce = cudaMalloc(&ctx->pool, total);
+  if (ce != cudaSuccess) { std::string m2 = cudaGetErrorString(ce); delete ctx; (void)m2; return EDMD_ERR_CUDA; }
+  if (cudaMalloc(&ctx->work, sizeof(int32_t)) != cudaSuccess) { cudaFree(ctx->pool); delete ctx; return EDMD_ERR_CUDA; }
+  if (cudaMalloc(&ctx->ds, nsys * sizeof(SysDev)) != cudaSuccess) { cudaFree(ctx->pool); cudaFree(ctx->work); delete ctx; return EDMD_ERR_CUDA; }
+  CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+  CK(cudaEventCreate(&ctx->e0));
+  CK(cudaEventCreate(&ctx->e1));
+  // ---- host-side staging of each system: cell lists (cellListInit src/EDMD.c:1906
+  // -> addToCell 2053: index order, push-front) and initial records
+  size_t base_disk = 0;
+  for (int s = 0; s < nsys; s++) {
+    SysDev& S = ctx->hs[s];
+    const edmd_system_desc& D = desc[s];
+    const Box& B = S.B;
+    size_t N = D.N, E = 2 * N + NSPECIAL, C = (size_t)B.Nxc * B.Nyc;
+    char* p = ctx->pool + off[s];
+    auto take = [&](size_t bytes) { char* r = p; p += align_up(bytes, 256); return r; };
+    S.st = (SysState*)take(sizeof(SysState));
+    S.d = (Disk*)take(N * sizeof(Disk));
+    S.vr = (double*)take(N * 8);
+    S.cx = (int32_t*)take(N * 4); S.cy = (int32_t*)take(N * 4); S.prv = (int32_t*)take(N * 4);
+    S.crossX = (int32_t*)take(N * 4); S.crossY = (int32_t*)take(N * 4);
+    S.head = (int32_t*)take(C * 4);
+    S.ev = (Ev*)take(E * sizeof(Ev));
+    S.on = (int32_t*)take(E * 4); S.op = (int32_t*)take(E * 4);
+    size_t nodes = 0;
+    for (int h = 0; h < S.nlev; h++) nodes += S.lev_cnt[h];
+    S.tree = (Node*)take(nodes * sizeof(Node));
+    S.trace = trace_cap > 0 ? (void*)take((size_t)trace_cap * sizeof(edmd_collision)) : nullptr;
+    S.trace_cap = trace_cap;
+    S.rows = (double*)take((size_t)rows_cap * 9 * 8);
+    S.rows_cap = rows_cap;
+    std::vector<Disk> hd(N);
+    std::vector<int32_t> hcx(N), hcy(N), hprv(N), hhead(C, NIL), zero(N, 0);
+    std::vector<double> hvr(N, 0.0);
+    for (size_t i = 0; i < N; i++) {
+      size_t g = base_disk + i;
+      if (!(x[g] >= 0 && x[g] < D.Lx && y[g] >= 0 && y[g] < D.Ly)) {
+        ctx->err = "position outside the box";
+        edmd_destroy(ctx);
+        return EDMD_ERR_ARG;
+      }
+      Disk& q = hd[i];
+      q.x = x[g]; q.y = y[g]; q.vx = vx[g]; q.vy = vy[g]; q.tl = 0; q.rad = rad[g]; q.m = m[g];
+      q.coll = 0;
+      if (vr) hvr[i] = vr[g];
+      int X = (int)(q.x * B.cxf), Y = (int)(q.y * B.cyf);
+      if (X >= B.Nxc) X = B.Nxc - 1;
+      if (Y >= B.Nyc) Y = B.Nyc - 1;
+      hcx[i] = X; hcy[i] = Y; hprv[i] = NIL;
+      q.nxt = hhead[Y * B.Nxc + X];
+      hhead[Y * B.Nxc + X] = (int32_t)i;
+      if (q.nxt != NIL) hprv[q.nxt] = (int32_t)i;
+    }
+    base_disk += N;
+    SysState st;
+    memset(&st, 0, sizeof(st));
+    st.k = 0; st.next_wrap = N; st.ovf = NIL;
+    st.grow = D.t_growstop > 0 ? 1 : 0;
+    st.lastThermo = D.first_thermo + 0.000000001;   // addEventThermo(firstThermo + 1e-9)
+    st.collT[0] = D.t_growstop;                      // consumed by k_init_events
+    st.collT[1] = D.first_screen;
+    CK(cudaMemcpyAsync(S.st, &st, sizeof(st), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(S.d, hd.data(), N * sizeof(Disk), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(S.vr, hvr.data(), N * 8, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(S.cx, hcx.data(), N * 4, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(S.cy, hcy.data(), N * 4, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(S.prv, hprv.data(), N * 4, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(S.crossX, zero.data(), N * 4, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(S.crossY, zero.data(), N * 4, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(S.head, hhead.data(), C * 4, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));   // staging vectors go out of scope
+  }
+  CK(cudaMemcpyAsync(ctx->ds, ctx->hs.data(), nsys * sizeof(SysDev), cudaMemcpyHostToDevice, ctx->stream));
+  for (int s = 0; s < nsys; s++) {
+    int N = ctx->hs[s].B.N;
+    k_init_events<<<(N + 1 + 127) / 128, 128, 0, ctx->stream>>>(ctx->ds, s);
+    k_init_finish<<<1, 32, 0, ctx->stream>>>(ctx->ds, s);
+    k_tree_build<<<1, 32, 0, ctx->stream>>>(ctx->ds, s);
+  }
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(ctx->stream));
+  for (int s = 0; s < nsys; s++) {
+    int32_t status = 0;
+    CK(cudaMemcpy(&status, &ctx->hs[s].st->status, 4, cudaMemcpyDeviceToHost));
+    if (status != EDMD_OK) {
+      ctx->err = "initial configuration has overlapping disks";
+      *out = ctx;
+      return status;
+    }
+  }
+  *out = ctx;
+  return EDMD_OK;
+}
+
+extern "C" int edmd_advance(edmd_ctx* ctx, int64_t max_coll, double t_stop, uint32_t flags,
+                            int64_t max_events, float* elapsed_ms) {
+  if (!ctx) return EDMD_ERR_ARG;
+  if (max_coll < 0 || max_events <= 0) return set_err(ctx, EDMD_ERR_ARG, "bad advance limits");
+  RunArgs A;
+  A.max_coll = max_coll; A.t_stop = t_stop; A.flags = flags; A.max_events = max_events;
+  A.nsys = ctx->nsys; A.work = ctx->work;
+  CK(cudaMemsetAsync(ctx->work, 0, sizeof(int32_t), ctx->stream));
+  int dev = 0, nsm = 0;
+  CK(cudaGetDevice(&dev));
+  CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  int per_sm = 0;
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_run, 32 * WARPS_PER_BLOCK, 0));
+  int want = (ctx->nsys + WARPS_PER_BLOCK - 1) / WARPS_PER_BLOCK;
+  int grid = per_sm * nsm;
+  if (grid > want) grid = want;
+  if (grid < 1) grid = 1;
+  CK(cudaEventRecord(ctx->e0, ctx->stream));
+  k_run<<<grid, 32 * WARPS_PER_BLOCK, 0, ctx->stream>>>(ctx->ds, A);
+  CK(cudaGetLastError());
+  CK(cudaEventRecord(ctx->e1, ctx->stream));
+  CK(cudaEventSynchronize(ctx->e1));
+  if (elapsed_ms) CK(cudaEventElapsedTime(elapsed_ms, ctx->e0, ctx->e1));
+  int worst = EDMD_OK;
+  for (int s = 0; s < ctx->nsys; s++) {
+    int32_t st[2];
+    CK(cudaMemcpy(st, &ctx->hs[s].st->status, 8, cudaMemcpyDeviceToHost));
+    if (st[0] != EDMD_OK && worst == EDMD_OK) {
+      worst = st[0];
+      char b[128];
+      snprintf(b, sizeof b, "system %d stopped with status %d", s, st[0]);
+      ctx->err = b;
+    }
+  }
+  return worst;
+}
+
+extern "C" int edmd_sync(edmd_ctx* ctx) {
+  if (!ctx) return EDMD_ERR_ARG;
+  k_sync<<<ctx->nsys, 256, 0, ctx->stream>>>(ctx->ds, ctx->nsys);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(ctx->stream));
+  return EDMD_OK;
+}
+
+extern "C" int edmd_get_state(edmd_ctx* ctx, int32_t s, double* x, double* y, double* vx,
+                              double* vy, double* rad, double* m, int32_t* cell, uint32_t* coll) {
+  if (!ctx || s < 0 || s >= ctx->nsys) return EDMD_ERR_ARG;
+  const SysDev& S = ctx->hs[s];
+  int N = S.B.N;
+  std::vector<Disk> hd(N);
+  std::vector<int32_t> hcx(N), hcy(N);
+  CK(cudaMemcpy(hd.data(), S.d, N * sizeof(Disk), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(hcx.data(), S.cx, N * 4, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(hcy.data(), S.cy, N * 4, cudaMemcpyDeviceToHost));
+  for (int i = 0; i < N; i++) {
+    if (x) x[i] = hd[i].x;
+    if (y) y[i] = hd[i].y;
+    if (vx) vx[i] = hd[i].vx;
+    if (vy) vy[i] = hd[i].vy;
+    if (rad) rad[i] = hd[i].rad;
+    if (m) m[i] = hd[i].m;
+    if (cell) cell[i] = hcy[i] * S.B.Nxc + hcx[i];
+    if (coll) coll[i] = hd[i].coll;
+  }
+  return EDMD_OK;
+}
+
+extern "C" int edmd_get_counters(edmd_ctx* ctx, int32_t s, edmd_counters* out) {
+  if (!ctx || s < 0 || s >= ctx->nsys || !out) return EDMD_ERR_ARG;
+  SysState R;
+  CK(cudaMemcpy(&R, ctx->hs[s].st, sizeof(R), cudaMemcpyDeviceToHost));
+  out->ncol = R.ncol; out->ncol_total = R.ncol_total; out->ncross = R.ncross;
+  out->nstale = R.nstale; out->npair = R.npair; out->npred = R.npred; out->nevents = R.nevents;
+  out->t = R.t; out->growing = R.grow; out->stop_reason = R.stop_reason;
+  return EDMD_OK;
+}
+
+extern "C" int edmd_get_virial(edmd_ctx* ctx, int32_t s, double out[4], int32_t reset) {
+  if (!ctx || s < 0 || s >= ctx->nsys || !out) return EDMD_ERR_ARG;
+  SysState* p = ctx->hs[s].st;
+  CK(cudaMemcpy(out, p->collT, 4 * sizeof(double), cudaMemcpyDeviceToHost));
+  if (reset) CK(cudaMemset(p->collT, 0, 4 * sizeof(double)));
+  return EDMD_OK;
+}
+
+extern "C" int edmd_get_thermo(edmd_ctx* ctx, int32_t s, double* rows, int32_t cap, int32_t* n) {
+  if (!ctx || s < 0 || s >= ctx->nsys || !n) return EDMD_ERR_ARG;
+  const SysDev& S = ctx->hs[s];
+  int32_t nr = 0;
+  CK(cudaMemcpy(&nr, &S.st->nrows, 4, cudaMemcpyDeviceToHost));
+  *n = nr;
+  int k = nr < cap ? nr : cap;
+  if (k > S.rows_cap) k = S.rows_cap;
+  if (rows && k > 0) CK(cudaMemcpy(rows, S.rows, (size_t)k * 9 * 8, cudaMemcpyDeviceToHost));
+  return nr > S.rows_cap ? EDMD_ERR_CAPACITY : EDMD_OK;
+}
+
+extern "C" int edmd_get_trace(edmd_ctx* ctx, int32_t s, edmd_collision* out, int64_t cap, int64_t* n) {
+  if (!ctx || s < 0 || s >= ctx->nsys || !n) return EDMD_ERR_ARG;
+  const SysDev& S = ctx->hs[s];
+  uint64_t nt = 0;
+  CK(cudaMemcpy(&nt, &S.st->ntrace, 8, cudaMemcpyDeviceToHost));
+  *n = (int64_t)nt;
+  int64_t k = (int64_t)nt < cap ? (int64_t)nt : cap;
+  if (k > S.trace_cap) k = S.trace_cap;
+  if (out && k > 0) CK(cudaMemcpy(out, S.trace, k * sizeof(edmd_collision), cudaMemcpyDeviceToHost));
+  return (int64_t)nt > S.trace_cap ? EDMD_ERR_CAPACITY : EDMD_OK;
+}
+
+extern "C" int edmd_destroy(edmd_ctx* ctx) {
+  if (!ctx) return EDMD_OK;
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  if (ctx->pool) cudaFree(ctx->pool);
+  if (ctx->work) cudaFree(ctx->work);
+  if (ctx->ds) cudaFree(ctx->ds);
+  if (ctx->e0) cudaEventDestroy(ctx->e0);
+  if (ctx->e1) cudaEventDestroy(ctx->e1);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return EDMD_OK;
+}
+
+extern "C" const char* edmd_last_error(const edmd_ctx* ctx) {
+  return ctx ? ctx->err.c_str() : "null context";
+}

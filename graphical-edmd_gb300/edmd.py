@@ -1,0 +1,259 @@
+"""Python mirror of the engine's C ABI (include/edmd_gpu.h, include/edmd_host.h).
+
+Thin ctypes layer over ``libedmd_gpu.so`` for the tests and the benchmark; the
+product's own host is the C driver ``edmd`` (host/edmd_main.c).  Everything
+here goes through the C ABI: there is no Python or CPU fallback, and loading
+fails loudly when the library has not been built.
+
+Reference flow being mirrored (src/EDMD.c:498-661):
+    constantInit / particlesInit   -> hex_start() / grow_start()   (host C)
+    cellListInit / eventListInit   -> Engine(...)                   (edmd_create)
+    while (t <= tmax) { ... }      -> Engine.advance(...)           (edmd_advance)
+    takeAScreenshot's freeFly-all  -> Engine.sync()                 (edmd_sync)
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libedmd_gpu.so")
+
+OK, ERR_ARG, ERR_CUDA, ERR_OVERLAP, ERR_BUDGET, ERR_CAPACITY, ERR_NODEV = range(7)
+STOP_COLL, STOP_TIME, STOP_TMAX, STOP_SCREEN, STOP_GROW = 1, 2, 3, 4, 5
+F_STOP_AT_SCREEN, F_STOP_AT_GROW, F_TRACE, F_COUNT_NORMAL = 1, 2, 4, 8
+
+
+class SystemDesc(C.Structure):
+    _fields_ = [("N", C.c_int32), ("Lx", C.c_double), ("Ly", C.c_double), ("res", C.c_double),
+                ("Einit", C.c_double), ("first_screen", C.c_double), ("dtime", C.c_double),
+                ("first_thermo", C.c_double), ("dtime_thermo", C.c_double),
+                ("t_growstop", C.c_double), ("tmax", C.c_double)]
+
+
+class Collision(C.Structure):
+    _fields_ = [("i", C.c_int32), ("j", C.c_int32), ("cell_i", C.c_int32), ("cell_j", C.c_int32),
+                ("t", C.c_double)]
+
+
+COLLISION_DTYPE = np.dtype([("i", "<i4"), ("j", "<i4"), ("cell_i", "<i4"), ("cell_j", "<i4"),
+                            ("t", "<f8")])
+
+
+class Counters(C.Structure):
+    _fields_ = [("ncol", C.c_uint64), ("ncol_total", C.c_uint64), ("ncross", C.c_uint64),
+                ("nstale", C.c_uint64), ("npair", C.c_uint64), ("npred", C.c_uint64),
+                ("nevents", C.c_uint64), ("t", C.c_double), ("growing", C.c_int32),
+                ("stop_reason", C.c_int32)]
+
+
+# every symbol the public headers declare, in declaration order
+EXPORTS = [
+    "edmd_create", "edmd_advance", "edmd_sync", "edmd_get_state", "edmd_get_counters",
+    "edmd_get_virial", "edmd_get_thermo", "edmd_get_trace", "edmd_destroy", "edmd_last_error",
+    "edmd_device_info",
+    "edmd_mt_seed", "edmd_mt_u32", "edmd_mt_double", "edmd_hex_size", "edmd_random_size",
+    "edmd_grow_rate", "edmd_normalize", "edmd_init_hex", "edmd_init_grow", "edmd_default_desc",
+]
+
+_lib = None
+_dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+_up = np.ctypeslib.ndpointer(dtype=np.uint32, flags="C_CONTIGUOUS")
+
+
+def load(path=LIB_PATH):
+    """Load libedmd_gpu.so (raises if it is missing: there is no fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is not built; run __graft_entry__.build()")
+    L = C.CDLL(path)
+    L.edmd_create.argtypes = [C.c_int32, C.POINTER(SystemDesc), _dp, _dp, _dp, _dp, _dp, _dp,
+                              C.c_void_p, C.c_int64, C.POINTER(C.c_void_p)]
+    L.edmd_advance.argtypes = [C.c_void_p, C.c_int64, C.c_double, C.c_uint32, C.c_int64,
+                               C.POINTER(C.c_float)]
+    L.edmd_sync.argtypes = [C.c_void_p]
+    L.edmd_get_state.argtypes = [C.c_void_p, C.c_int32] + [C.c_void_p] * 8
+    L.edmd_get_counters.argtypes = [C.c_void_p, C.c_int32, C.POINTER(Counters)]
+    L.edmd_get_virial.argtypes = [C.c_void_p, C.c_int32, _dp, C.c_int32]
+    L.edmd_get_thermo.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.POINTER(C.c_int32)]
+    L.edmd_get_trace.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_int64, C.POINTER(C.c_int64)]
+    L.edmd_destroy.argtypes = [C.c_void_p]
+    L.edmd_last_error.argtypes = [C.c_void_p]
+    L.edmd_last_error.restype = C.c_char_p
+    L.edmd_device_info.argtypes = [C.c_char_p, C.c_int32, C.POINTER(C.c_int32)]
+    L.edmd_mt_seed.argtypes = [C.c_uint32]
+    L.edmd_mt_u32.restype = C.c_uint32
+    L.edmd_mt_double.restype = C.c_double
+    L.edmd_hex_size.argtypes = [C.c_int, C.c_double, C.c_double, C.POINTER(C.c_int),
+                                C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    L.edmd_random_size.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
+                                   C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    L.edmd_grow_rate.argtypes = [C.c_double]
+    L.edmd_grow_rate.restype = C.c_double
+    L.edmd_normalize.argtypes = [C.c_int, C.c_double, _dp, _dp, _dp]
+    L.edmd_init_hex.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, C.c_uint32,
+                                _dp, _dp, _dp, _dp, _dp, _dp, _ip,
+                                C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    L.edmd_init_grow.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, C.c_uint32,
+                                 _dp, _dp, _dp, _dp, _dp, _dp, _dp, _ip,
+                                 C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    L.edmd_default_desc.argtypes = [C.POINTER(SystemDesc), C.c_int, C.c_double, C.c_double,
+                                    C.c_double, C.c_double, C.c_double, C.c_double]
+    _lib = L
+    return L
+
+
+class EngineError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"edmd error {code}: {msg}")
+        self.code = code
+
+
+def _ptr(a):
+    return a.ctypes.data_as(C.c_void_p) if a is not None else None
+
+
+# ------------------------------------------------------------------ host init
+
+def hex_start(N, phi, seed, aspect=1.0, Einit=1.0):
+    """Triangular-lattice start of the reference (Hex = 1) on the host."""
+    L = load()
+    arrs = [np.zeros(N) for _ in range(6)]
+    typ = np.zeros(N, np.int32)
+    Lx, Ly = C.c_double(), C.c_double()
+    n = L.edmd_init_hex(N, phi, aspect, Einit, seed, *arrs, typ, C.byref(Lx), C.byref(Ly))
+    if n < 0:
+        raise EngineError(ERR_ARG, "bad Hex parameters")
+    x, y, vx, vy, rad, m = (a[:n].copy() for a in arrs)
+    return dict(N=n, Lx=Lx.value, Ly=Ly.value, x=x, y=y, vx=vx, vy=vy, rad=rad, m=m,
+                type=typ[:n].copy(), vr=None, vr_base=0.0)
+
+
+def grow_start(N, phi, seed, xs=0.3, q=0.4, aspect=1.0):
+    """Random start with Lubachevsky-Stillinger growth (the reference default)."""
+    L = load()
+    arrs = [np.zeros(N) for _ in range(7)]
+    typ = np.zeros(N, np.int32)
+    Lx, Ly, vrb = C.c_double(), C.c_double(), C.c_double()
+    L.edmd_init_grow(N, phi, xs, q, aspect, seed, *arrs, typ, C.byref(Lx), C.byref(Ly), C.byref(vrb))
+    x, y, vx, vy, rad, m, vr = arrs
+    return dict(N=N, Lx=Lx.value, Ly=Ly.value, x=x, y=y, vx=vx, vy=vy, rad=rad, m=m,
+                type=typ, vr=vr, vr_base=vrb.value)
+
+
+def default_desc(N, Lx, Ly, vr_base=0.0, tmax=4000.0, dtime=100.0, dtime_thermo=100.0):
+    d = SystemDesc()
+    load().edmd_default_desc(C.byref(d), N, Lx, Ly, vr_base, tmax, dtime, dtime_thermo)
+    return d
+
+
+# ------------------------------------------------------------------ engine
+
+class Engine:
+    """A set of independent systems on the GPU (one edmd_ctx)."""
+
+    def __init__(self, systems, trace_cap=0):
+        """systems: list of dicts with N, x, y, vx, vy, rad, m, [vr] and 'desc'."""
+        L = load()
+        self._L = L
+        n = len(systems)
+        descs = (SystemDesc * n)(*[s["desc"] for s in systems])
+        cat = lambda k: np.ascontiguousarray(np.concatenate([np.asarray(s[k], np.float64) for s in systems]))
+        x, y, vx, vy, rad, m = (cat(k) for k in ("x", "y", "vx", "vy", "rad", "m"))
+        vr = None
+        if any(s.get("vr") is not None for s in systems):
+            vr = np.ascontiguousarray(np.concatenate(
+                [np.asarray(s["vr"], np.float64) if s.get("vr") is not None else np.zeros(s["desc"].N)
+                 for s in systems]))
+        h = C.c_void_p()
+        rc = L.edmd_create(n, descs, x, y, vx, vy, rad, m, _ptr(vr), int(trace_cap), C.byref(h))
+        if h.value is None and rc != OK:
+            raise EngineError(rc, "edmd_create failed")
+        self.h = h
+        self.n = n
+        self.N = [s["desc"].N for s in systems]
+        self.trace_cap = trace_cap
+        if rc != OK:
+            msg = self.last_error()
+            self.close()
+            raise EngineError(rc, msg)
+
+    def last_error(self):
+        return self._L.edmd_last_error(self.h).decode()
+
+    def _ck(self, rc):
+        if rc != OK:
+            raise EngineError(rc, self.last_error())
+
+    def advance(self, max_coll=2**62, t_stop=float("inf"), flags=0, max_events=2**62, check=True):
+        ms = C.c_float()
+        rc = self._L.edmd_advance(self.h, int(max_coll), float(t_stop), int(flags), int(max_events),
+                                  C.byref(ms))
+        if check:
+            self._ck(rc)
+        return rc, ms.value
+
+    def sync(self):
+        self._ck(self._L.edmd_sync(self.h))
+
+    def state(self, s=0):
+        N = self.N[s]
+        out = {k: np.zeros(N) for k in ("x", "y", "vx", "vy", "rad", "m")}
+        cell = np.zeros(N, np.int32)
+        coll = np.zeros(N, np.uint32)
+        self._ck(self._L.edmd_get_state(self.h, s, *[_ptr(out[k]) for k in ("x", "y", "vx", "vy", "rad", "m")],
+                                        _ptr(cell), _ptr(coll)))
+        out["cell"] = cell
+        out["coll"] = coll
+        return out
+
+    def counters(self, s=0):
+        c = Counters()
+        self._ck(self._L.edmd_get_counters(self.h, s, C.byref(c)))
+        return {k: getattr(c, k) for k, _ in Counters._fields_}
+
+    def virial(self, s=0, reset=False):
+        v = np.zeros(4)
+        self._ck(self._L.edmd_get_virial(self.h, s, v, int(reset)))
+        return v
+
+    def thermo(self, s=0, cap=1024):
+        rows = np.zeros((cap, 9))
+        n = C.c_int32()
+        rc = self._L.edmd_get_thermo(self.h, s, _ptr(rows), cap, C.byref(n))
+        if rc not in (OK, ERR_CAPACITY):
+            self._ck(rc)
+        return rows[: min(n.value, cap)]
+
+    def trace(self, s=0):
+        cap = max(self.trace_cap, 1)
+        out = np.zeros(cap, COLLISION_DTYPE)
+        n = C.c_int64()
+        rc = self._L.edmd_get_trace(self.h, s, _ptr(out), cap, C.byref(n))
+        if rc not in (OK, ERR_CAPACITY):
+            self._ck(rc)
+        return out[: min(n.value, cap)]
+
+    def close(self):
+        if getattr(self, "h", None) is not None and self.h.value:
+            self._L.edmd_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def device_info():
+    L = load()
+    name = C.create_string_buffer(256)
+    sms = C.c_int32()
+    rc = L.edmd_device_info(name, 256, C.byref(sms))
+    if rc != OK:
+        return None
+    return name.value.decode(), sms.value

@@ -1,0 +1,141 @@
+/*
+ * edmd_gpu.h -- C ABI of the GB300 event-driven hard-disk engine.
+ *
+ * Drop-in boundary for the no-graphics event loop of Syrocco/Graphical-EDMD.
+ * The reference binds its hot path through five function pointers
+ * (src/EDMD.c:317-321: collisionEvent, doTheCollision, freeFly, doTheWall,
+ * crossingEvent) bound at src/EDMD.c:1974-1990 / 4755-4759 and driven one
+ * event at a time by the loop in main (src/EDMD.c:523-618).  A GPU cannot be
+ * driven one event per call, so this ABI replaces that whole loop body in
+ * chunks: the host creates systems, then advances them by a number of
+ * collisions or up to a time, and reads state back at sampling points.
+ *
+ * Conventions
+ *   - Plain C types only.  Host arrays are caller-owned; the context owns all
+ *     device memory and one CUDA stream.  A context is not thread-safe.
+ *   - Every function returns an int status (EDMD_OK = 0) and records a
+ *     message readable with edmd_last_error(ctx).
+ *   - Systems are independent; arrays passed for several systems are the
+ *     per-system arrays concatenated in system order.
+ *   - Device loops are bounded: a call that would exceed its event budget
+ *     returns EDMD_ERR_BUDGET instead of spinning.
+ */
+#ifndef EDMD_GPU_H
+#define EDMD_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define EDMD_OK             0
+#define EDMD_ERR_ARG        1   /* bad argument or configuration              */
+#define EDMD_ERR_CUDA       2   /* a CUDA runtime call failed                 */
+#define EDMD_ERR_OVERLAP    3   /* overlap found, as src/EDMD.c:2708-2717     */
+#define EDMD_ERR_BUDGET     4   /* per-call event budget exhausted            */
+#define EDMD_ERR_CAPACITY   5   /* an internal buffer is too small            */
+#define EDMD_ERR_NODEV      6   /* no CUDA device                             */
+
+/* per-system stop reasons reported by edmd_advance */
+#define EDMD_STOP_COLL      1   /* max_coll accepted collisions reached       */
+#define EDMD_STOP_TIME      2   /* next event at or after t_stop              */
+#define EDMD_STOP_TMAX      3   /* loop condition t <= tmax failed            */
+#define EDMD_STOP_SCREEN    4   /* stopped right after a screenshot           */
+#define EDMD_STOP_GROW      5   /* stopped right after the growth stop        */
+
+/* edmd_advance flags */
+#define EDMD_F_STOP_AT_SCREEN  1u  /* return after each screenshot event      */
+#define EDMD_F_STOP_AT_GROW    2u  /* return after the growth-stop event      */
+#define EDMD_F_TRACE           4u  /* record accepted collisions              */
+#define EDMD_F_COUNT_NORMAL    8u  /* max_coll counts normal-phase only       */
+
+/*
+ * One periodic 2D system.  Replaces the globals that constantInit
+ * (src/EDMD.c:745-1219) and eventListInit (src/EDMD.c:1935-2019) set up.
+ */
+typedef struct edmd_system_desc {
+	int32_t N;             /* number of disks                                  */
+	double  Lx, Ly;        /* periodic box                                     */
+	double  res;           /* restitution coefficient (-r), 1 = elastic        */
+	double  Einit;         /* energy per disk after the growth stop (-E)       */
+	double  first_screen;  /* first screenshot time (firstScreen, growth-adjusted) */
+	double  dtime;         /* screenshot period (-D)                           */
+	double  first_thermo;  /* first thermo time (firstThermo, growth-adjusted) */
+	double  dtime_thermo;  /* thermo period (-o)                               */
+	double  t_growstop;    /* 1/vr for a growth start, < 0 for a direct start  */
+	double  tmax;          /* loop bound (-t, +1/vr for a growth start)        */
+} edmd_system_desc;
+
+/* one accepted collision, as logged by the reference harness */
+typedef struct edmd_collision {
+	int32_t i, j;          /* owner and partner disk                           */
+	int32_t cell_i, cell_j;/* linear cells Y*Nxcells+X                         */
+	double  t;
+} edmd_collision;
+
+/* per-system counters, cumulative since creation */
+typedef struct edmd_counters {
+	uint64_t ncol;         /* accepted collisions (ncol, reset at growth stop) */
+	uint64_t ncol_total;   /* accepted collisions including the growth phase   */
+	uint64_t ncross;       /* cell crossings                                   */
+	uint64_t nstale;       /* stale collision events popped                    */
+	uint64_t npair;        /* pair contact-time solves                         */
+	uint64_t npred;        /* collision predictions                            */
+	uint64_t nevents;      /* popped events                                    */
+	double   t;            /* current simulation time                          */
+	int32_t  growing;      /* 1 while the growth phase runs                    */
+	int32_t  stop_reason;  /* EDMD_STOP_* of the last advance                  */
+} edmd_counters;
+
+typedef struct edmd_ctx edmd_ctx;
+
+/* Create `nsys` systems (replaces particlesInit's hand-off, cellListInit
+ * src/EDMD.c:1906 and eventListInit src/EDMD.c:1935).  Arrays hold the sum
+ * of desc[k].N entries.  `vr` (growth rate per disk) may be NULL for direct
+ * starts.  Positions must lie in [0,L).  trace_cap is the per-system
+ * capacity of the collision trace (0 disables tracing). */
+int edmd_create(int32_t nsys, const edmd_system_desc* desc,
+                const double* x, const double* y, const double* vx, const double* vy,
+                const double* rad, const double* m, const double* vr,
+                int64_t trace_cap, edmd_ctx** out);
+
+/* Advance every system (replaces the loop body src/EDMD.c:523-618).  Each
+ * system stops on its own at max_coll accepted collisions of this call, at
+ * the first event with t >= t_stop, when t > tmax, or per `flags`.
+ * max_events bounds the events one system may pop in this call.
+ * elapsed_ms (may be NULL) receives the device time of the call measured with
+ * CUDA events on the context's stream. */
+int edmd_advance(edmd_ctx* ctx, int64_t max_coll, double t_stop, uint32_t flags,
+                 int64_t max_events, float* elapsed_ms);
+
+/* Free-fly every disk of every system to its current time, the first step of
+ * takeAScreenshot (src/EDMD.c:4657-4661). */
+int edmd_sync(edmd_ctx* ctx);
+
+/* Copy the state of one system to host arrays (any pointer may be NULL). */
+int edmd_get_state(edmd_ctx* ctx, int32_t sys, double* x, double* y, double* vx,
+                   double* vy, double* rad, double* m, int32_t* cell, uint32_t* coll);
+
+int edmd_get_counters(edmd_ctx* ctx, int32_t sys, edmd_counters* out);
+
+/* Collision-virial accumulators collTermX, collTermY, collTermXY, collTermYX
+ * (src/EDMD.c:3809-3817) of one system; reset them if `reset`. */
+int edmd_get_virial(edmd_ctx* ctx, int32_t sys, double out[4], int32_t reset);
+
+/* Thermo rows of one system (t Ncol E p px py pxy pyx a2, saveThermo
+ * src/EDMD.c:5232-5697 with Nthermo = 1); returns the row count in *n. */
+int edmd_get_thermo(edmd_ctx* ctx, int32_t sys, double* rows, int32_t cap, int32_t* n);
+
+/* Collision trace of one system recorded since creation (EDMD_F_TRACE). */
+int edmd_get_trace(edmd_ctx* ctx, int32_t sys, edmd_collision* out, int64_t cap, int64_t* n);
+
+int edmd_destroy(edmd_ctx* ctx);
+const char* edmd_last_error(const edmd_ctx* ctx);
+int edmd_device_info(char* name, int32_t cap, int32_t* sm_count);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

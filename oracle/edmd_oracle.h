@@ -99,6 +99,8 @@ void     orc_virial(orc_sys* s, double out[4], int reset);
 /* g(r) histogram (pcf.c:61-120), counts then normalised */
 int      orc_pcf(const orc_sys* s, double dr, double max_r, double* g, int nbins);
 double   orc_vr(const orc_sys* s);
+/* thermo rows (t Ncol E p px py pxy pyx a2), 9 doubles each; returns count */
+int      orc_thermo_rows(const orc_sys* s, double* out, int cap);
 
 /* MT19937 exposed for tests of the host-side init */
 void     orc_mt_seed(uint32_t s);

@@ -1,0 +1,82 @@
+"""Shared test fixtures.
+
+GPU tests are marked ``@pytest.mark.gpu``; everything else runs on a CPU-only
+machine.  The engine package lives in ``graphical-edmd_gb300/`` (not an
+importable name), so it is loaded by path.
+"""
+import importlib.util
+import os
+import subprocess
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+PKG = os.path.join(ROOT, "graphical-edmd_gb300")
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+sys.path.insert(0, ROOT)
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300)")
+
+
+def load_pkg_module(name):
+    key = "edmd_gb300_" + name
+    if key in sys.modules:
+        return sys.modules[key]
+    spec = importlib.util.spec_from_file_location(key, os.path.join(PKG, name + ".py"))
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules[key] = mod
+    spec.loader.exec_module(mod)
+    return mod
+
+
+@pytest.fixture(scope="session")
+def built():
+    """Build the engine library and the oracle once per session."""
+    b = load_pkg_module("build")
+    b.build()
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
+    return True
+
+
+@pytest.fixture(scope="session")
+def edmd(built):
+    return load_pkg_module("edmd")
+
+
+@pytest.fixture(scope="session")
+def oracle(built):
+    from oracle import oracle as o
+    return o
+
+
+def golden(name):
+    return dict(np.load(os.path.join(GOLDEN, name + ".npz"), allow_pickle=False))
+
+
+def golden_names():
+    return sorted(f[:-4] for f in os.listdir(GOLDEN) if f.endswith(".npz") and not f.startswith("files_"))
+
+
+def parse_args(args):
+    """Reference CLI string of a fixture -> start parameters."""
+    a = str(args).split()
+    out = dict(hex="--hex" in a, N=500, phi=0.38, xs=0.3, q=0.4, seed=1, tmax=4000.0, dtime=100.0,
+               dtime_thermo=100.0)
+    keys = {"-N": ("N", int), "--phi": ("phi", float), "-x": ("xs", float), "-q": ("q", float),
+            "-v": ("seed", int), "-t": ("tmax", float), "-D": ("dtime", float), "-o": ("dtime_thermo", float)}
+    for k, (name, f) in keys.items():
+        if k in a:
+            out[name] = f(a[a.index(k) + 1])
+    return out
+
+
+def has_gpu():
+    try:
+        import torch  # noqa: F401
+        return torch.cuda.is_available()
+    except Exception:
+        return False

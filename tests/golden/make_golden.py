@@ -1,0 +1,128 @@
+"""Generate the golden fixtures in tests/golden/ from the reference's own C.
+
+Run here (where the reference checkout exists):
+
+    python tests/golden/make_golden.py [--ref /root/reference]
+
+It builds ``oracle/_ref/ref_trace`` (``make -C oracle ref``), which compiles
+the reference's unmodified src/EDMD.c and satellites with IEEE flags and
+re-runs its main loop (src/EDMD.c:523-618) with a trace hook, then stores
+for each case:
+
+* the initial state after the reference's own init (src/EDMD.c:1356-1839,
+  normalizePhysicalQ 5723-5764),
+* every accepted collision ``(i, j, cell_i, cell_j, t)`` in processing order,
+* the collision-virial accumulators, final time and counters,
+* the state after free-flying every disk to the final time.
+
+The fixtures are what the GPU parity tests compare against on the GPU machine,
+where the reference checkout does not exist.
+"""
+import argparse
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+
+# name: (reference CLI args, max accepted collisions, keep full final state)
+CASES = {
+    "hex2000_v1": ("--hex -N 2000 --phi 0.70 -x 0 -v 1", 10000, True),
+    "hex2000_v2": ("--hex -N 2000 --phi 0.70 -x 0 -v 2", 10000, True),
+    "hex1024_v3": ("--hex -N 1024 --phi 0.60 -x 0 -v 3", 10000, True),
+    "hex10000_v4": ("--hex -N 10000 --phi 0.72 -x 0 -v 4", 10000, False),
+    "grow256_v7": ("-N 256 --phi 0.5 -x 0.5 -q 0.7142857 -v 7", 20000, True),
+    "grow400_v11": ("-N 400 --phi 0.74 -x 0.5 -q 0.7142857 -v 11", 20000, True),
+    "grow300_v5": ("-N 300 --phi 0.3 -x 0.5 -q 0.7142857 -v 5", 20000, True),
+}
+
+# a short run whose dump and thermo files are kept verbatim (format pin)
+FILES_CASE = ("files_hex64", "--hex -N 64 --phi 0.5 -x 0 -v 9 -t 1200 -D 100 -o 50")
+
+
+def hx(s):
+    return float.fromhex(s)
+
+
+def parse_trace(path):
+    init, colls, state = [], [], []
+    vir = tfin = None
+    head = None
+    with open(path) as f:
+        for line in f:
+            p = line.split()
+            if p[0] == "#":
+                head = dict(N=int(p[2]), Lx=hx(p[4]), Ly=hx(p[6]), Nxc=int(p[8]), Nyc=int(p[10]))
+            elif p[0] == "I":
+                init.append([hx(v) for v in p[2:8]] + [int(p[8])])
+            elif p[0] == "C":
+                colls.append((int(p[2]), int(p[3]), int(p[4]), int(p[5]), hx(p[6])))
+            elif p[0] == "V":
+                vir = [hx(v) for v in p[1:5]]
+            elif p[0] == "T":
+                tfin = (hx(p[1]), int(p[2]), int(p[3]))
+            elif p[0] == "S":
+                state.append([hx(v) for v in p[2:7]] + [int(p[7]), int(p[8])])
+    init = np.array(init, dtype=object)
+    state = np.array(state, dtype=object)
+    c = np.array(colls, dtype=object) if colls else np.zeros((0, 5), dtype=object)
+    return head, init, c, vir, tfin, state
+
+
+def run_case(exe, args, maxcoll, trace, extra_env=None):
+    env = dict(os.environ)
+    env["MAXCOLL"] = str(maxcoll)
+    env["TRACE_OUT"] = trace
+    env.update(extra_env or {})
+    subprocess.run([exe] + args.split(), env=env, check=True,
+                   stdout=subprocess.DEVNULL)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default="/root/reference")
+    a = ap.parse_args()
+    subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "ref", f"REF={a.ref}"], check=True)
+    exe = os.path.join(ROOT, "oracle", "_ref", "ref_trace")
+    tmp = os.path.join(HERE, "_tmp_trace.txt")
+    for name, (args, maxcoll, full) in CASES.items():
+        run_case(exe, args, maxcoll, tmp)
+        head, init, c, vir, tfin, state = parse_trace(tmp)
+        out = dict(
+            args=np.array(args), N=head["N"], Lx=head["Lx"], Ly=head["Ly"],
+            Nxc=head["Nxc"], Nyc=head["Nyc"],
+            x0=init[:, 0].astype(np.float64), y0=init[:, 1].astype(np.float64),
+            vx0=init[:, 2].astype(np.float64), vy0=init[:, 3].astype(np.float64),
+            rad0=init[:, 4].astype(np.float64), m0=init[:, 5].astype(np.float64),
+            type0=init[:, 6].astype(np.int32),
+            ci=np.array([r[0] for r in c], np.int32),
+            cj=np.array([r[1] for r in c], np.int32),
+            ccell_i=np.array([r[2] for r in c], np.int32),
+            ccell_j=np.array([r[3] for r in c], np.int32),
+            ct=np.array([r[4] for r in c], np.float64),
+            virial=np.array(vir, np.float64), t_final=tfin[0], ncol=tfin[1], ncross=tfin[2],
+            xf=state[:, 0].astype(np.float64), yf=state[:, 1].astype(np.float64),
+            cellf=state[:, 5].astype(np.int32), collf=state[:, 6].astype(np.int64),
+        )
+        if full:
+            out.update(vxf=state[:, 2].astype(np.float64), vyf=state[:, 3].astype(np.float64),
+                       radf=state[:, 4].astype(np.float64))
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+        print(name, "N", head["N"], "collisions", len(c), "t_final", tfin[0])
+    # verbatim dump + thermo files of a short run (ovito/LAMMPS text format pin)
+    name, args = FILES_CASE
+    dump = os.path.join(HERE, name + ".dump")
+    thermo = os.path.join(HERE, name + ".thermo")
+    run_case(exe, args, 10**12, tmp, {"DUMP_OUT": dump, "THERMO_OUT": thermo})
+    head, init, c, vir, tfin, state = parse_trace(tmp)
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), args=np.array(args), N=head["N"],
+                        ncol=tfin[1], t_final=tfin[0])
+    print(name, "N", head["N"], "collisions", len(c))
+    os.remove(tmp)
+
+
+if __name__ == "__main__":
+    sys.exit(main())
