@@ -85,6 +85,22 @@ struct SysDev {
   int64_t trace_cap;
   double* rows;                // thermo rows, 9 doubles each
   int32_t rows_cap, pad;
+  // calendar of the thread-per-system engine (edmd_lane.cu)
+  uint16_t* cal;               // N buckets x CAL_SUB lines of CAL_LINE u16: [count, ids...]
+  uint8_t* mask;               // per bucket: bit k set when sub-bucket k is non-empty
+  double invw;                 // CAL_SUB / dtP
+};
+
+constexpr int CAL_SUB = 8;     // sub-buckets per calendar bucket (ordered by time)
+constexpr int CAL_LINE = 32;   // u16 per sub-bucket line: a count and up to 31 event ids
+
+struct RunArgs {
+  int64_t max_coll;
+  double t_stop;
+  uint32_t flags;
+  int64_t max_events;
+  int32_t nsys;
+  int32_t* work;               // persistent work counter (warp engine)
 };
 
 // ---------------------------------------------------------------- arithmetic

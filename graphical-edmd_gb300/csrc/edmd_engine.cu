@@ -30,21 +30,17 @@
 
 using namespace edmd;
 
+namespace edmd {
+cudaError_t lane_build(const SysDev* ds, int nsys, cudaStream_t st);
+cudaError_t lane_run_launch(const SysDev* ds, const RunArgs& A, int threads_per_block, cudaStream_t st);
+}
+
 #define FULL 0xffffffffu
 
 namespace {
 
 constexpr int MAXC = 8;          // candidates buffered per cell list per lane
 constexpr int WARPS_PER_BLOCK = 4;
-
-struct RunArgs {
-  int64_t max_coll;
-  double t_stop;
-  uint32_t flags;
-  int64_t max_events;
-  int32_t nsys;
-  int32_t* work;                 // persistent work counter
-};
 
 struct WarpSmem {
   int32_t reg[32 * MAXC];        // per-lane walk buffers
@@ -664,8 +660,9 @@ k_run(const SysDev* __restrict__ sys, RunArgs A) {
 // initial predictions of eventListInit (src/EDMD.c:2007-2012): all disks are
 // current at t = 0 and the calendar sits at bucket 0, so every key is known
 // without serialising: the k-th scheduled event has counter k.
-__global__ void k_init_events(const SysDev* __restrict__ sys, int s) {
-  const SysDev S = sys[s];
+// grid.y = system, grid.x covers the disks of the largest system + 1.
+__global__ void k_init_events(const SysDev* __restrict__ sys) {
+  const SysDev& S = sys[blockIdx.y];
   const Box& B = S.B;
   const int N = B.N;
   const bool grow = S.st->grow != 0;
@@ -720,10 +717,12 @@ __global__ void k_init_events(const SysDev* __restrict__ sys, int s) {
   }
 }
 
-// link the initial overflow bucket in LIFO order and finish the scalar state
-__global__ void k_init_finish(const SysDev* __restrict__ sys, int s) {
-  const SysDev S = sys[s];
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+// link the initial overflow bucket in LIFO order and finish the scalar state;
+// one thread per system
+__global__ void k_init_finish(const SysDev* __restrict__ sys, int nsys) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nsys) return;
+  const SysDev& S = sys[s];
   const int N = S.B.N;
   const bool grow = S.st->grow != 0;
   int head = NIL;
@@ -745,15 +744,17 @@ __global__ void k_init_finish(const SysDev* __restrict__ sys, int s) {
   R.collT[0] = R.collT[1] = 0;
 }
 
-__global__ void k_tree_build(const SysDev* __restrict__ sys, int s) {
-  const SysDev S = sys[s];
-  tree_rebuild(S, threadIdx.x & 31);
+// one warp per system
+__global__ void k_tree_build(const SysDev* __restrict__ sys, int nsys) {
+  int s = blockIdx.x;
+  if (s >= nsys) return;
+  tree_rebuild(sys[s], threadIdx.x & 31);
 }
 
 __global__ void k_sync(const SysDev* __restrict__ sys, int nsys) {
   int s = blockIdx.x;
   if (s >= nsys) return;
-  const SysDev S = sys[s];
+  const SysDev& S = sys[s];
   const double t = S.st->t;
   const bool grow = S.st->grow != 0;
   for (int i = threadIdx.x; i < S.B.N; i += blockDim.x) {
@@ -763,20 +764,61 @@ __global__ void k_sync(const SysDev* __restrict__ sys, int nsys) {
   }
 }
 
+// disk records of every system -> concatenated SoA staging (x y vx vy rad m)
+__global__ void k_gather(const Disk* __restrict__ d, int64_t total, double* __restrict__ out) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= total) return;
+  Disk p = d[i];
+  out[i] = p.x; out[total + i] = p.y; out[2 * total + i] = p.vx;
+  out[3 * total + i] = p.vy; out[4 * total + i] = p.rad; out[5 * total + i] = p.m;
+}
+
 }  // namespace
 
 // ==================================================================== C ABI
 
 struct edmd_ctx {
   int nsys = 0;
+  int64_t total_N = 0;
+  int maxN = 0;
   cudaStream_t stream = nullptr;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   std::vector<SysDev> hs;
+  std::vector<edmd_system_desc> desc;
+  std::vector<int64_t> disk_off, cell_off;
   SysDev* ds = nullptr;
-  char* pool = nullptr;
+  // device arrays shared by all systems (each system owns a slice)
+  Disk* d = nullptr; double* vr = nullptr;
+  int32_t *cx = nullptr, *cy = nullptr, *prv = nullptr, *crossX = nullptr, *crossY = nullptr;
+  int32_t* head = nullptr;
+  Ev* ev = nullptr; int32_t *on = nullptr, *op = nullptr;
+  Node* tree = nullptr;
+  SysState* st = nullptr;
+  edmd_collision* trace = nullptr;
+  double* rows = nullptr;
+  double* stage = nullptr;          // SoA gather buffer (6 x total_N)
   int32_t* work = nullptr;
+  uint16_t* cal = nullptr;          // calendars of the thread-per-system engine
+  uint8_t* mask = nullptr;
+  int engine = 0;                   // EDMD_ENGINE_WARP or EDMD_ENGINE_LANE
+  int64_t total_C = 0;
   std::string err;
 };
+
+static int g_engine = EDMD_ENGINE_AUTO;
+static int g_lane_threads = 32;
+
+extern "C" int edmd_set_engine(int32_t kind) {
+  if (kind < EDMD_ENGINE_AUTO || kind > EDMD_ENGINE_LANE) return EDMD_ERR_ARG;
+  g_engine = kind;
+  return EDMD_OK;
+}
+
+extern "C" int edmd_set_lane_threads(int32_t threads_per_block) {
+  if (threads_per_block < 1 || threads_per_block > 1024) return EDMD_ERR_ARG;
+  g_lane_threads = threads_per_block;
+  return EDMD_OK;
+}
 
 static int set_err(edmd_ctx* c, int code, const std::string& m) {
   if (c) c->err = m;
@@ -789,8 +831,6 @@ static int set_err(edmd_ctx* c, int code, const std::string& m) {
                                                                   cudaGetErrorString(_e)); \
   } while (0)
 
-static size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
-
 extern "C" int edmd_device_info(char* name, int32_t cap, int32_t* sm_count) {
   int n = 0;
   if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) return EDMD_ERR_NODEV;
@@ -801,153 +841,187 @@ extern "C" int edmd_device_info(char* name, int32_t cap, int32_t* sm_count) {
   return EDMD_OK;
 }
 
+template <class T>
+static cudaError_t dalloc(T** p, size_t n) { return cudaMalloc((void**)p, (n ? n : 1) * sizeof(T)); }
+
+// (Re)initialise every system from host arrays: the cell lists are built on
+// the host in index order (cellListInit src/EDMD.c:1906 -> addToCell 2053,
+// push-front), the event set on the device (eventListInit 1935).
+// first_screen/first_thermo/t_growstop per system come from `desc` unless
+// `restart`, which follows the -l load path: normal phase, firstScreen 1,
+// firstThermo 1000 (src/EDMD.c:244-247; eventListInit 1958 skips the growth
+// shift when load != 0).
+static int stage_all(edmd_ctx* ctx, const double* x, const double* y, const double* vx,
+                     const double* vy, const double* rad, const double* m, const double* vr,
+                     bool restart) {
+  const int64_t TN = ctx->total_N;
+  std::vector<Disk> hd(TN);
+  std::vector<int32_t> hcx(TN), hcy(TN), hprv(TN);
+  std::vector<int32_t> hhead(ctx->total_C, NIL);
+  std::vector<SysState> hst(ctx->nsys);
+  for (int s = 0; s < ctx->nsys; s++) {
+    const SysDev& S = ctx->hs[s];
+    const Box& B = S.B;
+    const edmd_system_desc& D = ctx->desc[s];
+    const int64_t o = ctx->disk_off[s];
+    int32_t* head = hhead.data() + ctx->cell_off[s];
+    for (int64_t i = 0; i < B.N; i++) {
+      int64_t g = o + i;
+      double px = x[g], py = y[g];
+      if (restart) {                     // PBCpostX/Y on loaded positions (src/EDMD.c:1405-1406)
+        if (px < 0) px += D.Lx; else if (px >= D.Lx) px -= D.Lx;
+        if (py < 0) py += D.Ly; else if (py >= D.Ly) py -= D.Ly;
+      }
+      if (!(px >= 0 && px < D.Lx && py >= 0 && py < D.Ly))
+        return set_err(ctx, EDMD_ERR_ARG, "position outside the box (system " + std::to_string(s) + ")");
+      Disk& q = hd[g];
+      q.x = px; q.y = py; q.vx = vx[g]; q.vy = vy[g]; q.tl = 0; q.rad = rad[g]; q.m = m[g];
+      q.coll = 0;
+      int X = (int)(q.x * B.cxf), Y = (int)(q.y * B.cyf);
+      if (X >= B.Nxc) X = B.Nxc - 1;
+      if (Y >= B.Nyc) Y = B.Nyc - 1;
+      hcx[g] = X; hcy[g] = Y; hprv[g] = NIL;
+      q.nxt = head[Y * B.Nxc + X];
+      head[Y * B.Nxc + X] = (int32_t)i;
+      if (q.nxt != NIL) hprv[o + q.nxt] = (int32_t)i;
+    }
+    SysState& st = hst[s];
+    memset(&st, 0, sizeof(st));
+    st.k = 0; st.next_wrap = (uint64_t)B.N; st.ovf = NIL;
+    st.grow = (!restart && D.t_growstop > 0) ? 1 : 0;
+    double fs = restart ? 1.0 : D.first_screen, ft = restart ? 1000.0 : D.first_thermo;
+    st.lastThermo = ft + 0.000000001;   // addEventThermo(firstThermo + 1e-9), read by k_init_events
+    st.collT[0] = st.grow ? D.t_growstop : -1;
+    st.collT[1] = fs;
+  }
+  cudaStream_t sm = ctx->stream;
+  CK(cudaMemcpyAsync(ctx->st, hst.data(), ctx->nsys * sizeof(SysState), cudaMemcpyHostToDevice, sm));
+  CK(cudaMemcpyAsync(ctx->d, hd.data(), TN * sizeof(Disk), cudaMemcpyHostToDevice, sm));
+  if (vr && !restart) CK(cudaMemcpyAsync(ctx->vr, vr, TN * 8, cudaMemcpyHostToDevice, sm));
+  else if (!vr && !restart) CK(cudaMemsetAsync(ctx->vr, 0, TN * 8, sm));
+  CK(cudaMemcpyAsync(ctx->cx, hcx.data(), TN * 4, cudaMemcpyHostToDevice, sm));
+  CK(cudaMemcpyAsync(ctx->cy, hcy.data(), TN * 4, cudaMemcpyHostToDevice, sm));
+  CK(cudaMemcpyAsync(ctx->prv, hprv.data(), TN * 4, cudaMemcpyHostToDevice, sm));
+  CK(cudaMemsetAsync(ctx->crossX, 0, TN * 4, sm));
+  CK(cudaMemsetAsync(ctx->crossY, 0, TN * 4, sm));
+  CK(cudaMemcpyAsync(ctx->head, hhead.data(), ctx->total_C * 4, cudaMemcpyHostToDevice, sm));
+  dim3 g((ctx->maxN + 1 + 127) / 128, ctx->nsys);
+  k_init_events<<<g, 128, 0, sm>>>(ctx->ds);
+  k_init_finish<<<(ctx->nsys + 127) / 128, 128, 0, sm>>>(ctx->ds, ctx->nsys);
+  if (ctx->engine == EDMD_ENGINE_LANE) CK(lane_build(ctx->ds, ctx->nsys, sm));
+  else k_tree_build<<<ctx->nsys, 32, 0, sm>>>(ctx->ds, ctx->nsys);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(sm));   // host staging vectors go out of scope
+  std::vector<int32_t> status(ctx->nsys);
+  for (int s = 0; s < ctx->nsys; s++) status[s] = 0;
+  CK(cudaMemcpy2D(status.data(), 4, &ctx->st[0].status, sizeof(SysState), 4, ctx->nsys,
+                  cudaMemcpyDeviceToHost));
+  for (int s = 0; s < ctx->nsys; s++)
+    if (status[s] != EDMD_OK)
+      return set_err(ctx, status[s], "initial configuration of system " + std::to_string(s) +
+                                         " has overlapping disks");
+  return EDMD_OK;
+}
+
 extern "C" int edmd_create(int32_t nsys, const edmd_system_desc* desc, const double* x,
                            const double* y, const double* vx, const double* vy,
                            const double* rad, const double* m, const double* vr,
                            int64_t trace_cap, edmd_ctx** out) {
-  if (!out || nsys <= 0 || !desc || !x || !y || !vx || !vy || !rad || !m) return EDMD_ERR_ARG;
+  if (!out || nsys <= 0 || !desc || !x || !y || !vx || !vy || !rad || !m || trace_cap < 0)
+    return EDMD_ERR_ARG;
   *out = nullptr;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return EDMD_ERR_NODEV;
   edmd_ctx* ctx = new edmd_ctx();
+  *out = ctx;
   ctx->nsys = nsys;
   ctx->hs.resize(nsys);
+  ctx->desc.assign(desc, desc + nsys);
+  ctx->disk_off.resize(nsys);
+  ctx->cell_off.resize(nsys);
   const int rows_cap = 1024;
-  // ---- layout
-  std::vector<size_t> off(nsys);
-  size_t total = 0;
-  std::vector<std::vector<int>> lev_cnt(nsys);
+  std::vector<int64_t> ev_off(nsys), node_off(nsys);
+  int64_t TN = 0, TC = 0, TE = 0, TT = 0;
   for (int s = 0; s < nsys; s++) {
     const edmd_system_desc& D = desc[s];
-    if (D.N < 2 || !(D.Lx > 0) || !(D.Ly > 0)) { delete ctx; return EDMD_ERR_ARG; }
+    if (D.N < 2 || !(D.Lx > 0) || !(D.Ly > 0)) return set_err(ctx, EDMD_ERR_ARG, "bad system descriptor");
     SysDev& S = ctx->hs[s];
     memset(&S, 0, sizeof(S));
     Box& B = S.B;
     B.N = D.N; B.Lx = D.Lx; B.Ly = D.Ly;
     B.hLx = D.Lx / 2; B.hLy = D.Ly / 2;                      // boxConstantHelper 679-714
     B.Nyc = (int)(B.hLy); B.Nxc = (int)(B.hLx);
-    if (B.Nxc < 1 || B.Nyc < 1) { delete ctx; return EDMD_ERR_ARG; }
+    if (B.Nxc < 1 || B.Nyc < 1) return set_err(ctx, EDMD_ERR_ARG, "box smaller than one cell");
     B.cxs = D.Lx / B.Nxc; B.cys = D.Ly / B.Nyc;
     B.cxf = 1 / B.cxs; B.cyf = 1 / B.cys;
     B.dtP = 5.0 / (double)D.N;
     B.dtPN = B.dtP * D.N;
     S.res = D.res; S.Einit = D.Einit; S.dtime = D.dtime; S.dtimeTh = D.dtime_thermo; S.tmax = D.tmax;
     S.L = D.N + NSPECIAL;
-    int c = S.L, h = 0;
-    lev_cnt[s].push_back(c);
-    while (c > 1) { c = (c + 31) / 32; lev_cnt[s].push_back(c); }
-    S.nlev = (int)lev_cnt[s].size();
-    if (S.nlev > MAXLEV) { delete ctx; return EDMD_ERR_ARG; }
-    size_t nodes = 0;
-    for (h = 0; h < S.nlev; h++) { S.lev_off[h] = (int)nodes; S.lev_cnt[h] = lev_cnt[s][h]; nodes += lev_cnt[s][h]; }
-    size_t N = D.N, E = 2 * N + NSPECIAL, C = (size_t)B.Nxc * B.Nyc;
-    size_t sz = 0;
-    sz += align_up(sizeof(SysState), 256);
-    sz += align_up(N * sizeof(Disk), 256);
-    sz += align_up(N * 8, 256);            // vr
-    sz += 5 * align_up(N * 4, 256);        // cx cy prv crossX crossY
-    sz += align_up(C * 4, 256);            // head
-    sz += align_up(E * sizeof(Ev), 256);
-    sz += 2 * align_up(E * 4, 256);        // on op
-    sz += align_up(nodes * sizeof(Node), 256);
-    sz += align_up((size_t)trace_cap * sizeof(edmd_collision), 256);
-    sz += align_up((size_t)rows_cap * 9 * 8, 256);
-    off[s] = total;
-    total += sz;
+    int c = S.L;
+    S.nlev = 0;
+    int64_t nodes = 0;
+    for (;;) {
+      if (S.nlev >= MAXLEV) return set_err(ctx, EDMD_ERR_ARG, "system too large");
+      S.lev_off[S.nlev] = (int32_t)nodes; S.lev_cnt[S.nlev] = c; nodes += c; S.nlev++;
+      if (c == 1) break;
+      c = (c + 31) / 32;
+    }
+    ctx->disk_off[s] = TN; ctx->cell_off[s] = TC; ev_off[s] = TE; node_off[s] = TT;
+    TN += D.N; TC += (int64_t)B.Nxc * B.Nyc; TE += 2 * (int64_t)D.N + NSPECIAL; TT += nodes;
+    if (D.N > ctx->maxN) ctx->maxN = D.N;
   }
-  cudaError_t ce = cudaMalloc(&ctx->pool, total);
-  if (ce != cudaSuccess) { std::string m2 = cudaGetErrorString(ce); delete ctx; (void)m2; return EDMD_ERR_CUDA; }
-  if (cudaMalloc(&ctx->work, sizeof(int32_t)) != cudaSuccess) { cudaFree(ctx->pool); delete ctx; return EDMD_ERR_CUDA; }
-  if (cudaMalloc(&ctx->ds, nsys * sizeof(SysDev)) != cudaSuccess) { cudaFree(ctx->pool); cudaFree(ctx->work); delete ctx; return EDMD_ERR_CUDA; }
+  ctx->total_N = TN; ctx->total_C = TC;
+  ctx->engine = g_engine;
+  if (ctx->engine == EDMD_ENGINE_AUTO) ctx->engine = nsys >= 64 ? EDMD_ENGINE_LANE : EDMD_ENGINE_WARP;
+  if (ctx->engine == EDMD_ENGINE_LANE && 2 * (int64_t)ctx->maxN + NSPECIAL > 65535)
+    return set_err(ctx, EDMD_ERR_ARG, "thread-per-system engine supports N <= 32766");
   CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
   CK(cudaEventCreate(&ctx->e0));
   CK(cudaEventCreate(&ctx->e1));
-  // ---- host-side staging of each system: cell lists (cellListInit src/EDMD.c:1906
-  // -> addToCell 2053: index order, push-front) and initial records
-  size_t base_disk = 0;
+  CK(dalloc(&ctx->d, TN)); CK(dalloc(&ctx->vr, TN));
+  CK(dalloc(&ctx->cx, TN)); CK(dalloc(&ctx->cy, TN)); CK(dalloc(&ctx->prv, TN));
+  CK(dalloc(&ctx->crossX, TN)); CK(dalloc(&ctx->crossY, TN));
+  CK(dalloc(&ctx->head, TC));
+  CK(dalloc(&ctx->ev, TE)); CK(dalloc(&ctx->on, TE)); CK(dalloc(&ctx->op, TE));
+  CK(dalloc(&ctx->tree, TT));
+  CK(dalloc(&ctx->st, nsys));
+  CK(dalloc(&ctx->trace, (size_t)nsys * trace_cap));
+  CK(dalloc(&ctx->rows, (size_t)nsys * rows_cap * 9));
+  CK(dalloc(&ctx->work, 1));
+  CK(dalloc(&ctx->ds, nsys));
+  if (ctx->engine == EDMD_ENGINE_LANE) {
+    CK(dalloc(&ctx->cal, (size_t)TN * CAL_SUB * CAL_LINE));
+    CK(dalloc(&ctx->mask, (size_t)TN));
+  }
   for (int s = 0; s < nsys; s++) {
     SysDev& S = ctx->hs[s];
-    const edmd_system_desc& D = desc[s];
-    const Box& B = S.B;
-    size_t N = D.N, E = 2 * N + NSPECIAL, C = (size_t)B.Nxc * B.Nyc;
-    char* p = ctx->pool + off[s];
-    auto take = [&](size_t bytes) { char* r = p; p += align_up(bytes, 256); return r; };
-    S.st = (SysState*)take(sizeof(SysState));
-    S.d = (Disk*)take(N * sizeof(Disk));
-    S.vr = (double*)take(N * 8);
-    S.cx = (int32_t*)take(N * 4); S.cy = (int32_t*)take(N * 4); S.prv = (int32_t*)take(N * 4);
-    S.crossX = (int32_t*)take(N * 4); S.crossY = (int32_t*)take(N * 4);
-    S.head = (int32_t*)take(C * 4);
-    S.ev = (Ev*)take(E * sizeof(Ev));
-    S.on = (int32_t*)take(E * 4); S.op = (int32_t*)take(E * 4);
-    size_t nodes = 0;
-    for (int h = 0; h < S.nlev; h++) nodes += S.lev_cnt[h];
-    S.tree = (Node*)take(nodes * sizeof(Node));
-    S.trace = trace_cap > 0 ? (void*)take((size_t)trace_cap * sizeof(edmd_collision)) : nullptr;
+    int64_t o = ctx->disk_off[s];
+    S.d = ctx->d + o; S.vr = ctx->vr + o;
+    S.cx = ctx->cx + o; S.cy = ctx->cy + o; S.prv = ctx->prv + o;
+    S.crossX = ctx->crossX + o; S.crossY = ctx->crossY + o;
+    S.head = ctx->head + ctx->cell_off[s];
+    S.ev = ctx->ev + ev_off[s]; S.on = ctx->on + ev_off[s]; S.op = ctx->op + ev_off[s];
+    S.tree = ctx->tree + node_off[s];
+    S.st = ctx->st + s;
+    S.trace = trace_cap > 0 ? (void*)(ctx->trace + (size_t)s * trace_cap) : nullptr;
     S.trace_cap = trace_cap;
-    S.rows = (double*)take((size_t)rows_cap * 9 * 8);
+    S.rows = ctx->rows + (size_t)s * rows_cap * 9;
     S.rows_cap = rows_cap;
-    std::vector<Disk> hd(N);
-    std::vector<int32_t> hcx(N), hcy(N), hprv(N), hhead(C, NIL), zero(N, 0);
-    std::vector<double> hvr(N, 0.0);
-    for (size_t i = 0; i < N; i++) {
-      size_t g = base_disk + i;
-      if (!(x[g] >= 0 && x[g] < D.Lx && y[g] >= 0 && y[g] < D.Ly)) {
-        ctx->err = "position outside the box";
-        edmd_destroy(ctx);
-        return EDMD_ERR_ARG;
-      }
-      Disk& q = hd[i];
-      q.x = x[g]; q.y = y[g]; q.vx = vx[g]; q.vy = vy[g]; q.tl = 0; q.rad = rad[g]; q.m = m[g];
-      q.coll = 0;
-      if (vr) hvr[i] = vr[g];
-      int X = (int)(q.x * B.cxf), Y = (int)(q.y * B.cyf);
-      if (X >= B.Nxc) X = B.Nxc - 1;
-      if (Y >= B.Nyc) Y = B.Nyc - 1;
-      hcx[i] = X; hcy[i] = Y; hprv[i] = NIL;
-      q.nxt = hhead[Y * B.Nxc + X];
-      hhead[Y * B.Nxc + X] = (int32_t)i;
-      if (q.nxt != NIL) hprv[q.nxt] = (int32_t)i;
+    if (ctx->engine == EDMD_ENGINE_LANE) {
+      S.cal = ctx->cal + (size_t)o * CAL_SUB * CAL_LINE;
+      S.mask = ctx->mask + o;
+      S.invw = CAL_SUB / S.B.dtP;
     }
-    base_disk += N;
-    SysState st;
-    memset(&st, 0, sizeof(st));
-    st.k = 0; st.next_wrap = N; st.ovf = NIL;
-    st.grow = D.t_growstop > 0 ? 1 : 0;
-    st.lastThermo = D.first_thermo + 0.000000001;   // addEventThermo(firstThermo + 1e-9)
-    st.collT[0] = D.t_growstop;                      // consumed by k_init_events
-    st.collT[1] = D.first_screen;
-    CK(cudaMemcpyAsync(S.st, &st, sizeof(st), cudaMemcpyHostToDevice, ctx->stream));
-    CK(cudaMemcpyAsync(S.d, hd.data(), N * sizeof(Disk), cudaMemcpyHostToDevice, ctx->stream));
-    CK(cudaMemcpyAsync(S.vr, hvr.data(), N * 8, cudaMemcpyHostToDevice, ctx->stream));
-    CK(cudaMemcpyAsync(S.cx, hcx.data(), N * 4, cudaMemcpyHostToDevice, ctx->stream));
-    CK(cudaMemcpyAsync(S.cy, hcy.data(), N * 4, cudaMemcpyHostToDevice, ctx->stream));
-    CK(cudaMemcpyAsync(S.prv, hprv.data(), N * 4, cudaMemcpyHostToDevice, ctx->stream));
-    CK(cudaMemcpyAsync(S.crossX, zero.data(), N * 4, cudaMemcpyHostToDevice, ctx->stream));
-    CK(cudaMemcpyAsync(S.crossY, zero.data(), N * 4, cudaMemcpyHostToDevice, ctx->stream));
-    CK(cudaMemcpyAsync(S.head, hhead.data(), C * 4, cudaMemcpyHostToDevice, ctx->stream));
-    CK(cudaStreamSynchronize(ctx->stream));   // staging vectors go out of scope
   }
   CK(cudaMemcpyAsync(ctx->ds, ctx->hs.data(), nsys * sizeof(SysDev), cudaMemcpyHostToDevice, ctx->stream));
-  for (int s = 0; s < nsys; s++) {
-    int N = ctx->hs[s].B.N;
-    k_init_events<<<(N + 1 + 127) / 128, 128, 0, ctx->stream>>>(ctx->ds, s);
-    k_init_finish<<<1, 32, 0, ctx->stream>>>(ctx->ds, s);
-    k_tree_build<<<1, 32, 0, ctx->stream>>>(ctx->ds, s);
-  }
-  CK(cudaGetLastError());
-  CK(cudaStreamSynchronize(ctx->stream));
-  for (int s = 0; s < nsys; s++) {
-    int32_t status = 0;
-    CK(cudaMemcpy(&status, &ctx->hs[s].st->status, 4, cudaMemcpyDeviceToHost));
-    if (status != EDMD_OK) {
-      ctx->err = "initial configuration has overlapping disks";
-      *out = ctx;
-      return status;
-    }
-  }
-  *out = ctx;
-  return EDMD_OK;
+  return stage_all(ctx, x, y, vx, vy, rad, m, vr, false);
+}
+
+extern "C" int edmd_load_state(edmd_ctx* ctx, const double* x, const double* y, const double* vx,
+                               const double* vy, const double* rad, const double* m) {
+  if (!ctx || !x || !y || !vx || !vy || !rad || !m) return EDMD_ERR_ARG;
+  return stage_all(ctx, x, y, vx, vy, rad, m, nullptr, true);
 }
 
 extern "C" int edmd_advance(edmd_ctx* ctx, int64_t max_coll, double t_stop, uint32_t flags,
@@ -957,34 +1031,37 @@ extern "C" int edmd_advance(edmd_ctx* ctx, int64_t max_coll, double t_stop, uint
   RunArgs A;
   A.max_coll = max_coll; A.t_stop = t_stop; A.flags = flags; A.max_events = max_events;
   A.nsys = ctx->nsys; A.work = ctx->work;
-  CK(cudaMemsetAsync(ctx->work, 0, sizeof(int32_t), ctx->stream));
-  int dev = 0, nsm = 0;
-  CK(cudaGetDevice(&dev));
-  CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-  int per_sm = 0;
-  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_run, 32 * WARPS_PER_BLOCK, 0));
-  int want = (ctx->nsys + WARPS_PER_BLOCK - 1) / WARPS_PER_BLOCK;
-  int grid = per_sm * nsm;
-  if (grid > want) grid = want;
-  if (grid < 1) grid = 1;
-  CK(cudaEventRecord(ctx->e0, ctx->stream));
-  k_run<<<grid, 32 * WARPS_PER_BLOCK, 0, ctx->stream>>>(ctx->ds, A);
+  if (ctx->engine == EDMD_ENGINE_LANE) {
+    CK(cudaEventRecord(ctx->e0, ctx->stream));
+    CK(lane_run_launch(ctx->ds, A, g_lane_threads, ctx->stream));
+  } else {
+    CK(cudaMemsetAsync(ctx->work, 0, sizeof(int32_t), ctx->stream));
+    int dev = 0, nsm = 0;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    int per_sm = 0;
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_run, 32 * WARPS_PER_BLOCK, 0));
+    int want = (ctx->nsys + WARPS_PER_BLOCK - 1) / WARPS_PER_BLOCK;
+    int grid = per_sm * nsm;
+    if (grid > want) grid = want;
+    if (grid < 1) grid = 1;
+    CK(cudaEventRecord(ctx->e0, ctx->stream));
+    k_run<<<grid, 32 * WARPS_PER_BLOCK, 0, ctx->stream>>>(ctx->ds, A);
+  }
   CK(cudaGetLastError());
   CK(cudaEventRecord(ctx->e1, ctx->stream));
   CK(cudaEventSynchronize(ctx->e1));
   if (elapsed_ms) CK(cudaEventElapsedTime(elapsed_ms, ctx->e0, ctx->e1));
-  int worst = EDMD_OK;
-  for (int s = 0; s < ctx->nsys; s++) {
-    int32_t st[2];
-    CK(cudaMemcpy(st, &ctx->hs[s].st->status, 8, cudaMemcpyDeviceToHost));
-    if (st[0] != EDMD_OK && worst == EDMD_OK) {
-      worst = st[0];
+  std::vector<int32_t> status(ctx->nsys);
+  CK(cudaMemcpy2D(status.data(), 4, &ctx->st[0].status, sizeof(SysState), 4, ctx->nsys,
+                  cudaMemcpyDeviceToHost));
+  for (int s = 0; s < ctx->nsys; s++)
+    if (status[s] != EDMD_OK) {
       char b[128];
-      snprintf(b, sizeof b, "system %d stopped with status %d", s, st[0]);
-      ctx->err = b;
+      snprintf(b, sizeof b, "system %d stopped with status %d", s, status[s]);
+      return set_err(ctx, status[s], b);
     }
-  }
-  return worst;
+  return EDMD_OK;
 }
 
 extern "C" int edmd_sync(edmd_ctx* ctx) {
@@ -1018,6 +1095,20 @@ extern "C" int edmd_get_state(edmd_ctx* ctx, int32_t s, double* x, double* y, do
   return EDMD_OK;
 }
 
+extern "C" int edmd_get_states(edmd_ctx* ctx, double* x, double* y, double* vx, double* vy,
+                               double* rad, double* m) {
+  if (!ctx) return EDMD_ERR_ARG;
+  const int64_t TN = ctx->total_N;
+  if (!ctx->stage) CK(dalloc(&ctx->stage, 6 * TN));
+  k_gather<<<(unsigned)((TN + 255) / 256), 256, 0, ctx->stream>>>(ctx->d, TN, ctx->stage);
+  CK(cudaGetLastError());
+  double* outs[6] = {x, y, vx, vy, rad, m};
+  for (int k = 0; k < 6; k++)
+    if (outs[k]) CK(cudaMemcpyAsync(outs[k], ctx->stage + k * TN, TN * 8, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return EDMD_OK;
+}
+
 extern "C" int edmd_get_counters(edmd_ctx* ctx, int32_t s, edmd_counters* out) {
   if (!ctx || s < 0 || s >= ctx->nsys || !out) return EDMD_ERR_ARG;
   SysState R;
@@ -1025,6 +1116,19 @@ extern "C" int edmd_get_counters(edmd_ctx* ctx, int32_t s, edmd_counters* out) {
   out->ncol = R.ncol; out->ncol_total = R.ncol_total; out->ncross = R.ncross;
   out->nstale = R.nstale; out->npair = R.npair; out->npred = R.npred; out->nevents = R.nevents;
   out->t = R.t; out->growing = R.grow; out->stop_reason = R.stop_reason;
+  return EDMD_OK;
+}
+
+extern "C" int edmd_get_all_counters(edmd_ctx* ctx, edmd_counters* out) {
+  if (!ctx || !out) return EDMD_ERR_ARG;
+  std::vector<SysState> R(ctx->nsys);
+  CK(cudaMemcpy(R.data(), ctx->st, ctx->nsys * sizeof(SysState), cudaMemcpyDeviceToHost));
+  for (int s = 0; s < ctx->nsys; s++) {
+    edmd_counters& o = out[s];
+    o.ncol = R[s].ncol; o.ncol_total = R[s].ncol_total; o.ncross = R[s].ncross;
+    o.nstale = R[s].nstale; o.npair = R[s].npair; o.npred = R[s].npred; o.nevents = R[s].nevents;
+    o.t = R[s].t; o.growing = R[s].grow; o.stop_reason = R[s].stop_reason;
+  }
   return EDMD_OK;
 }
 
@@ -1060,17 +1164,36 @@ extern "C" int edmd_get_trace(edmd_ctx* ctx, int32_t s, edmd_collision* out, int
   return (int64_t)nt > S.trace_cap ? EDMD_ERR_CAPACITY : EDMD_OK;
 }
 
+extern "C" int edmd_set_device(int32_t dev) {
+  return cudaSetDevice(dev) == cudaSuccess ? EDMD_OK : EDMD_ERR_CUDA;
+}
+
+extern "C" int edmd_host_alloc(void** p, int64_t bytes) {
+  if (!p || bytes <= 0) return EDMD_ERR_ARG;
+  return cudaMallocHost(p, (size_t)bytes) == cudaSuccess ? EDMD_OK : EDMD_ERR_CUDA;
+}
+
+extern "C" int edmd_host_free(void* p) {
+  return cudaFreeHost(p) == cudaSuccess ? EDMD_OK : EDMD_ERR_CUDA;
+}
+
 extern "C" int edmd_destroy(edmd_ctx* ctx) {
   if (!ctx) return EDMD_OK;
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
-  if (ctx->pool) cudaFree(ctx->pool);
-  if (ctx->work) cudaFree(ctx->work);
-  if (ctx->ds) cudaFree(ctx->ds);
+  void* ptrs[] = {ctx->d, ctx->vr, ctx->cx, ctx->cy, ctx->prv, ctx->crossX, ctx->crossY, ctx->head,
+                  ctx->ev, ctx->on, ctx->op, ctx->tree, ctx->st, ctx->trace, ctx->rows, ctx->stage,
+                  ctx->work, ctx->ds, ctx->cal, ctx->mask};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
   if (ctx->e0) cudaEventDestroy(ctx->e0);
   if (ctx->e1) cudaEventDestroy(ctx->e1);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
   return EDMD_OK;
+}
+
+extern "C" int edmd_get_engine(const edmd_ctx* ctx) {
+  return ctx ? ctx->engine : -1;
 }
 
 extern "C" const char* edmd_last_error(const edmd_ctx* ctx) {

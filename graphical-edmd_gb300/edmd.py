@@ -22,6 +22,7 @@ LIB_PATH = os.path.join(HERE, "libedmd_gpu.so")
 OK, ERR_ARG, ERR_CUDA, ERR_OVERLAP, ERR_BUDGET, ERR_CAPACITY, ERR_NODEV = range(7)
 STOP_COLL, STOP_TIME, STOP_TMAX, STOP_SCREEN, STOP_GROW = 1, 2, 3, 4, 5
 F_STOP_AT_SCREEN, F_STOP_AT_GROW, F_TRACE, F_COUNT_NORMAL = 1, 2, 4, 8
+ENGINE_AUTO, ENGINE_WARP, ENGINE_LANE = 0, 1, 2
 
 
 class SystemDesc(C.Structure):
@@ -49,9 +50,11 @@ class Counters(C.Structure):
 
 # every symbol the public headers declare, in declaration order
 EXPORTS = [
-    "edmd_create", "edmd_advance", "edmd_sync", "edmd_get_state", "edmd_get_counters",
-    "edmd_get_virial", "edmd_get_thermo", "edmd_get_trace", "edmd_destroy", "edmd_last_error",
-    "edmd_device_info",
+    "edmd_create", "edmd_load_state", "edmd_advance", "edmd_sync", "edmd_get_state",
+    "edmd_get_states", "edmd_get_counters", "edmd_get_all_counters", "edmd_get_virial",
+    "edmd_get_thermo", "edmd_get_trace", "edmd_set_engine", "edmd_set_lane_threads",
+    "edmd_get_engine", "edmd_set_device", "edmd_host_alloc", "edmd_host_free", "edmd_destroy",
+    "edmd_last_error", "edmd_device_info",
     "edmd_mt_seed", "edmd_mt_u32", "edmd_mt_double", "edmd_hex_size", "edmd_random_size",
     "edmd_grow_rate", "edmd_normalize", "edmd_init_hex", "edmd_init_grow", "edmd_default_desc",
 ]
@@ -74,6 +77,15 @@ def load(path=LIB_PATH):
                               C.c_void_p, C.c_int64, C.POINTER(C.c_void_p)]
     L.edmd_advance.argtypes = [C.c_void_p, C.c_int64, C.c_double, C.c_uint32, C.c_int64,
                                C.POINTER(C.c_float)]
+    L.edmd_load_state.argtypes = [C.c_void_p] + [C.c_void_p] * 6
+    L.edmd_get_states.argtypes = [C.c_void_p] + [C.c_void_p] * 6
+    L.edmd_get_all_counters.argtypes = [C.c_void_p, C.c_void_p]
+    L.edmd_host_alloc.argtypes = [C.POINTER(C.c_void_p), C.c_int64]
+    L.edmd_host_free.argtypes = [C.c_void_p]
+    L.edmd_set_device.argtypes = [C.c_int32]
+    L.edmd_set_engine.argtypes = [C.c_int32]
+    L.edmd_set_lane_threads.argtypes = [C.c_int32]
+    L.edmd_get_engine.argtypes = [C.c_void_p]
     L.edmd_sync.argtypes = [C.c_void_p]
     L.edmd_get_state.argtypes = [C.c_void_p, C.c_int32] + [C.c_void_p] * 8
     L.edmd_get_counters.argtypes = [C.c_void_p, C.c_int32, C.POINTER(Counters)]
@@ -155,9 +167,11 @@ def default_desc(N, Lx, Ly, vr_base=0.0, tmax=4000.0, dtime=100.0, dtime_thermo=
 class Engine:
     """A set of independent systems on the GPU (one edmd_ctx)."""
 
-    def __init__(self, systems, trace_cap=0):
+    def __init__(self, systems, trace_cap=0, engine=ENGINE_AUTO, lane_threads=32):
         """systems: list of dicts with N, x, y, vx, vy, rad, m, [vr] and 'desc'."""
         L = load()
+        L.edmd_set_engine(engine)
+        L.edmd_set_lane_threads(lane_threads)
         self._L = L
         n = len(systems)
         descs = (SystemDesc * n)(*[s["desc"] for s in systems])
@@ -180,6 +194,10 @@ class Engine:
             msg = self.last_error()
             self.close()
             raise EngineError(rc, msg)
+
+    @property
+    def engine(self):
+        return self._L.edmd_get_engine(self.h)
 
     def last_error(self):
         return self._L.edmd_last_error(self.h).decode()
@@ -209,6 +227,24 @@ class Engine:
         out["cell"] = cell
         out["coll"] = coll
         return out
+
+    def load_state(self, x, y, vx, vy, rad, m):
+        """Restart every system from concatenated host arrays (-l semantics)."""
+        self._ck(self._L.edmd_load_state(self.h, *[_ptr(np.ascontiguousarray(a, np.float64))
+                                                   for a in (x, y, vx, vy, rad, m)]))
+
+    def states(self, out=None):
+        """x, y, vx, vy, rad, m of every system, concatenated (optionally into `out`)."""
+        T = sum(self.N)
+        if out is None:
+            out = {k: np.zeros(T) for k in ("x", "y", "vx", "vy", "rad", "m")}
+        self._ck(self._L.edmd_get_states(self.h, *[_ptr(out[k]) for k in ("x", "y", "vx", "vy", "rad", "m")]))
+        return out
+
+    def all_counters(self):
+        arr = (Counters * self.n)()
+        self._ck(self._L.edmd_get_all_counters(self.h, C.cast(arr, C.c_void_p)))
+        return {k: np.array([getattr(c, k) for c in arr]) for k, _ in Counters._fields_}
 
     def counters(self, s=0):
         c = Counters()
@@ -247,6 +283,23 @@ class Engine:
             self.close()
         except Exception:
             pass
+
+
+class PinnedArray:
+    """float64 array in page-locked host memory (edmd_host_alloc)."""
+
+    def __init__(self, n):
+        self._p = C.c_void_p()
+        rc = load().edmd_host_alloc(C.byref(self._p), max(int(n), 1) * 8)
+        if rc != OK:
+            raise EngineError(rc, "edmd_host_alloc failed")
+        buf = (C.c_double * max(int(n), 1)).from_address(self._p.value)
+        self.a = np.ctypeslib.as_array(buf)[: int(n)]
+
+    def free(self):
+        if self._p.value:
+            load().edmd_host_free(self._p)
+            self._p = C.c_void_p()
 
 
 def device_info():

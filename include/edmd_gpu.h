@@ -45,6 +45,11 @@ extern "C" {
 #define EDMD_STOP_SCREEN    4   /* stopped right after a screenshot           */
 #define EDMD_STOP_GROW      5   /* stopped right after the growth stop        */
 
+/* engines (edmd_set_engine) */
+#define EDMD_ENGINE_AUTO    0   /* lane engine for >= 64 systems, else warp  */
+#define EDMD_ENGINE_WARP    1   /* one warp per system: single large systems  */
+#define EDMD_ENGINE_LANE    2   /* one thread per system: large batches, N <= 32766 */
+
 /* edmd_advance flags */
 #define EDMD_F_STOP_AT_SCREEN  1u  /* return after each screenshot event      */
 #define EDMD_F_STOP_AT_GROW    2u  /* return after the growth-stop event      */
@@ -95,11 +100,19 @@ typedef struct edmd_ctx edmd_ctx;
  * src/EDMD.c:1906 and eventListInit src/EDMD.c:1935).  Arrays hold the sum
  * of desc[k].N entries.  `vr` (growth rate per disk) may be NULL for direct
  * starts.  Positions must lie in [0,L).  trace_cap is the per-system
- * capacity of the collision trace (0 disables tracing). */
+ * capacity of the collision trace (0 disables tracing).  *out is set even when
+ * the call fails, so that edmd_last_error can be read; destroy it either way. */
 int edmd_create(int32_t nsys, const edmd_system_desc* desc,
                 const double* x, const double* y, const double* vx, const double* vy,
                 const double* rad, const double* m, const double* vr,
                 int64_t trace_cap, edmd_ctx** out);
+
+/* Restart every system from host state (the -l load path, particlesInit
+ * src/EDMD.c:1366-1451 + cellListInit + eventListInit): clocks, counters and
+ * queues are rebuilt, the normal phase is used, the first screenshot is at
+ * t = 1 and the first thermo at t = 1000 (src/EDMD.c:244-247). */
+int edmd_load_state(edmd_ctx* ctx, const double* x, const double* y, const double* vx,
+                    const double* vy, const double* rad, const double* m);
 
 /* Advance every system (replaces the loop body src/EDMD.c:523-618).  Each
  * system stops on its own at max_coll accepted collisions of this call, at
@@ -118,7 +131,13 @@ int edmd_sync(edmd_ctx* ctx);
 int edmd_get_state(edmd_ctx* ctx, int32_t sys, double* x, double* y, double* vx,
                    double* vy, double* rad, double* m, int32_t* cell, uint32_t* coll);
 
+/* The state of every system, concatenated in system order (one gather
+ * kernel and one copy per array; any pointer may be NULL). */
+int edmd_get_states(edmd_ctx* ctx, double* x, double* y, double* vx, double* vy,
+                    double* rad, double* m);
+
 int edmd_get_counters(edmd_ctx* ctx, int32_t sys, edmd_counters* out);
+int edmd_get_all_counters(edmd_ctx* ctx, edmd_counters* out);   /* nsys entries */
 
 /* Collision-virial accumulators collTermX, collTermY, collTermXY, collTermYX
  * (src/EDMD.c:3809-3817) of one system; reset them if `reset`. */
@@ -130,6 +149,21 @@ int edmd_get_thermo(edmd_ctx* ctx, int32_t sys, double* rows, int32_t cap, int32
 
 /* Collision trace of one system recorded since creation (EDMD_F_TRACE). */
 int edmd_get_trace(edmd_ctx* ctx, int32_t sys, edmd_collision* out, int64_t cap, int64_t* n);
+
+/* Engine used by contexts created afterwards (default EDMD_ENGINE_AUTO) and
+ * the block size of the thread-per-system engine.  Both engines pop events in
+ * the reference's exact order and give bit-identical results. */
+int edmd_set_engine(int32_t kind);
+int edmd_set_lane_threads(int32_t threads_per_block);
+int edmd_get_engine(const edmd_ctx* ctx);
+
+/* Select the CUDA device used by contexts created afterwards in this thread
+ * (one process per GPU). */
+int edmd_set_device(int32_t dev);
+
+/* Page-locked host buffers for fast host<->device staging. */
+int edmd_host_alloc(void** p, int64_t bytes);
+int edmd_host_free(void* p);
 
 int edmd_destroy(edmd_ctx* ctx);
 const char* edmd_last_error(const edmd_ctx* ctx);

@@ -1,0 +1,31 @@
+"""The drop-in driver writes the reference's dump and thermo files byte for byte.
+
+tests/golden/files_hex64.{dump,thermo} were written by the reference's own
+saveTXT / saveThermo (tests/golden/make_golden.py).  The driver runs the same
+command line on the GPU; since the trajectory is bit-identical, the text
+files must be identical too (134,574 collisions, 12 frames, 5 thermo rows).
+"""
+import glob
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, PKG
+
+pytestmark = pytest.mark.gpu
+
+
+def test_dump_and_thermo_files_identical(built, tmp_path):
+    g = dict(np.load(os.path.join(GOLDEN, "files_hex64.npz")))
+    args = str(g["args"]).split()
+    exe = os.path.join(PKG, "edmd")
+    r = subprocess.run([exe] + args + ["--quiet"], cwd=tmp_path, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 1, r.stderr          # the reference's main returns 1
+    dumps = glob.glob(str(tmp_path / "dump" / "*.dump"))
+    thermos = glob.glob(str(tmp_path / "dump" / "*.thermo"))
+    assert len(dumps) == 1 and len(thermos) == 1
+    assert os.path.basename(dumps[0]).startswith("N_64res_1.000phi_0.500000q_0.000rat_0.400Lx_")
+    assert open(dumps[0]).read() == open(os.path.join(GOLDEN, "files_hex64.dump")).read()
+    assert open(thermos[0]).read() == open(os.path.join(GOLDEN, "files_hex64.thermo")).read()

@@ -52,17 +52,23 @@ def check_against_golden(eng, s, g):
         np.testing.assert_array_equal(st["rad"], g["radf"])
 
 
+ENGINES = [("warp", 1), ("lane", 2)]
+
+
+@pytest.mark.parametrize("engine", ENGINES, ids=[e[0] for e in ENGINES])
 @pytest.mark.parametrize("name", golden_names())
-def test_single_system_matches_reference(edmd, name):
+def test_single_system_matches_reference(edmd, name, engine):
     g = golden(name)
-    eng = edmd.Engine([system_from_golden(edmd, g)], trace_cap=len(g["ct"]) + 16)
+    eng = edmd.Engine([system_from_golden(edmd, g)], trace_cap=len(g["ct"]) + 16, engine=engine[1])
+    assert eng.engine == engine[1]
     rc, ms = eng.advance(max_coll=len(g["ct"]), flags=edmd.F_TRACE)
     eng.sync()
     check_against_golden(eng, 0, g)
     eng.close()
 
 
-def test_batched_systems_match_reference(edmd):
+@pytest.mark.parametrize("engine", ENGINES, ids=[e[0] for e in ENGINES])
+def test_batched_systems_match_reference(edmd, engine):
     """Several systems of different N in one launch, each replicated 3 times."""
     by_len = {}
     for n in golden_names():
@@ -70,7 +76,7 @@ def test_batched_systems_match_reference(edmd):
         by_len.setdefault(len(g["ct"]), []).append(g)
     for L, gs in sorted(by_len.items()):
         systems = [system_from_golden(edmd, g) for g in gs] * 3
-        eng = edmd.Engine(systems, trace_cap=L + 16)
+        eng = edmd.Engine(systems, trace_cap=L + 16, engine=engine[1])
         eng.advance(max_coll=L, flags=edmd.F_TRACE)
         eng.sync()
         for s in range(len(systems)):
