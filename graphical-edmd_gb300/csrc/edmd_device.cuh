@@ -39,13 +39,22 @@ struct __align__(32) Ev {
   uint32_t st;     // ST_*
 };
 
-// tournament-tree node: the minimum key of its subtree and the leaf holding it
+// tournament-tree node: the minimum key of its subtree and the leaf holding it;
+// the time is held as its order-preserving integer image (time_key) so that
+// tree comparisons run on the integer pipe
 struct Node {
-  double t;
+  uint64_t tk;
   uint64_t tie;
   uint32_t b;
   int32_t idx;
 };
+
+// order-preserving integer image of a double (non-NaN; -0 orders as +0)
+__device__ __forceinline__ uint64_t time_key(double t) {
+  uint64_t u = (uint64_t)__double_as_longlong(t);
+  if (u == 0x8000000000000000ull) u = 0;
+  return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
+}
 
 struct Box {
   double Lx, Ly, hLx, hLy;     // box and halves (boxConstantHelper src/EDMD.c:679)
@@ -86,13 +95,14 @@ struct SysDev {
   double* rows;                // thermo rows, 9 doubles each
   int32_t rows_cap, pad;
   // calendar of the thread-per-system engine (edmd_lane.cu)
-  uint16_t* cal;               // N buckets x CAL_SUB lines of CAL_LINE u16: [count, ids...]
-  uint8_t* mask;               // per bucket: bit k set when sub-bucket k is non-empty
+  uint16_t* cal;               // N buckets x CAL_SUB lines of CAL_LINE u16, see edmd_lane.cu
+  uint16_t* mask;              // per bucket: bit k set when sub-bucket k is non-empty
   double invw;                 // CAL_SUB / dtP
+  double rdtP;                 // 1 / dtP
 };
 
-constexpr int CAL_SUB = 8;     // sub-buckets per calendar bucket (ordered by time)
-constexpr int CAL_LINE = 32;   // u16 per sub-bucket line: a count and up to 31 event ids
+constexpr int CAL_SUB = 16;    // sub-buckets per calendar bucket (ordered by time)
+constexpr int CAL_LINE = 32;   // u16 per sub-bucket line: count, 29 ids, spill-list head
 
 struct RunArgs {
   int64_t max_coll;
@@ -198,12 +208,96 @@ __device__ __forceinline__ double crossing_time(const Box& B, const Disk& p, int
   return t + ty;
 }
 
-__device__ __forceinline__ bool key_less(uint32_t b1, double t1, uint64_t k1, int32_t i1,
-                                         uint32_t b2, double t2, uint64_t k2, int32_t i2) {
+// Comparisons against a positive constant on the integer pipe.  For finite a
+// and c > 0 these are exactly the IEEE comparisons (including -0 and +0):
+//   ge_pos(a, c) == (a >= c),  lt_neg(a, c) == (a < -c),  is_neg(a) == (a < 0),
+//   is_pos(a) == (a > 0).  FP64 compares issue on GB300's narrow FP64 pipe.
+__device__ __forceinline__ bool ge_pos(double a, double c) {
+  return __double_as_longlong(a) >= __double_as_longlong(c);
+}
+__device__ __forceinline__ bool lt_neg(double a, double c) {
+  long long ia = __double_as_longlong(a);
+  return ia < 0 && (ia & 0x7fffffffffffffffll) > __double_as_longlong(c);
+}
+__device__ __forceinline__ bool is_neg(double a) {
+  long long ia = __double_as_longlong(a);
+  return ia < 0 && (ia & 0x7fffffffffffffffll) != 0;
+}
+__device__ __forceinline__ bool is_pos(double a) { return __double_as_longlong(a) > 0; }
+
+// pbc / pbc_in / free flight with integer-pipe comparisons (same results)
+__device__ __forceinline__ void pbc_i(const Box& B, double& dx, double& dy) {
+  if (ge_pos(dx, B.hLx)) dx -= B.Lx;
+  else if (lt_neg(dx, B.hLx)) dx += B.Lx;
+  if (ge_pos(dy, B.hLy)) dy -= B.Ly;
+  else if (lt_neg(dy, B.hLy)) dy += B.Ly;
+}
+__device__ __forceinline__ void free_fly_i(const Box& B, Disk& p, double t) {
+  double dt = t - p.tl;
+  p.tl = t;
+  p.x += dt * p.vx;
+  p.y += dt * p.vy;
+  if (is_neg(p.x)) p.x += B.Lx;
+  else if (ge_pos(p.x, B.Lx)) p.x -= B.Lx;
+  if (is_neg(p.y)) p.y += B.Ly;
+  else if (ge_pos(p.y, B.Ly)) p.y -= B.Ly;
+}
+// collisionTimeNormal (src/EDMD.c:2661-2723), same operations as
+// coll_time_normal with the tests on the integer pipe
+__device__ __forceinline__ double coll_time_normal_i(const Box& B, const Disk& p1, const Disk& p2,
+                                                     double t, bool* overlap) {
+  double lat2 = t - p2.tl;
+  double dvx = p2.vx - p1.vx;
+  double dvy = p2.vy - p1.vy;
+  double dx = (p2.x + lat2 * p2.vx) - p1.x;
+  double dy = (p2.y + lat2 * p2.vy) - p1.y;
+  pbc_i(B, dx, dy);
+  double b = dx * dvx + dy * dvy;
+  if (is_pos(b)) return NEVER;
+  double v2 = dvx * dvx + dvy * dvy;
+  double d2 = dx * dx + dy * dy - 4 * p1.rad * p2.rad;
+  double det = b * b - v2 * d2;
+  if (lt_neg(d2, 0.01)) { *overlap = true; return NEVER; }
+  if (is_neg(det)) return NEVER;
+  return (-b - sqrt(det)) / v2;
+}
+
+__device__ __forceinline__ bool key_less(uint32_t b1, uint64_t t1, uint64_t k1, int32_t i1,
+                                         uint32_t b2, uint64_t t2, uint64_t k2, int32_t i2) {
   if (b1 != b2) return b1 < b2;
   if (t1 != t2) return t1 < t2;
   if (k1 != k2) return k1 < k2;
   return i1 < i2;
+}
+
+// crossingEventNormal (src/EDMD.c:2405-2482) with the sign and periodic tests
+// on the integer pipe; same operations and results as crossing_time
+__device__ __forceinline__ double crossing_time_i(const Box& B, const Disk& p, int cx, int cy,
+                                                  double t, int* dir) {
+  double tx, ty, a;
+  int xx, yy;
+  if (is_neg(p.vx)) { a = cx * B.cxs - p.x; xx = 1; }
+  else { a = (1 + cx) * B.cxs - p.x; xx = 2; }
+  if (ge_pos(a, B.hLx)) a = a - B.Lx; else if (lt_neg(a, B.hLx)) a = a + B.Lx;
+  tx = a / p.vx;
+  if (is_neg(p.vy)) { a = cy * B.cys - p.y; yy = 3; }
+  else { a = (1 + cy) * B.cys - p.y; yy = 4; }
+  if (ge_pos(a, B.hLy)) a = a - B.Ly; else if (lt_neg(a, B.hLy)) a = a + B.Ly;
+  ty = a / p.vy;
+  if (tx < ty) { *dir = xx; return t + tx; }
+  *dir = yy;
+  return t + ty;
+}
+
+// (int)(dt / dtP) of addEventToQueue without the FP64 division when provably
+// equal: |dt*rdtP - fl(dt/dtP)| <= 3*q*2^-53 < 1e-9 for q < 2^22, so the floor
+// is unchanged unless q is within 1e-9 of an integer (then divide exactly)
+__device__ __forceinline__ int bucket_offset(double dt, double dtP, double rdtP) {
+  double q = dt * rdtP;
+  int d = (int)q;
+  double fr = q - (double)d;
+  if (fr > 1e-9 && fr < 1.0 - 1e-9) return d;
+  return (int)(dt / dtP);
 }
 
 }  // namespace edmd

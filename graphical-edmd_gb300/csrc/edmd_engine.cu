@@ -49,19 +49,19 @@ struct WarpSmem {
 };
 
 __device__ __forceinline__ Node empty_node(int idx) {
-  Node n; n.t = __longlong_as_double(0x7ff0000000000000ll); n.tie = ~0ull; n.b = BINF; n.idx = idx;
+  Node n; n.tk = ~0ull; n.tie = ~0ull; n.b = BINF; n.idx = idx;
   return n;
 }
 
 __device__ __forceinline__ bool node_less(const Node& a, const Node& b) {
-  return key_less(a.b, a.t, a.tie, a.idx, b.b, b.t, b.tie, b.idx);
+  return key_less(a.b, a.tk, a.tie, a.idx, b.b, b.tk, b.tie, b.idx);
 }
 
 __device__ __forceinline__ void warp_min(Node& n) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     Node m;
-    m.t = __shfl_xor_sync(FULL, n.t, o);
+    m.tk = __shfl_xor_sync(FULL, n.tk, o);
     m.tie = __shfl_xor_sync(FULL, n.tie, o);
     m.b = __shfl_xor_sync(FULL, n.b, o);
     m.idx = __shfl_xor_sync(FULL, n.idx, o);
@@ -70,7 +70,7 @@ __device__ __forceinline__ void warp_min(Node& n) {
 }
 
 __device__ __forceinline__ Node ev_node(const Ev& e, int idx) {
-  Node n; n.t = e.t; n.tie = e.tie; n.b = e.b; n.idx = idx;
+  Node n; n.tk = time_key(e.t); n.tie = e.tie; n.b = e.b; n.idx = idx;
   return n;
 }
 
@@ -89,7 +89,9 @@ __device__ void leaf_update(const SysDev& S, int leaf, int lane) {
   if (lane == 0) S.tree[leaf] = n;
   __syncwarp();
   int idx = leaf;
-  for (int h = 1; h < S.nlev; h++) {
+#pragma unroll
+  for (int h = 1; h < MAXLEV; h++) {
+    if (h >= S.nlev) break;
     int par = idx >> 5;
     int ch = (par << 5) + lane;
     Node c = ch < S.lev_cnt[h - 1] ? S.tree[S.lev_off[h - 1] + ch] : empty_node(0x7fffffff);
@@ -116,7 +118,9 @@ __device__ void tree_rebuild(const SysDev& S, int lane) {
     S.tree[l] = n;
   }
   __syncwarp();
-  for (int h = 1; h < S.nlev; h++) {
+#pragma unroll
+  for (int h = 1; h < MAXLEV; h++) {
+    if (h >= S.nlev) break;
     for (int par = 0; par < S.lev_cnt[h]; par++) {
       int ch = (par << 5) + lane;
       Node c = ch < S.lev_cnt[h - 1] ? S.tree[S.lev_off[h - 1] + ch] : empty_node(0x7fffffff);
@@ -137,9 +141,9 @@ __device__ void schedule(const SysDev& S, SysState& R, int e, double T, int32_t 
   Ev ev;
   ev.t = T; ev.j = j; ev.ca = ca;
   double dt = T - R.P;
-  if (dt < B.dtP) {
+  if (!ge_pos(dt, B.dtP)) {                    // dt < dtPaul
     ev.b = (uint32_t)R.k; ev.tie = (cls_direct << 62) | R.C; ev.st = ST_QUEUED;
-  } else if (dt >= B.dtPN) {
+  } else if (ge_pos(dt, B.dtPN)) {             // dt >= dtPaul * N
     ev.b = BINF; ev.tie = R.C; ev.st = ST_OVF;
     if (lane == 0) {
       S.on[e] = R.ovf; S.op[e] = NIL;
@@ -147,7 +151,7 @@ __device__ void schedule(const SysDev& S, SysState& R, int e, double T, int32_t 
     }
     R.ovf = e;
   } else {
-    int d = (int)(dt / B.dtP);
+    int d = bucket_offset(dt, B.dtP, S.rdtP);
     ev.b = (uint32_t)(R.k + (uint64_t)d); ev.tie = (1ull << 62) | (TIE_MAX - R.C); ev.st = ST_QUEUED;
   }
   R.C++;
@@ -196,19 +200,20 @@ struct Pred { double dt; int32_t partner; uint32_t ca; };
 
 __device__ __forceinline__ void grow_fly(const SysDev& S, Disk& p, int i, double t, bool grow) {
   double dt = t - p.tl;
-  free_fly(S.B, p, t);
+  free_fly_i(S.B, p, t);
   if (grow) p.rad += dt * S.vr[i];
 }
 
 __device__ __forceinline__ double pair_time(const SysDev& S, const Disk& A, int a, const Disk& P,
                                             int p, double t, bool grow, bool* ovl) {
   if (grow) return coll_time_grow(S.B, A, S.vr[a], P, S.vr[p], t, ovl);
-  return coll_time_normal(S.B, A, P, t, ovl);
+  return coll_time_normal_i(S.B, A, P, t, ovl);
 }
 
 __device__ __forceinline__ void best_merge(double& bd, int& bo, int& bp, uint32_t& bc,
                                            double d, int o, int p, uint32_t c) {
-  if (d < bd || (d == bd && o < bo)) { bd = d; bo = o; bp = p; bc = c; }
+  uint64_t kd = time_key(d), kb = time_key(bd);
+  if (kd < kb || (kd == kb && o < bo)) { bd = d; bo = o; bp = p; bc = c; }
 }
 
 // collisionEventNormal / Grow (src/EDMD.c:2829 / 3104) for disks a0 and a1
@@ -433,7 +438,7 @@ __device__ void do_growstop(const SysDev& S, SysState& R, int lane, WarpSmem* sm
     unqueue(S, R, i, lane);
     int dir;
     Disk p = S.d[i];
-    double tc = crossing_time(S.B, p, S.cx[i], S.cy[i], R.t, &dir);
+    double tc = crossing_time_i(S.B, p, S.cx[i], S.cy[i], R.t, &dir);
     schedule(S, R, i, tc, dir, 0, 2ull, lane);
     __syncwarp();
   }
@@ -475,7 +480,7 @@ __device__ void run_system(const SysDev& S, const RunArgs& A, int lane, WarpSmem
     int leaf = r.idx, e;
     if (leaf < N) {
       Ev e0 = S.ev[leaf];
-      e = (e0.st == ST_QUEUED && e0.b == r.b && e0.t == r.t && e0.tie == r.tie) ? leaf : N + leaf;
+      e = (e0.st == ST_QUEUED && e0.b == r.b && time_key(e0.t) == r.tk && e0.tie == r.tie) ? leaf : N + leaf;
     } else {
       e = 2 * N + (leaf - N);
     }
@@ -519,11 +524,13 @@ __device__ void run_system(const SysDev& S, const RunArgs& A, int lane, WarpSmem
         double dx = dj.x - di.x, dy = dj.y - di.y;
         double dvx = dj.vx - di.vx, dvy = dj.vy - di.vy;
         if (!grow) {   // elastic branch src/EDMD.c:3802-3827
-          double invMass = 1 / (di.m + dj.m);
-          pbc(B, dx, dy);
+          // 1/(1+1) and x/4 are exact, so these shortcuts round identically
+          double msum = di.m + dj.m;
+          double invMass = msum == 2.0 ? 0.5 : 1 / msum;
+          pbc_i(B, dx, dy);
           double collKernel = invMass * (1 + S.res) * (dx * dvx + dy * dvy);
           double distSquared = 4 * di.rad * dj.rad;
-          double f = collKernel / distSquared;
+          double f = distSquared == 4.0 ? collKernel * 0.25 : collKernel / distSquared;
           double ct = di.m * dj.m * f;
           R.collT[0] += ct * dx * dx;
           R.collT[1] += ct * dy * dy;
@@ -552,8 +559,8 @@ __device__ void run_system(const SysDev& S, const RunArgs& A, int lane, WarpSmem
         unqueue(S, R, i, lane);
         unqueue(S, R, j, lane);
         int diri, dirj;
-        double tci = crossing_time(B, di, S.cx[i], S.cy[i], R.t, &diri);
-        double tcj = crossing_time(B, dj, S.cx[j], S.cy[j], R.t, &dirj);
+        double tci = crossing_time_i(B, di, S.cx[i], S.cy[i], R.t, &diri);
+        double tcj = crossing_time_i(B, dj, S.cx[j], S.cy[j], R.t, &dirj);
         schedule(S, R, i, tci, diri, 0, 2ull, lane);
         schedule(S, R, j, tcj, dirj, 0, 2ull, lane);
         unqueue(S, R, N + j, lane);
@@ -600,7 +607,7 @@ __device__ void run_system(const SysDev& S, const RunArgs& A, int lane, WarpSmem
       }
       __syncwarp();
       int dir;
-      double tc = crossing_time(B, di, cx, cy, R.t, &dir);
+      double tc = crossing_time_i(B, di, cx, cy, R.t, &dir);
       schedule(S, R, i, tc, dir, 0, 2ull, lane);
       unqueue(S, R, N + i, lane);
       __syncwarp();
@@ -799,7 +806,7 @@ struct edmd_ctx {
   double* stage = nullptr;          // SoA gather buffer (6 x total_N)
   int32_t* work = nullptr;
   uint16_t* cal = nullptr;          // calendars of the thread-per-system engine
-  uint8_t* mask = nullptr;
+  uint16_t* mask = nullptr;
   int engine = 0;                   // EDMD_ENGINE_WARP or EDMD_ENGINE_LANE
   int64_t total_C = 0;
   std::string err;
@@ -918,8 +925,9 @@ static int stage_all(edmd_ctx* ctx, const double* x, const double* y, const doub
                   cudaMemcpyDeviceToHost));
   for (int s = 0; s < ctx->nsys; s++)
     if (status[s] != EDMD_OK)
-      return set_err(ctx, status[s], "initial configuration of system " + std::to_string(s) +
-                                         " has overlapping disks");
+      return set_err(ctx, status[s], std::string("initial configuration of system ") + std::to_string(s) +
+                                         (status[s] == EDMD_ERR_OVERLAP ? " has overlapping disks"
+                                                                        : " could not be queued"));
   return EDMD_OK;
 }
 
@@ -956,6 +964,7 @@ extern "C" int edmd_create(int32_t nsys, const edmd_system_desc* desc, const dou
     B.cxf = 1 / B.cxs; B.cyf = 1 / B.cys;
     B.dtP = 5.0 / (double)D.N;
     B.dtPN = B.dtP * D.N;
+    S.rdtP = 1.0 / B.dtP;
     S.res = D.res; S.Einit = D.Einit; S.dtime = D.dtime; S.dtimeTh = D.dtime_thermo; S.tmax = D.tmax;
     S.L = D.N + NSPECIAL;
     int c = S.L;
@@ -973,7 +982,7 @@ extern "C" int edmd_create(int32_t nsys, const edmd_system_desc* desc, const dou
   }
   ctx->total_N = TN; ctx->total_C = TC;
   ctx->engine = g_engine;
-  if (ctx->engine == EDMD_ENGINE_AUTO) ctx->engine = nsys >= 64 ? EDMD_ENGINE_LANE : EDMD_ENGINE_WARP;
+  if (ctx->engine == EDMD_ENGINE_AUTO) ctx->engine = EDMD_ENGINE_WARP;
   if (ctx->engine == EDMD_ENGINE_LANE && 2 * (int64_t)ctx->maxN + NSPECIAL > 65535)
     return set_err(ctx, EDMD_ERR_ARG, "thread-per-system engine supports N <= 32766");
   CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));

@@ -23,11 +23,17 @@ namespace edmd {
 
 namespace {
 
-constexpr int CAP = CAL_LINE - 1;
+// A sub-bucket line is 64 bytes: u16 count, 29 u16 event ids, and the i32
+// head of a spill list that takes the events beyond 29 (many events can share
+// one time, e.g. disks of a lattice start sitting on cell edges).  The spill
+// list reuses the overflow links on/op: an event is never in both.
+constexpr int CAP = 29;
+constexpr uint32_t SPILLED = 31;
 
 __device__ __forceinline__ uint16_t* line_of(const SysDev& S, uint32_t rb, int sub) {
   return S.cal + ((size_t)rb * CAL_SUB + sub) * CAL_LINE;
 }
+__device__ __forceinline__ int32_t* spill_head(uint16_t* L) { return (int32_t*)(L + 30); }
 
 // sub-bucket of time T inside absolute bucket b: monotone in T
 __device__ __forceinline__ int sub_of(const SysDev& S, double T, uint32_t b) {
@@ -42,28 +48,46 @@ struct Lane {
   int status;
 };
 
-__device__ __forceinline__ bool cal_insert(const SysDev& S, int e, Ev& ev, uint32_t rb) {
+__device__ __forceinline__ void cal_insert(const SysDev& S, int e, Ev& ev, uint32_t rb) {
   int sub = sub_of(S, ev.t, ev.b);
   uint16_t* L = line_of(S, rb, sub);
   int cnt = L[0];
-  if (cnt >= CAP) return false;
-  L[1 + cnt] = (uint16_t)e;
-  L[0] = (uint16_t)(cnt + 1);
-  S.mask[rb] |= (uint8_t)(1u << sub);
-  ev.st = ST_QUEUED | ((uint32_t)sub << 2) | ((uint32_t)cnt << 5) | (rb << 10);
-  return true;
+  uint32_t pos;
+  if (cnt < CAP) {
+    L[1 + cnt] = (uint16_t)e;
+    L[0] = (uint16_t)(cnt + 1);
+    pos = (uint32_t)cnt;
+  } else {
+    int32_t* H = spill_head(L);
+    int h = *H;
+    S.on[e] = h; S.op[e] = NIL;
+    if (h != NIL) S.op[h] = e;
+    *H = e;
+    pos = SPILLED;
+  }
+  S.mask[rb] |= (uint16_t)(1u << sub);
+  ev.st = ST_QUEUED | ((uint32_t)sub << 2) | (pos << 6) | (rb << 11);
 }
 
 __device__ __forceinline__ void cal_remove(const SysDev& S, int e, uint32_t st) {
-  int sub = (st >> 2) & 7, pos = (st >> 5) & 31;
-  uint32_t rb = st >> 10;
+  int sub = (st >> 2) & 15;
+  uint32_t pos = (st >> 6) & 31;
+  uint32_t rb = st >> 11;
   uint16_t* L = line_of(S, rb, sub);
   int cnt = L[0];
-  int last = L[cnt];
-  L[1 + pos] = (uint16_t)last;
-  if (last != e) S.ev[last].st = (S.ev[last].st & ~(31u << 5)) | ((uint32_t)pos << 5);
-  L[0] = (uint16_t)(cnt - 1);
-  if (cnt == 1) S.mask[rb] &= (uint8_t)~(1u << sub);
+  int32_t* H = spill_head(L);
+  if (pos == SPILLED) {
+    int p = S.op[e], n = S.on[e];
+    if (p != NIL) S.on[p] = n; else *H = n;
+    if (n != NIL) S.op[n] = p;
+  } else {
+    int last = L[cnt];
+    L[1 + pos] = (uint16_t)last;
+    if (last != e) S.ev[last].st = (S.ev[last].st & ~(31u << 6)) | (pos << 6);
+    L[0] = (uint16_t)(cnt - 1);
+    cnt--;
+  }
+  if (cnt == 0 && *H == NIL) S.mask[rb] &= (uint16_t)~(1u << sub);
 }
 
 // addEventToQueue (src/EDMD.c:2144) in key form; cls_direct 2 from a handler,
@@ -77,18 +101,18 @@ __device__ void schedule(const SysDev& S, Lane& W, int e, double T, int32_t j, u
   double dt = T - R.P;
   if (dt < B.dtP) {
     ev.b = (uint32_t)R.k; ev.tie = (cls_direct << 62) | R.C;
-    if (!cal_insert(S, e, ev, W.actual)) W.status = EDMD_ERR_CAPACITY;
+    cal_insert(S, e, ev, W.actual);
   } else if (dt >= B.dtPN) {
     ev.b = BINF; ev.tie = R.C; ev.st = ST_OVF;
     S.on[e] = R.ovf; S.op[e] = NIL;
     if (R.ovf != NIL) S.op[R.ovf] = e;
     R.ovf = e;
   } else {
-    int d = (int)(dt / B.dtP);
+    int d = bucket_offset(dt, B.dtP, S.rdtP);
     uint32_t rb = W.actual + (uint32_t)d;
     if (rb >= (uint32_t)B.N) rb -= (uint32_t)B.N;
     ev.b = (uint32_t)(R.k + (uint64_t)d); ev.tie = (1ull << 62) | (TIE_MAX - R.C);
-    if (!cal_insert(S, e, ev, rb)) W.status = EDMD_ERR_CAPACITY;
+    cal_insert(S, e, ev, rb);
   }
   R.C++;
   S.ev[e] = ev;
@@ -121,7 +145,7 @@ __device__ void do_wrap(const SysDev& S, Lane& W) {
 
 __device__ __forceinline__ void fly(const SysDev& S, Disk& p, int i, double t, bool grow) {
   double dt = t - p.tl;
-  free_fly(S.B, p, t);
+  free_fly_i(S.B, p, t);
   if (grow) p.rad += dt * S.vr[i];
 }
 
@@ -147,9 +171,9 @@ __device__ void predict(const SysDev& S, Lane& W, int a, double* dt_out, int* p_
       Disk P = S.d[p];
       if (p != a) {
         double d = grow ? coll_time_grow(B, A, vra, P, S.vr[p], W.R.t, &ovl)
-                        : coll_time_normal(B, A, P, W.R.t, &ovl);
+                        : coll_time_normal_i(B, A, P, W.R.t, &ovl);
         np++;
-        if (bd > d) { bd = d; bp = p; bc = P.coll; any = true; }
+        if (time_key(bd) > time_key(d)) { bd = d; bp = p; bc = P.coll; any = true; }
       }
       p = P.nxt;
     }
@@ -169,7 +193,7 @@ __device__ void predict_and_schedule(const SysDev& S, Lane& W, int a) {
 
 __device__ void cross_schedule(const SysDev& S, Lane& W, int i, const Disk& di) {
   int dir;
-  double tc = crossing_time(S.B, di, S.cx[i], S.cy[i], W.R.t, &dir);
+  double tc = crossing_time_i(S.B, di, S.cx[i], S.cy[i], W.R.t, &dir);
   schedule(S, W, i, tc, dir, 0, 2ull);
 }
 
@@ -260,6 +284,12 @@ __device__ void do_growstop(const SysDev& S, Lane& W) {
   }
 }
 
+// One event of every lane's system per iteration, along a single predicated
+// path: the collision, stale-collision and crossing handlers of the reference
+// (src/EDMD.c:3542, 3553-3556, 2501) are merged so that the 32 systems of a
+// warp issue their loads and FP64 together instead of serialising divergent
+// branches.  Each system still performs its own queue operations in the
+// reference's order.
 __device__ void lane_run(const SysDev& S, const RunArgs& A) {
   const Box& B = S.B;
   const int N = B.N;
@@ -288,138 +318,149 @@ __device__ void lane_run(const SysDev& S, const RunArgs& A) {
         R.next_wrap += (uint64_t)N;
       }
       m = S.mask[W.actual];
-      if (++guard > 4 * N + 16 && R.ovf == NIL) { W.status = EDMD_ERR_BUDGET; break; }
+      if (++guard > (1 << 26)) { W.status = EDMD_ERR_BUDGET; break; }
     }
     if (W.status != EDMD_OK) break;
-    const uint16_t* Lp = line_of(S, W.actual, __ffs(m) - 1);
+    uint16_t* Lp = line_of(S, W.actual, __ffs(m) - 1);
     int cnt = Lp[0];
-    int e = Lp[1];
-    double bt = S.ev[e].t;
-    uint64_t bk = S.ev[e].tie;
-    for (int k = 2; k <= cnt; k++) {
+    int e = -1;
+    uint64_t bt = 0, bk = 0;
+    for (int k = 1; k <= cnt; k++) {
       int f = Lp[k];
-      double ft = S.ev[f].t;
+      uint64_t ft = time_key(S.ev[f].t);
       uint64_t fk = S.ev[f].tie;
-      if (ft < bt || (ft == bt && fk < bk)) { e = f; bt = ft; bk = fk; }
+      if (e < 0 || ft < bt || (ft == bt && fk < bk)) { e = f; bt = ft; bk = fk; }
     }
-    if (bt >= A.t_stop) { stop = EDMD_STOP_TIME; break; }
+    for (int f = *spill_head(Lp); f != NIL; f = S.on[f]) {
+      uint64_t ft = time_key(S.ev[f].t);
+      uint64_t fk = S.ev[f].tie;
+      if (e < 0 || ft < bt || (ft == bt && fk < bk)) { e = f; bt = ft; bk = fk; }
+    }
     Ev E = S.ev[e];
+    if (E.t >= A.t_stop) { stop = EDMD_STOP_TIME; break; }
     R.t = E.t;
     nev++;
     R.nevents++;
     cal_remove(S, e, E.st);
     S.ev[e].st = ST_NONE;
     const bool grow = R.grow != 0;
-    if (e >= N && e < 2 * N) {
-      // ---------------- collision (doTheCollisionNormal 3542 / Grow 3465)
-      const int i = e - N, j = E.j;
-      Disk di = S.d[i];
-      fly(S, di, i, R.t, grow);
-      Disk dj = S.d[j];
-      if (E.ca != dj.coll) {
-        S.d[i] = di;
-        R.nstale++;
-        predict_and_schedule(S, W, i);
+    if (e >= 2 * N) {
+      // ---------------- sampling events (rare): screenshot, thermo, growth stop
+      if (e == 2 * N + SP_SCREEN) {
+        for (int i = 0; i < N; i++) {
+          Disk p = S.d[i];
+          fly(S, p, i, R.t, grow);
+          S.d[i] = p;
+        }
+        schedule(S, W, e, R.t + S.dtime, 0, 0, 2ull);
+        if (A.flags & EDMD_F_STOP_AT_SCREEN) stop = EDMD_STOP_SCREEN;
+      } else if (e == 2 * N + SP_THERMO) {
+        do_thermo(S, W);
+        schedule(S, W, e, R.t + S.dtimeTh, 0, 0, 2ull);
       } else {
-        if ((A.flags & EDMD_F_TRACE) && S.trace && (int64_t)R.ntrace < S.trace_cap) {
-          edmd_collision* tr = (edmd_collision*)S.trace + R.ntrace;
-          tr->i = i; tr->j = j;
-          tr->cell_i = S.cy[i] * B.Nxc + S.cx[i];
-          tr->cell_j = S.cy[j] * B.Nxc + S.cx[j];
-          tr->t = R.t;
-        }
-        R.ntrace++;
-        if (!(A.flags & EDMD_F_COUNT_NORMAL) || !grow) logged++;
-        R.ncol++;
-        R.ncol_total++;
-        fly(S, dj, j, R.t, grow);
-        di.coll++;
-        dj.coll++;
-        double dx = dj.x - di.x, dy = dj.y - di.y;
-        double dvx = dj.vx - di.vx, dvy = dj.vy - di.vy;
-        if (!grow) {   // elastic branch src/EDMD.c:3802-3827
-          double invMass = 1 / (di.m + dj.m);
-          pbc(B, dx, dy);
-          double collKernel = invMass * (1 + S.res) * (dx * dvx + dy * dvy);
-          double distSquared = 4 * di.rad * dj.rad;
-          double f = collKernel / distSquared;
-          double ct = di.m * dj.m * f;
-          R.collT[0] += ct * dx * dx;
-          R.collT[1] += ct * dy * dy;
-          R.collT[2] += ct * dx * dy;
-          R.collT[3] += ct * dy * dx;
-          di.vx += f * dj.m * dx;
-          di.vy += f * dj.m * dy;
-          dj.vx -= f * di.m * dx;
-          dj.vy -= f * di.m * dy;
-        } else {       // growth rule src/EDMD.c:3479-3520
-          double delta = 0.1 * 0;
-          double res = 0.75 * 0 + 1;
-          double dvr = S.vr[i] + S.vr[j];
-          pbc(B, dx, dy);
-          double dist = sqrt(dx * dx + dy * dy);
-          double dxr = dx / dist, dyr = dy / dist;
-          double invMass = 1 / (di.m + dj.m);
-          double collKernel = invMass * (1 + res) * (dxr * dvx + dyr * dvy - dvr);
-          di.vx += collKernel * dj.m * dxr - 2 * dj.m * invMass * delta * dxr;
-          di.vy += collKernel * dj.m * dyr - 2 * dj.m * invMass * delta * dyr;
-          dj.vx -= collKernel * di.m * dxr - 2 * di.m * invMass * delta * dxr;
-          dj.vy -= collKernel * di.m * dyr - 2 * di.m * invMass * delta * dyr;
-        }
-        S.d[i] = di;
-        S.d[j] = dj;
-        unqueue(S, W, i);
-        unqueue(S, W, j);
-        cross_schedule(S, W, i, di);
-        cross_schedule(S, W, j, dj);
-        unqueue(S, W, N + j);
-        predict_and_schedule(S, W, i);
-        predict_and_schedule(S, W, j);
+        do_growstop(S, W);
+        if (A.flags & EDMD_F_STOP_AT_GROW) stop = EDMD_STOP_GROW;
       }
-    } else if (e < N) {
+      if (W.status != EDMD_OK || stop) break;
+      continue;
+    }
+    const bool isColl = e >= N;
+    const bool cross = !isColl;
+    const int a = isColl ? e - N : e;
+    const int b = isColl ? E.j : a;
+    Disk Da = S.d[a];
+    Disk Db = S.d[b];
+    fly(S, Da, a, R.t, grow);
+    const bool valid = isColl && (E.ca == Db.coll);
+    if (isColl && !valid) R.nstale++;
+    if (valid) {
+      // ---------------- collision (doTheCollisionNormal 3542 / Grow 3465)
+      if ((A.flags & EDMD_F_TRACE) && S.trace && (int64_t)R.ntrace < S.trace_cap) {
+        edmd_collision* tr = (edmd_collision*)S.trace + R.ntrace;
+        tr->i = a; tr->j = b;
+        tr->cell_i = S.cy[a] * B.Nxc + S.cx[a];
+        tr->cell_j = S.cy[b] * B.Nxc + S.cx[b];
+        tr->t = R.t;
+      }
+      R.ntrace++;
+      if (!(A.flags & EDMD_F_COUNT_NORMAL) || !grow) logged++;
+      R.ncol++;
+      R.ncol_total++;
+      fly(S, Db, b, R.t, grow);
+      Da.coll++;
+      Db.coll++;
+      double dx = Db.x - Da.x, dy = Db.y - Da.y;
+      double dvx = Db.vx - Da.vx, dvy = Db.vy - Da.vy;
+      if (!grow) {   // elastic branch src/EDMD.c:3802-3827
+        // 1/(1+1) and x/4 are exact, so the shortcuts below round identically
+        double msum = Da.m + Db.m;
+        double invMass = msum == 2.0 ? 0.5 : 1 / msum;
+        pbc(B, dx, dy);
+        double collKernel = invMass * (1 + S.res) * (dx * dvx + dy * dvy);
+        double distSquared = 4 * Da.rad * Db.rad;
+        double f = distSquared == 4.0 ? collKernel * 0.25 : collKernel / distSquared;
+        double ct = Da.m * Db.m * f;
+        R.collT[0] += ct * dx * dx;
+        R.collT[1] += ct * dy * dy;
+        R.collT[2] += ct * dx * dy;
+        R.collT[3] += ct * dy * dx;
+        Da.vx += f * Db.m * dx;
+        Da.vy += f * Db.m * dy;
+        Db.vx -= f * Da.m * dx;
+        Db.vy -= f * Da.m * dy;
+      } else {       // growth rule src/EDMD.c:3479-3520
+        double delta = 0.1 * 0;
+        double res = 0.75 * 0 + 1;
+        double dvr = S.vr[a] + S.vr[b];
+        pbc(B, dx, dy);
+        double dist = sqrt(dx * dx + dy * dy);
+        double dxr = dx / dist, dyr = dy / dist;
+        double invMass = 1 / (Da.m + Db.m);
+        double collKernel = invMass * (1 + res) * (dxr * dvx + dyr * dvy - dvr);
+        Da.vx += collKernel * Db.m * dxr - 2 * Db.m * invMass * delta * dxr;
+        Da.vy += collKernel * Db.m * dyr - 2 * Db.m * invMass * delta * dyr;
+        Db.vx -= collKernel * Da.m * dxr - 2 * Da.m * invMass * delta * dxr;
+        Db.vy -= collKernel * Da.m * dyr - 2 * Da.m * invMass * delta * dyr;
+      }
+    }
+    if (cross) {
       // ---------------- cell crossing (doTheCrossing 2501)
-      const int i = e;
       R.ncross++;
-      Disk di = S.d[i];
-      fly(S, di, i, R.t, grow);
-      int cx = S.cx[i], cy = S.cy[i];
-      int pv = S.prv[i], nx = di.nxt;
+      int cx = S.cx[a], cy = S.cy[a];
+      int pv = S.prv[a], nx = Da.nxt;
       if (pv == NIL) S.head[cy * B.Nxc + cx] = nx;
       else S.d[pv].nxt = nx;
       if (nx != NIL) S.prv[nx] = pv;
       switch (E.j) {
-        case 1: if (cx - 1 == -1) { cx = B.Nxc - 1; S.crossX[i] -= 1; } else cx -= 1; break;
-        case 2: if (cx + 1 == B.Nxc) { cx = 0; S.crossX[i] += 1; } else cx += 1; break;
-        case 3: if (cy - 1 == -1) { cy = B.Nyc - 1; S.crossY[i] -= 1; } else cy -= 1; break;
-        case 4: if (cy + 1 == B.Nyc) { cy = 0; S.crossY[i] += 1; } else cy += 1; break;
+        case 1: if (cx - 1 == -1) { cx = B.Nxc - 1; S.crossX[a] -= 1; } else cx -= 1; break;
+        case 2: if (cx + 1 == B.Nxc) { cx = 0; S.crossX[a] += 1; } else cx += 1; break;
+        case 3: if (cy - 1 == -1) { cy = B.Nyc - 1; S.crossY[a] -= 1; } else cy -= 1; break;
+        case 4: if (cy + 1 == B.Nyc) { cy = 0; S.crossY[a] += 1; } else cy += 1; break;
       }
       int c = cy * B.Nxc + cx;
       int h = S.head[c];
-      S.cx[i] = cx; S.cy[i] = cy;
-      S.prv[i] = NIL;
-      di.nxt = h;
-      S.d[i] = di;
-      S.head[c] = i;
-      if (h != NIL) S.prv[h] = i;
-      cross_schedule(S, W, i, di);
-      unqueue(S, W, N + i);
-      predict_and_schedule(S, W, i);
-    } else if (e == 2 * N + SP_SCREEN) {
-      for (int i = 0; i < N; i++) {
-        Disk p = S.d[i];
-        fly(S, p, i, R.t, grow);
-        S.d[i] = p;
-      }
-      schedule(S, W, e, R.t + S.dtime, 0, 0, 2ull);
-      if (A.flags & EDMD_F_STOP_AT_SCREEN) stop = EDMD_STOP_SCREEN;
-    } else if (e == 2 * N + SP_THERMO) {
-      do_thermo(S, W);
-      schedule(S, W, e, R.t + S.dtimeTh, 0, 0, 2ull);
-    } else {
-      do_growstop(S, W);
-      if (A.flags & EDMD_F_STOP_AT_GROW) stop = EDMD_STOP_GROW;
+      S.cx[a] = cx; S.cy[a] = cy;
+      S.prv[a] = NIL;
+      Da.nxt = h;
+      S.head[c] = a;
+      if (h != NIL) S.prv[h] = a;
     }
-    if (W.status != EDMD_OK || stop) break;
+    S.d[a] = Da;
+    if (valid) S.d[b] = Db;
+    // queue operations in the reference's order (3872-3879 / 2587-2589)
+    if (valid) { unqueue(S, W, a); unqueue(S, W, b); }
+    if (valid || cross) cross_schedule(S, W, a, Da);
+    if (valid) cross_schedule(S, W, b, Db);
+    if (valid) unqueue(S, W, N + b);
+    if (cross) unqueue(S, W, N + a);
+    double dta, dtb = 0;
+    int pa, pb = 0;
+    uint32_t caa, cab = 0;
+    predict(S, W, a, &dta, &pa, &caa);
+    if (valid) predict(S, W, b, &dtb, &pb, &cab);
+    schedule(S, W, N + a, R.t + dta, pa, caa, 2ull);
+    if (valid) schedule(S, W, N + b, R.t + dtb, pb, cab, 2ull);
+    if (W.status != EDMD_OK) break;
   }
   R.stop_reason = stop;
   R.status = W.status;
@@ -440,12 +481,15 @@ __global__ void k_lane_build(const SysDev* __restrict__ sys, int nsys) {
   const int N = S.B.N;
   const int E = 2 * N + NSPECIAL;
   for (int k = 0; k < N; k++) S.mask[k] = 0;
-  for (int k = 0; k < N * CAL_SUB; k++) S.cal[(size_t)k * CAL_LINE] = 0;
+  for (int k = 0; k < N * CAL_SUB; k++) {
+    uint16_t* L = S.cal + (size_t)k * CAL_LINE;
+    L[0] = 0;
+    *spill_head(L) = NIL;
+  }
   for (int e = 0; e < E; e++) {
     Ev ev = S.ev[e];
     if ((ev.st & 3u) != ST_QUEUED) continue;
-    uint32_t rb = ev.b;                    // the calendar starts at bucket 0
-    if (!cal_insert(S, e, ev, rb)) { S.st->status = EDMD_ERR_CAPACITY; return; }
+    cal_insert(S, e, ev, ev.b);            // the calendar starts at bucket 0
     S.ev[e].st = ev.st;
   }
 }

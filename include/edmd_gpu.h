@@ -46,7 +46,7 @@ extern "C" {
 #define EDMD_STOP_GROW      5   /* stopped right after the growth stop        */
 
 /* engines (edmd_set_engine) */
-#define EDMD_ENGINE_AUTO    0   /* lane engine for >= 64 systems, else warp  */
+#define EDMD_ENGINE_AUTO    0   /* the warp engine (fastest measured)         */
 #define EDMD_ENGINE_WARP    1   /* one warp per system: single large systems  */
 #define EDMD_ENGINE_LANE    2   /* one thread per system: large batches, N <= 32766 */
 
