@@ -848,6 +848,8 @@ extern "C" int edmd_device_info(char* name, int32_t cap, int32_t* sm_count) {
   return EDMD_OK;
 }
 
+static size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
 template <class T>
 static cudaError_t dalloc(T** p, size_t n) { return cudaMalloc((void**)p, (n ? n : 1) * sizeof(T)); }
 
@@ -1205,6 +1207,178 @@ extern "C" int edmd_get_engine(const edmd_ctx* ctx) {
   return ctx ? ctx->engine : -1;
 }
 
+// ==================================================================== allocation-free entry point
+//
+// edmd_run_noalloc serves callers that must not allocate device memory, for
+// example code that runs inside a latency-critical loop or a host framework
+// that owns every device buffer and forbids cudaMalloc/cudaFree after start-up.
+// The caller passes its own device arrays (the state in and out); everything
+// the engine needs besides them -- the system descriptor, cell lists, event
+// records, the tournament tree, the scalar state and the work counter -- lives
+// in the file-scope array below, which every GPU that loads this library keeps
+// until the process exits.
+namespace {
+constexpr int64_t NOALLOC_MAX_N = 8192;        // disks per call
+constexpr int64_t NOALLOC_MAX_CELLS = 65536;   // Nxcells * Nycells per call
+constexpr size_t NOALLOC_BYTES = (size_t)4 << 20;
+constexpr int NOALLOC_MAX_DEVICES = 64;
+}
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_BYTES];
+static unsigned char* g_noalloc_addr[NOALLOC_MAX_DEVICES];   // device address, per device
+static thread_local std::string g_noalloc_err;
+
+namespace {
+
+__global__ void k_noalloc_put(SysDev s, SysDev* dst) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) *dst = s;
+}
+
+// disk records, cell lists (index order, push-front as addToCell) and the
+// scalar state from the caller's device arrays; one thread, N <= 8192
+__global__ void k_noalloc_stage(const SysDev* __restrict__ sys, const double* x, const double* y,
+                                const double* vx, const double* vy, const double* rad,
+                                const double* m, double first_screen, double first_thermo) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const SysDev& S = sys[0];
+  const Box& B = S.B;
+  const int N = B.N;
+  for (int c = 0; c < B.Nxc * B.Nyc; c++) S.head[c] = NIL;
+  for (int i = 0; i < N; i++) {
+    Disk q;
+    q.x = x[i]; q.y = y[i]; q.vx = vx[i]; q.vy = vy[i]; q.tl = 0; q.rad = rad[i]; q.m = m[i];
+    q.coll = 0;
+    int X = (int)(q.x * B.cxf), Y = (int)(q.y * B.cyf);
+    if (X >= B.Nxc) X = B.Nxc - 1;
+    if (Y >= B.Nyc) Y = B.Nyc - 1;
+    if (X < 0) X = 0;
+    if (Y < 0) Y = 0;
+    S.cx[i] = X; S.cy[i] = Y; S.prv[i] = NIL;
+    S.crossX[i] = 0; S.crossY[i] = 0;
+    S.vr[i] = 0;
+    q.nxt = S.head[Y * B.Nxc + X];
+    S.head[Y * B.Nxc + X] = i;
+    if (q.nxt != NIL) S.prv[q.nxt] = i;
+    S.d[i] = q;
+  }
+  SysState st;
+  memset(&st, 0, sizeof(st));
+  st.k = 0; st.next_wrap = (uint64_t)N; st.ovf = NIL; st.grow = 0;
+  st.lastThermo = first_thermo + 0.000000001;   // read by k_init_events
+  st.collT[0] = -1;
+  st.collT[1] = first_screen;
+  *S.st = st;
+}
+
+__global__ void k_noalloc_out(const SysDev* __restrict__ sys, double* x, double* y, double* vx,
+                              double* vy) {
+  const SysDev& S = sys[0];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < S.B.N; i += gridDim.x * blockDim.x) {
+    Disk p = S.d[i];
+    x[i] = p.x; y[i] = p.y; vx[i] = p.vx; vy[i] = p.vy;
+  }
+}
+
+int noalloc_fail(int code, const char* m) {
+  g_noalloc_err = m;
+  return code;
+}
+
+}  // namespace
+
+extern "C" int edmd_run_noalloc(const edmd_system_desc* desc, double* x, double* y, double* vx,
+                                double* vy, const double* rad, const double* m, int64_t max_coll,
+                                double t_stop, int64_t* ncol_out, double* t_out, void* stream) {
+  if (!desc || !x || !y || !vx || !vy || !rad || !m || max_coll < 0)
+    return noalloc_fail(EDMD_ERR_ARG, "edmd_run_noalloc: null argument or negative max_coll");
+  const edmd_system_desc& D = *desc;
+  if (D.t_growstop > 0)
+    return noalloc_fail(EDMD_ERR_ARG, "edmd_run_noalloc: growth starts are not supported");
+  if (D.N < 2 || D.N > NOALLOC_MAX_N)
+    return noalloc_fail(EDMD_ERR_CAPACITY, "edmd_run_noalloc: N must be in [2, 8192]");
+  SysDev S;
+  memset(&S, 0, sizeof(S));
+  Box& B = S.B;
+  B.N = D.N; B.Lx = D.Lx; B.Ly = D.Ly;
+  B.hLx = D.Lx / 2; B.hLy = D.Ly / 2;                      // boxConstantHelper 679-714
+  B.Nyc = (int)(B.hLy); B.Nxc = (int)(B.hLx);
+  if (!(D.Lx > 0) || !(D.Ly > 0) || B.Nxc < 1 || B.Nyc < 1)
+    return noalloc_fail(EDMD_ERR_ARG, "edmd_run_noalloc: box smaller than one cell");
+  if ((int64_t)B.Nxc * B.Nyc > NOALLOC_MAX_CELLS)
+    return noalloc_fail(EDMD_ERR_CAPACITY, "edmd_run_noalloc: more than 65536 cells");
+  B.cxs = D.Lx / B.Nxc; B.cys = D.Ly / B.Nyc;
+  B.cxf = 1 / B.cxs; B.cyf = 1 / B.cys;
+  B.dtP = 5.0 / (double)D.N;
+  B.dtPN = B.dtP * D.N;
+  S.rdtP = 1.0 / B.dtP;
+  S.res = D.res; S.Einit = D.Einit; S.dtime = D.dtime; S.dtimeTh = D.dtime_thermo; S.tmax = D.tmax;
+  S.L = D.N + NSPECIAL;
+  int c = S.L;
+  size_t nodes = 0;
+  for (;;) {
+    S.lev_off[S.nlev] = (int32_t)nodes; S.lev_cnt[S.nlev] = c; nodes += c; S.nlev++;
+    if (c == 1) break;
+    c = (c + 31) / 32;
+  }
+  // once per device, with that device current: the device address of the array
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= NOALLOC_MAX_DEVICES)
+    return noalloc_fail(EDMD_ERR_CUDA, "edmd_run_noalloc: no current CUDA device");
+  if (!g_noalloc_addr[dev]) {
+    void* a = nullptr;
+    cudaError_t ce = cudaGetSymbolAddress(&a, g_noalloc_scratch);
+    if (ce != cudaSuccess || !a) return noalloc_fail(EDMD_ERR_CUDA, cudaGetErrorString(ce));
+    g_noalloc_addr[dev] = (unsigned char*)a;
+  }
+  unsigned char* base = g_noalloc_addr[dev];
+  size_t off = 0;
+  auto take = [&](size_t bytes) { unsigned char* r = base + off; off += align_up(bytes, 256); return r; };
+  size_t N = D.N, E = 2 * N + NSPECIAL, C = (size_t)B.Nxc * B.Nyc;
+  SysDev* dsys = (SysDev*)take(sizeof(SysDev));
+  int32_t* work = (int32_t*)take(sizeof(int32_t));
+  S.st = (SysState*)take(sizeof(SysState));
+  S.d = (Disk*)take(N * sizeof(Disk));
+  S.vr = (double*)take(N * 8);
+  S.cx = (int32_t*)take(N * 4); S.cy = (int32_t*)take(N * 4); S.prv = (int32_t*)take(N * 4);
+  S.crossX = (int32_t*)take(N * 4); S.crossY = (int32_t*)take(N * 4);
+  S.head = (int32_t*)take(C * 4);
+  S.ev = (Ev*)take(E * sizeof(Ev));
+  S.on = (int32_t*)take(E * 4); S.op = (int32_t*)take(E * 4);
+  S.tree = (Node*)take(nodes * sizeof(Node));
+  S.rows = (double*)take(64 * 9 * 8);
+  S.rows_cap = 64;
+  S.trace = nullptr; S.trace_cap = 0;
+  if (off > NOALLOC_BYTES)
+    return noalloc_fail(EDMD_ERR_CAPACITY, "edmd_run_noalloc: system does not fit the 4 MiB scratch array");
+  cudaStream_t st = (cudaStream_t)stream;
+  RunArgs A;
+  A.max_coll = max_coll; A.t_stop = t_stop; A.flags = 0; A.max_events = (int64_t)1 << 60;
+  A.nsys = 1; A.work = work;
+  k_noalloc_put<<<1, 1, 0, st>>>(S, dsys);
+  k_noalloc_stage<<<1, 32, 0, st>>>(dsys, x, y, vx, vy, rad, m, D.first_screen, D.first_thermo);
+  k_init_events<<<dim3((unsigned)((N + 1 + 127) / 128), 1), 128, 0, st>>>(dsys);
+  k_init_finish<<<1, 32, 0, st>>>(dsys, 1);
+  k_tree_build<<<1, 32, 0, st>>>(dsys, 1);
+  if (cudaMemsetAsync(work, 0, sizeof(int32_t), st) != cudaSuccess)
+    return noalloc_fail(EDMD_ERR_CUDA, "edmd_run_noalloc: memset failed");
+  k_run<<<1, 32 * WARPS_PER_BLOCK, 0, st>>>(dsys, A);
+  k_sync<<<1, 256, 0, st>>>(dsys, 1);
+  k_noalloc_out<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(dsys, x, y, vx, vy);
+  cudaError_t ce = cudaGetLastError();
+  if (ce != cudaSuccess) return noalloc_fail(EDMD_ERR_CUDA, cudaGetErrorString(ce));
+  SysState R;
+  ce = cudaMemcpyAsync(&R, S.st, sizeof(R), cudaMemcpyDeviceToHost, st);
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
+  if (ce != cudaSuccess) return noalloc_fail(EDMD_ERR_CUDA, cudaGetErrorString(ce));
+  if (ncol_out) *ncol_out = (int64_t)R.ncol;
+  if (t_out) *t_out = R.t;
+  if (R.status != EDMD_OK)
+    return noalloc_fail(R.status, R.status == EDMD_ERR_OVERLAP ? "edmd_run_noalloc: overlapping disks"
+                                                               : "edmd_run_noalloc: event loop stopped");
+  g_noalloc_err.clear();
+  return EDMD_OK;
+}
+
 extern "C" const char* edmd_last_error(const edmd_ctx* ctx) {
-  return ctx ? ctx->err.c_str() : "null context";
+  return ctx ? ctx->err.c_str() : g_noalloc_err.c_str();
 }

@@ -53,7 +53,8 @@ EXPORTS = [
     "edmd_create", "edmd_load_state", "edmd_advance", "edmd_sync", "edmd_get_state",
     "edmd_get_states", "edmd_get_counters", "edmd_get_all_counters", "edmd_get_virial",
     "edmd_get_thermo", "edmd_get_trace", "edmd_set_engine", "edmd_set_lane_threads",
-    "edmd_get_engine", "edmd_set_device", "edmd_host_alloc", "edmd_host_free", "edmd_destroy",
+    "edmd_get_engine", "edmd_set_device", "edmd_host_alloc", "edmd_host_free", "edmd_run_noalloc",
+    "edmd_destroy",
     "edmd_last_error", "edmd_device_info",
     "edmd_mt_seed", "edmd_mt_u32", "edmd_mt_double", "edmd_hex_size", "edmd_random_size",
     "edmd_grow_rate", "edmd_normalize", "edmd_init_hex", "edmd_init_grow", "edmd_default_desc",
@@ -84,6 +85,8 @@ def load(path=LIB_PATH):
     L.edmd_host_free.argtypes = [C.c_void_p]
     L.edmd_set_device.argtypes = [C.c_int32]
     L.edmd_set_engine.argtypes = [C.c_int32]
+    L.edmd_run_noalloc.argtypes = [C.POINTER(SystemDesc)] + [C.c_void_p] * 6 + [
+        C.c_int64, C.c_double, C.POINTER(C.c_int64), C.POINTER(C.c_double), C.c_void_p]
     L.edmd_set_lane_threads.argtypes = [C.c_int32]
     L.edmd_get_engine.argtypes = [C.c_void_p]
     L.edmd_sync.argtypes = [C.c_void_p]

@@ -165,7 +165,33 @@ int edmd_set_device(int32_t dev);
 int edmd_host_alloc(void** p, int64_t bytes);
 int edmd_host_free(void* p);
 
+/*
+ * Allocation-free run of one system.  No counterpart in the reference: it
+ * exists for callers that cannot call cudaMalloc -- code in a loop where
+ * device allocation is forbidden, or a host framework that owns every device
+ * buffer.  x, y, vx, vy, rad, m are the CALLER's DEVICE arrays of desc->N
+ * entries; the call restarts the system from them (t = 0, normal phase, the
+ * -l semantics of edmd_load_state), runs until max_coll accepted collisions,
+ * t_stop or desc->tmax, free-flies every disk to the final time and writes x,
+ * y, vx, vy back.  ncol_out / t_out (host, may be NULL) receive the collisions
+ * run and the final time.  `stream` is a cudaStream_t (NULL: default stream).
+ *
+ * Limits: N <= 8192, Nxcells*Nycells <= 65536, direct starts only
+ * (desc->t_growstop < 0); larger systems return EDMD_ERR_CAPACITY.
+ * It allocates nothing: all engine state lives in one file-scope 4 MiB
+ * __device__ array that each GPU using this library keeps until exit.  The
+ * first call on a device looks up that array's address (once per device, with
+ * the device current), so make the first call before any stream capture.
+ * Every call reuses the same array and re-initialises what it needs, so calls
+ * that overlap on the GPU (other streams, other host threads) race and must
+ * be serialised by the caller.  Errors are readable with edmd_last_error(NULL).
+ */
+int edmd_run_noalloc(const edmd_system_desc* desc, double* x, double* y, double* vx, double* vy,
+                     const double* rad, const double* m, int64_t max_coll, double t_stop,
+                     int64_t* ncol_out, double* t_out, void* stream);
+
 int edmd_destroy(edmd_ctx* ctx);
+/* message of the last failed call on `ctx`; NULL gives edmd_run_noalloc's */
 const char* edmd_last_error(const edmd_ctx* ctx);
 int edmd_device_info(char* name, int32_t cap, int32_t* sm_count);
 
