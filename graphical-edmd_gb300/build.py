@@ -20,7 +20,7 @@ HOST = os.path.join(HERE, "host")
 INCLUDE = os.path.join(ROOT, "include")
 BUILD = os.path.join(HERE, "_build")
 
-CUDA_SOURCES = ["edmd_engine.cu", "edmd_lane.cu"]
+CUDA_SOURCES = ["edmd_engine.cu", "edmd_lane.cu", "edmd_tangent.cu"]
 HOST_SOURCES = ["edmd_init.c"]
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "--fmad=false",
               "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I" + INCLUDE]
@@ -74,6 +74,10 @@ def build(verbose=False):
     if _newer(lib, objs):
         _run_all([[_nvcc(), "-gencode", "arch=compute_103a,code=sm_103a", "-shared", "-o", lib]
                   + objs + ["-lcudart", "-lm"]])
+    probe_src = os.path.join(CSRC, "peak_probe.cu")
+    probe = os.path.join(HERE, "peak_probe")
+    if _newer(probe, [probe_src, __file__]):
+        _run_all([[_nvcc(), "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-o", probe, probe_src]])
     main_src = os.path.join(HOST, "edmd_main.c")
     exe = os.path.join(HERE, "edmd")
     if os.path.exists(main_src) and _newer(exe, [main_src, lib] + headers):

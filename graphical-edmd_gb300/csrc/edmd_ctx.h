@@ -1,0 +1,58 @@
+// edmd_ctx.h -- host-side context shared by the engine translation units
+// (internal; the public interface is include/edmd_gpu.h).
+#pragma once
+#include <string>
+#include <vector>
+#include <cuda_runtime.h>
+#include "edmd_device.cuh"
+#include "../../include/edmd_gpu.h"
+
+using namespace edmd;
+
+struct edmd_ctx {
+  int nsys = 0;
+  int64_t total_N = 0;
+  int maxN = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  std::vector<SysDev> hs;
+  std::vector<edmd_system_desc> desc;
+  std::vector<int64_t> disk_off, cell_off;
+  SysDev* ds = nullptr;
+  // device arrays shared by all systems (each system owns a slice)
+  Disk* d = nullptr; double* vr = nullptr;
+  int32_t *cx = nullptr, *cy = nullptr, *prv = nullptr, *crossX = nullptr, *crossY = nullptr;
+  int32_t* head = nullptr;
+  Ev* ev = nullptr; int32_t *on = nullptr, *op = nullptr;
+  Node* tree = nullptr;
+  SysState* st = nullptr;
+  edmd_collision* trace = nullptr;
+  double* rows = nullptr;
+  double* stage = nullptr;          // SoA gather buffer (6 x total_N)
+  int32_t* work = nullptr;
+  edmd_log_entry* logbuf = nullptr; // per-system collision-geometry logs
+  int64_t log_cap = 0;
+  std::vector<void*> ckpt;          // device snapshots of the whole engine state
+  std::vector<size_t> ckpt_parts;   // bytes of each array in a snapshot
+  uint16_t* cal = nullptr;          // calendars of the thread-per-system engine
+  uint16_t* mask = nullptr;
+  int engine = 0;                   // EDMD_ENGINE_WARP or EDMD_ENGINE_LANE
+  int64_t total_C = 0;
+  std::string err;
+};
+
+static inline int set_err(edmd_ctx* c, int code, const std::string& m) {
+  if (c) c->err = m;
+  return code;
+}
+#define CK(call)                                                                         \
+  do {                                                                                   \
+    cudaError_t _e = (call);                                                             \
+    if (_e != cudaSuccess) return set_err(ctx, EDMD_ERR_CUDA, std::string(#call ": ") +   \
+                                                                  cudaGetErrorString(_e)); \
+  } while (0)
+
+static inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+template <class T>
+static inline cudaError_t dalloc(T** p, size_t n) { return cudaMalloc((void**)p, (n ? n : 1) * sizeof(T)); }

@@ -75,6 +75,7 @@ struct SysState {
   uint64_t ncol, ncol_total, ncross, nstale, npair, npred, nevents, ntrace;
   int32_t ovf, grow, nrows, stop_reason;
   int32_t status, err_a, err_b, pad;
+  uint64_t nlog;               // collision-geometry records written (EDMD_F_LOG)
 };
 
 struct SysDev {
@@ -92,6 +93,8 @@ struct SysDev {
   SysState* st;
   void* trace;                 // edmd_collision records
   int64_t trace_cap;
+  void* log;                   // edmd_log_entry records (differentiation)
+  int64_t log_cap;
   double* rows;                // thermo rows, 9 doubles each
   int32_t rows_cap, pad;
   // calendar of the thread-per-system engine (edmd_lane.cu)

@@ -536,6 +536,12 @@ __device__ void run_system(const SysDev& S, const RunArgs& A, int lane, WarpSmem
           R.collT[1] += ct * dy * dy;
           R.collT[2] += ct * dx * dy;
           R.collT[3] += ct * dy * dx;
+          if ((A.flags & EDMD_F_LOG) && S.log && (int64_t)R.nlog < S.log_cap && lane == 0) {
+            edmd_log_entry* lg = (edmd_log_entry*)S.log + R.nlog;
+            lg->i = i; lg->j = j; lg->t = R.t; lg->dx = dx; lg->dy = dy;
+            lg->dvx = dvx; lg->dvy = dvy; lg->f = f;
+          }
+          if (A.flags & EDMD_F_LOG) R.nlog++;
           di.vx += f * dj.m * dx;
           di.vy += f * dj.m * dy;
           dj.vx -= f * di.m * dx;
@@ -784,33 +790,7 @@ __global__ void k_gather(const Disk* __restrict__ d, int64_t total, double* __re
 
 // ==================================================================== C ABI
 
-struct edmd_ctx {
-  int nsys = 0;
-  int64_t total_N = 0;
-  int maxN = 0;
-  cudaStream_t stream = nullptr;
-  cudaEvent_t e0 = nullptr, e1 = nullptr;
-  std::vector<SysDev> hs;
-  std::vector<edmd_system_desc> desc;
-  std::vector<int64_t> disk_off, cell_off;
-  SysDev* ds = nullptr;
-  // device arrays shared by all systems (each system owns a slice)
-  Disk* d = nullptr; double* vr = nullptr;
-  int32_t *cx = nullptr, *cy = nullptr, *prv = nullptr, *crossX = nullptr, *crossY = nullptr;
-  int32_t* head = nullptr;
-  Ev* ev = nullptr; int32_t *on = nullptr, *op = nullptr;
-  Node* tree = nullptr;
-  SysState* st = nullptr;
-  edmd_collision* trace = nullptr;
-  double* rows = nullptr;
-  double* stage = nullptr;          // SoA gather buffer (6 x total_N)
-  int32_t* work = nullptr;
-  uint16_t* cal = nullptr;          // calendars of the thread-per-system engine
-  uint16_t* mask = nullptr;
-  int engine = 0;                   // EDMD_ENGINE_WARP or EDMD_ENGINE_LANE
-  int64_t total_C = 0;
-  std::string err;
-};
+#include "edmd_ctx.h"
 
 static int g_engine = EDMD_ENGINE_AUTO;
 static int g_lane_threads = 32;
@@ -827,17 +807,6 @@ extern "C" int edmd_set_lane_threads(int32_t threads_per_block) {
   return EDMD_OK;
 }
 
-static int set_err(edmd_ctx* c, int code, const std::string& m) {
-  if (c) c->err = m;
-  return code;
-}
-#define CK(call)                                                                         \
-  do {                                                                                   \
-    cudaError_t _e = (call);                                                             \
-    if (_e != cudaSuccess) return set_err(ctx, EDMD_ERR_CUDA, std::string(#call ": ") +   \
-                                                                  cudaGetErrorString(_e)); \
-  } while (0)
-
 extern "C" int edmd_device_info(char* name, int32_t cap, int32_t* sm_count) {
   int n = 0;
   if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) return EDMD_ERR_NODEV;
@@ -848,10 +817,7 @@ extern "C" int edmd_device_info(char* name, int32_t cap, int32_t* sm_count) {
   return EDMD_OK;
 }
 
-static size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
-template <class T>
-static cudaError_t dalloc(T** p, size_t n) { return cudaMalloc((void**)p, (n ? n : 1) * sizeof(T)); }
 
 // (Re)initialise every system from host arrays: the cell lists are built on
 // the host in index order (cellListInit src/EDMD.c:1906 -> addToCell 2053,

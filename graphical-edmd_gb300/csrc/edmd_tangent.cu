@@ -1,0 +1,487 @@
+// edmd_tangent.cu -- tangent-linear and adjoint dynamics of the hard-disk system,
+// engine checkpoints, and the collision-geometry log that feeds them.
+//
+// The reference has no derivatives; this is the differentiation pattern built on
+// top of its dynamics.  Between collisions a disk flies freely,
+//     dr(t) = dr(t0) + dv (t - t0),   dv constant,
+// and at an elastic collision of i and j (src/EDMD.c:3587-3827: r = r_j - r_i at
+// contact, v = v_j - v_i before it, f = (1+res)/(m_i+m_j) (r.v)/sigma^2,
+// v_i += f m_j r, v_j -= f m_i r) the tangent map is that of Dellago, Posch and
+// Hoover (Phys. Rev. E 53, 1485 (1996)), re-derived here:
+//     dt_c = -(r . dr_ij) / (r . v)                  shift of the collision time
+//     drc  = dr_ij + v dt_c                          relative position at contact
+//     df   = (f / (r . v)) (v . drc + r . dv_ij)
+//     w    = df r + f drc
+//     dr_i' = dr_i - Dv_i dt_c,  dr_j' = dr_j - Dv_j dt_c     (Dv = velocity jumps)
+//     dv_i' = dv_i + m_j w,      dv_j' = dv_j - m_i w
+// The adjoint applies the transpose of the same map backwards over the log.
+#include "edmd_ctx.h"
+
+#include <cmath>
+#include <cstring>
+#include <random>
+
+namespace {
+
+// ---------------------------------------------------------------- tangent kernels
+
+// T is row-major [4N][K]: row 4i+c holds component c (dx, dy, dvx, dvy) of disk
+// i for the K tangent vectors, so lane k of a warp reads one coalesced row.
+__global__ void k_tangent_apply(const edmd_log_entry* __restrict__ log, int64_t M,
+                                const Disk* __restrict__ d, double* __restrict__ T,
+                                double* __restrict__ tl, int K) {
+  const int k = threadIdx.x;
+  for (int64_t n = 0; n < M; n++) {
+    const edmd_log_entry L = log[n];
+    const int i = L.i, j = L.j;
+    const double mi = d[i].m, mj = d[j].m;
+    const double ti = tl[i], tj = tl[j];
+    double* Ri = T + (size_t)4 * i * K;
+    double* Rj = T + (size_t)4 * j * K;
+    if (k < K) {
+      double xi = Ri[k], yi = Ri[K + k], vxi = Ri[2 * K + k], vyi = Ri[3 * K + k];
+      double xj = Rj[k], yj = Rj[K + k], vxj = Rj[2 * K + k], vyj = Rj[3 * K + k];
+      // free flight to the collision
+      xi += vxi * (L.t - ti); yi += vyi * (L.t - ti);
+      xj += vxj * (L.t - tj); yj += vyj * (L.t - tj);
+      const double rv = L.dx * L.dvx + L.dy * L.dvy;
+      const double drx = xj - xi, dry = yj - yi, dvx = vxj - vxi, dvy = vyj - vyi;
+      const double dtc = -(L.dx * drx + L.dy * dry) / rv;
+      const double rcx = drx + L.dvx * dtc, rcy = dry + L.dvy * dtc;
+      const double df = (L.f / rv) * (L.dvx * rcx + L.dvy * rcy + L.dx * dvx + L.dy * dvy);
+      const double wx = df * L.dx + L.f * rcx, wy = df * L.dy + L.f * rcy;
+      const double Dvix = L.f * mj * L.dx, Dviy = L.f * mj * L.dy;
+      const double Dvjx = -L.f * mi * L.dx, Dvjy = -L.f * mi * L.dy;
+      Ri[k] = xi - Dvix * dtc;       Ri[K + k] = yi - Dviy * dtc;
+      Rj[k] = xj - Dvjx * dtc;       Rj[K + k] = yj - Dvjy * dtc;
+      Ri[2 * K + k] = vxi + mj * wx; Ri[3 * K + k] = vyi + mj * wy;
+      Rj[2 * K + k] = vxj - mi * wx; Rj[3 * K + k] = vyj - mi * wy;
+    }
+    __syncwarp();
+    if (k == 0) { tl[i] = L.t; tl[j] = L.t; }
+    __syncwarp();
+  }
+}
+
+// value of row e at the common time tq (virtual free flight, T itself unchanged)
+__device__ __forceinline__ double row_at(const double* T, const double* tl, int e, int k, int K,
+                                         double tq) {
+  int c = e & 3;
+  double v = T[(size_t)e * K + k];
+  if (c < 2) v += T[(size_t)(e + 2) * K + k] * (tq - tl[e >> 2]);
+  return v;
+}
+
+// Gram matrix G = T'^T T' of the tangent vectors flown to tq (G zeroed before)
+__global__ void k_gram(const double* __restrict__ T, const double* __restrict__ tl, int N, int K,
+                       double tq, double* __restrict__ G) {
+  __shared__ double rows[32][33];
+  const int k = threadIdx.x & 31, l = threadIdx.x >> 5;   // 32 x 32 threads
+  double acc = 0;
+  for (int e0 = blockIdx.x * 32; e0 < 4 * N; e0 += gridDim.x * 32) {
+    int e = e0 + l;
+    rows[l][k] = (e < 4 * N && k < K) ? row_at(T, tl, e, k, K, tq) : 0.0;
+    __syncthreads();
+    if (k < K && l < K)
+      for (int r = 0; r < 32; r++) acc += rows[r][k] * rows[r][l];
+    __syncthreads();
+  }
+  if (k < K && l < K) atomicAdd(&G[k * K + l], acc);
+}
+
+// Cholesky G = R^T R (R upper), logs of diag(R) accumulated, Rinv = R^-1
+__global__ void k_chol(const double* __restrict__ G, int K, double* __restrict__ Rinv,
+                       double* __restrict__ logdiag, int accumulate, int* __restrict__ fail) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double R[32][32];
+  for (int a = 0; a < K; a++)
+    for (int b = 0; b < K; b++) R[a][b] = 0;
+  for (int jj = 0; jj < K; jj++) {
+    double s = G[jj * K + jj];
+    for (int p = 0; p < jj; p++) s -= R[p][jj] * R[p][jj];
+    if (!(s > 0)) { *fail = 1; return; }
+    R[jj][jj] = sqrt(s);
+    for (int c = jj + 1; c < K; c++) {
+      double u = G[jj * K + c];
+      for (int p = 0; p < jj; p++) u -= R[p][jj] * R[p][c];
+      R[jj][c] = u / R[jj][jj];
+    }
+  }
+  if (accumulate)
+    for (int a = 0; a < K; a++) logdiag[a] += log(R[a][a]);
+  // invert the upper-triangular R column by column
+  for (int c = 0; c < K; c++) {
+    for (int a = K - 1; a >= 0; a--) {
+      double s = (a == c) ? 1.0 : 0.0;
+      for (int p = a + 1; p < K; p++) s -= R[a][p] * Rinv[p * K + c];
+      Rinv[a * K + c] = s / R[a][a];
+    }
+  }
+}
+
+// T <- T' Rinv at the common time tq (every disk's tangent clock set to tq)
+__global__ void k_apply_rinv(double* __restrict__ T, double* __restrict__ tl, int N, int K, double tq,
+                             const double* __restrict__ Rinv) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  double row[4][32];
+  for (int c = 0; c < 4; c++)
+    for (int k = 0; k < K; k++) row[c][k] = row_at(T, tl, 4 * i + c, k, K, tq);
+  for (int c = 0; c < 4; c++)
+    for (int k = 0; k < K; k++) {
+      double s = 0;
+      for (int l = 0; l <= k; l++) s += row[c][l] * Rinv[l * K + k];
+      T[(size_t)(4 * i + c) * K + k] = s;
+    }
+  tl[i] = tq;
+}
+
+// ---------------------------------------------------------------- adjoint kernels
+
+// one thread: sweep a segment of the log backwards, applying the transpose of
+// the collision map and of the free flights between collisions.
+// A is [N][4]: (g_x, g_y, g_vx, g_vy) of each disk at its time ta[i].
+__global__ void k_adjoint_segment(const edmd_log_entry* __restrict__ log, int64_t M,
+                                  const Disk* __restrict__ d, double* __restrict__ A,
+                                  double* __restrict__ ta) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  for (int64_t n = M - 1; n >= 0; n--) {
+    const edmd_log_entry L = log[n];
+    const int i = L.i, j = L.j;
+    const double mi = d[i].m, mj = d[j].m;
+    double* ai = A + 4 * (size_t)i;
+    double* aj = A + 4 * (size_t)j;
+    // transpose of the free flights from the collision to each disk's adjoint time
+    double gxi = ai[0], gyi = ai[1], gvxi = ai[2] + ai[0] * (ta[i] - L.t), gvyi = ai[3] + ai[1] * (ta[i] - L.t);
+    double gxj = aj[0], gyj = aj[1], gvxj = aj[2] + aj[0] * (ta[j] - L.t), gvyj = aj[3] + aj[1] * (ta[j] - L.t);
+    const double rv = L.dx * L.dvx + L.dy * L.dvy;
+    const double Dvix = L.f * mj * L.dx, Dviy = L.f * mj * L.dy;
+    const double Dvjx = -L.f * mi * L.dx, Dvjy = -L.f * mi * L.dy;
+    // w enters dv_i' with +m_j and dv_j' with -m_i
+    const double gwx = mj * gvxi - mi * gvxj, gwy = mj * gvyi - mi * gvyj;
+    // dt_c enters the positions through -Dv dt_c
+    double gdt = -(Dvix * gxi + Dviy * gyi) - (Dvjx * gxj + Dvjy * gyj);
+    // w = df r + f drc
+    const double gdf = L.dx * gwx + L.dy * gwy;
+    double grcx = L.f * gwx, grcy = L.f * gwy;
+    // df = (f/rv) (v . drc + r . dv_ij)
+    const double s = (L.f / rv) * gdf;
+    grcx += s * L.dvx; grcy += s * L.dvy;
+    const double gdvx = s * L.dx, gdvy = s * L.dy;
+    // drc = dr_ij + v dt_c
+    gdt += L.dvx * grcx + L.dvy * grcy;
+    // dt_c = -(r . dr_ij)/rv
+    const double grx = grcx - (gdt / rv) * L.dx, gry = grcy - (gdt / rv) * L.dy;
+    // dr_ij = dr_j - dr_i, dv_ij = dv_j - dv_i
+    ai[0] = gxi - grx; ai[1] = gyi - gry; ai[2] = gvxi - gdvx; ai[3] = gvyi - gdvy;
+    aj[0] = gxj + grx; aj[1] = gyj + gry; aj[2] = gvxj + gdvx; aj[3] = gvyj + gdvy;
+    ta[i] = L.t; ta[j] = L.t;
+  }
+}
+
+// every disk's adjoint brought back to t0 (transpose of the first free flight)
+__global__ void k_adjoint_finish(int N, double* __restrict__ A, const double* __restrict__ ta, double t0) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  A[4 * i + 2] += A[4 * i + 0] * (ta[i] - t0);
+  A[4 * i + 3] += A[4 * i + 1] * (ta[i] - t0);
+}
+
+__global__ void k_fill(double* p, int64_t n, double v) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) p[i] = v;
+}
+
+// positions of one system flown (virtually) to time t, without touching the state
+__global__ void k_positions_at(const Disk* __restrict__ d, int N, double t, double* __restrict__ x,
+                               double* __restrict__ y) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  Disk p = d[i];
+  x[i] = p.x + p.vx * (t - p.tl);
+  y[i] = p.y + p.vy * (t - p.tl);
+}
+
+}  // namespace
+
+// ==================================================================== log + checkpoints
+
+static int upload_sysdev(edmd_ctx* ctx) {
+  CK(cudaMemcpyAsync(ctx->ds, ctx->hs.data(), ctx->nsys * sizeof(SysDev), cudaMemcpyHostToDevice,
+                     ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return EDMD_OK;
+}
+
+extern "C" int edmd_set_log_capacity(edmd_ctx* ctx, int64_t cap) {
+  if (!ctx || cap < 0) return EDMD_ERR_ARG;
+  if (cap > ctx->log_cap) {
+    if (ctx->logbuf) cudaFree(ctx->logbuf);
+    ctx->logbuf = nullptr;
+    CK(dalloc(&ctx->logbuf, (size_t)ctx->nsys * cap));
+    ctx->log_cap = cap;
+  }
+  for (int s = 0; s < ctx->nsys; s++) {
+    ctx->hs[s].log = ctx->logbuf + (size_t)s * ctx->log_cap;
+    ctx->hs[s].log_cap = ctx->log_cap;
+  }
+  return upload_sysdev(ctx);
+}
+
+extern "C" int edmd_clear_log(edmd_ctx* ctx) {
+  if (!ctx) return EDMD_ERR_ARG;
+  for (int s = 0; s < ctx->nsys; s++) CK(cudaMemsetAsync(&ctx->st[s].nlog, 0, 8, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return EDMD_OK;
+}
+
+extern "C" int edmd_get_log(edmd_ctx* ctx, int32_t s, edmd_log_entry* out, int64_t cap, int64_t* n) {
+  if (!ctx || s < 0 || s >= ctx->nsys || !n) return EDMD_ERR_ARG;
+  uint64_t nl = 0;
+  CK(cudaMemcpy(&nl, &ctx->st[s].nlog, 8, cudaMemcpyDeviceToHost));
+  *n = (int64_t)nl;
+  int64_t k = (int64_t)nl < cap ? (int64_t)nl : cap;
+  if (k > ctx->log_cap) k = ctx->log_cap;
+  if (out && k > 0)
+    CK(cudaMemcpy(out, ctx->hs[s].log, k * sizeof(edmd_log_entry), cudaMemcpyDeviceToHost));
+  return (int64_t)nl > ctx->log_cap ? EDMD_ERR_CAPACITY : EDMD_OK;
+}
+
+// the arrays that make up the engine state of every system in the context
+static void state_parts(edmd_ctx* ctx, std::vector<std::pair<void*, size_t>>& parts) {
+  const size_t TN = ctx->total_N;
+  size_t TE = 0, TT = 0;
+  for (const SysDev& S : ctx->hs) {
+    TE += 2 * (size_t)S.B.N + NSPECIAL;
+    for (int h = 0; h < S.nlev; h++) TT += S.lev_cnt[h];
+  }
+  parts = {{ctx->d, TN * sizeof(Disk)}, {ctx->vr, TN * 8}, {ctx->cx, TN * 4}, {ctx->cy, TN * 4},
+           {ctx->prv, TN * 4}, {ctx->crossX, TN * 4}, {ctx->crossY, TN * 4},
+           {ctx->head, (size_t)ctx->total_C * 4}, {ctx->ev, TE * sizeof(Ev)}, {ctx->on, TE * 4},
+           {ctx->op, TE * 4}, {ctx->tree, TT * sizeof(Node)}, {ctx->st, ctx->nsys * sizeof(SysState)}};
+  if (ctx->cal) parts.push_back({ctx->cal, TN * CAL_SUB * CAL_LINE * 2});
+  if (ctx->mask) parts.push_back({ctx->mask, TN * 2});
+}
+
+extern "C" int edmd_checkpoint_save(edmd_ctx* ctx, int32_t slot) {
+  if (!ctx || slot < 0 || slot > 4096) return EDMD_ERR_ARG;
+  std::vector<std::pair<void*, size_t>> parts;
+  state_parts(ctx, parts);
+  size_t total = 0;
+  for (auto& p : parts) total += align_up(p.second, 256);
+  if ((int)ctx->ckpt.size() <= slot) ctx->ckpt.resize(slot + 1, nullptr);
+  if (!ctx->ckpt[slot]) CK(cudaMalloc(&ctx->ckpt[slot], total));
+  char* dst = (char*)ctx->ckpt[slot];
+  for (auto& p : parts) {
+    CK(cudaMemcpyAsync(dst, p.first, p.second, cudaMemcpyDeviceToDevice, ctx->stream));
+    dst += align_up(p.second, 256);
+  }
+  CK(cudaStreamSynchronize(ctx->stream));
+  return EDMD_OK;
+}
+
+extern "C" int edmd_checkpoint_restore(edmd_ctx* ctx, int32_t slot) {
+  if (!ctx || slot < 0 || slot >= (int)ctx->ckpt.size() || !ctx->ckpt[slot]) return EDMD_ERR_ARG;
+  std::vector<std::pair<void*, size_t>> parts;
+  state_parts(ctx, parts);
+  const char* src = (const char*)ctx->ckpt[slot];
+  for (auto& p : parts) {
+    CK(cudaMemcpyAsync(p.first, src, p.second, cudaMemcpyDeviceToDevice, ctx->stream));
+    src += align_up(p.second, 256);
+  }
+  CK(cudaStreamSynchronize(ctx->stream));
+  return EDMD_OK;
+}
+
+// ==================================================================== tangent driver
+
+static int current_time(edmd_ctx* ctx, int s, double* t) {
+  CK(cudaMemcpy(t, &ctx->st[s].t, 8, cudaMemcpyDeviceToHost));
+  return EDMD_OK;
+}
+
+// one advance of every system, logging collision geometry; returns the log length of `s`
+static int advance_logged(edmd_ctx* ctx, int s, int64_t ncoll, int64_t* nlog) {
+  int rc = edmd_clear_log(ctx);
+  if (rc) return rc;
+  rc = edmd_advance(ctx, ncoll, INFINITY, EDMD_F_LOG | EDMD_F_COUNT_NORMAL, (int64_t)1 << 60, nullptr);
+  if (rc) return rc;
+  uint64_t nl = 0;
+  CK(cudaMemcpy(&nl, &ctx->st[s].nlog, 8, cudaMemcpyDeviceToHost));
+  if ((int64_t)nl > ctx->log_cap) return set_err(ctx, EDMD_ERR_CAPACITY, "collision log overflow");
+  *nlog = (int64_t)nl;
+  return EDMD_OK;
+}
+
+static int cholqr(edmd_ctx* ctx, double* T, double* tl, int N, int K, double tq, double* G,
+                  double* Rinv, double* logdiag, int* fail, bool accumulate) {
+  for (int pass = 0; pass < 2; pass++) {    // CholQR2: the second pass restores orthogonality
+    CK(cudaMemsetAsync(G, 0, K * K * sizeof(double), ctx->stream));
+    int blocks = (4 * N + 31) / 32;
+    if (blocks > 1024) blocks = 1024;
+    k_gram<<<blocks, 1024, 0, ctx->stream>>>(T, tl, N, K, tq, G);
+    k_chol<<<1, 1, 0, ctx->stream>>>(G, K, Rinv, logdiag, accumulate ? 1 : 0, fail);
+    k_apply_rinv<<<(N + 127) / 128, 128, 0, ctx->stream>>>(T, tl, N, K, tq, Rinv);
+    CK(cudaGetLastError());
+  }
+  int h = 0;
+  CK(cudaMemcpy(&h, fail, 4, cudaMemcpyDeviceToHost));
+  if (h) return set_err(ctx, EDMD_ERR_ARG, "tangent vectors became linearly dependent");
+  return EDMD_OK;
+}
+
+extern "C" int edmd_tangent_run(edmd_ctx* ctx, int32_t s, int32_t K, int64_t n_coll, int64_t qr_every,
+                                uint64_t seed, double* tangent_io, double* lyap_out) {
+  if (!ctx || s < 0 || s >= ctx->nsys || K < 1 || K > 32 || n_coll < 0 || qr_every < 0)
+    return EDMD_ERR_ARG;
+  if (ctx->engine != EDMD_ENGINE_WARP) return set_err(ctx, EDMD_ERR_ARG, "tangents need the warp engine");
+  const int N = ctx->hs[s].B.N;
+  int64_t chunk = qr_every > 0 ? qr_every : (n_coll > 0 ? n_coll : 1);
+  int rc = edmd_set_log_capacity(ctx, chunk + 16);
+  if (rc) return rc;
+  double *T = nullptr, *tl = nullptr, *G = nullptr, *Rinv = nullptr, *logdiag = nullptr;
+  int* fail = nullptr;
+  CK(dalloc(&T, (size_t)4 * N * K));
+  CK(dalloc(&tl, N));
+  CK(dalloc(&G, K * K));
+  CK(dalloc(&Rinv, K * K));
+  CK(dalloc(&logdiag, K));
+  CK(dalloc(&fail, 1));
+  struct Free { void* p[6]; ~Free() { for (void* q : p) if (q) cudaFree(q); } } guard{{T, tl, G, Rinv, logdiag, fail}};
+  double t0;
+  if ((rc = current_time(ctx, s, &t0))) return rc;
+  // initial vectors: the caller's ([K][N][4]) or seeded random orthonormal ones
+  std::vector<double> h((size_t)4 * N * K);
+  if (tangent_io) {
+    for (int k = 0; k < K; k++)
+      for (int e = 0; e < 4 * N; e++) h[(size_t)e * K + k] = tangent_io[(size_t)k * 4 * N + e];
+  } else {
+    std::mt19937_64 g(seed);
+    std::normal_distribution<double> nd(0.0, 1.0);
+    for (auto& v : h) v = nd(g);
+  }
+  CK(cudaMemcpyAsync(T, h.data(), h.size() * 8, cudaMemcpyHostToDevice, ctx->stream));
+  k_fill<<<(N + 255) / 256, 256, 0, ctx->stream>>>(tl, N, t0);
+  CK(cudaMemsetAsync(logdiag, 0, K * sizeof(double), ctx->stream));
+  CK(cudaMemsetAsync(fail, 0, 4, ctx->stream));
+  if (!tangent_io && (rc = cholqr(ctx, T, tl, N, K, t0, G, Rinv, logdiag, fail, false))) return rc;
+  int64_t done = 0;
+  double t = t0;
+  while (done < n_coll) {
+    int64_t want = n_coll - done < chunk ? n_coll - done : chunk;
+    int64_t nl = 0;
+    if ((rc = advance_logged(ctx, s, want, &nl))) return rc;
+    k_tangent_apply<<<1, 32, 0, ctx->stream>>>((const edmd_log_entry*)ctx->hs[s].log, nl, ctx->hs[s].d, T, tl, K);
+    CK(cudaGetLastError());
+    if ((rc = current_time(ctx, s, &t))) return rc;
+    if (qr_every > 0 && (rc = cholqr(ctx, T, tl, N, K, t, G, Rinv, logdiag, fail, true))) return rc;
+    done += want;
+    if (nl < want) break;     // the run ended early (tmax or t_stop)
+  }
+  if (lyap_out) {
+    std::vector<double> ld(K);
+    CK(cudaMemcpy(ld.data(), logdiag, K * 8, cudaMemcpyDeviceToHost));
+    for (int k = 0; k < K; k++) lyap_out[k] = (t > t0) ? ld[k] / (t - t0) : 0.0;
+  }
+  if (tangent_io) {
+    // tangents at the final time (virtual flight of every row)
+    CK(cudaMemcpy(h.data(), T, h.size() * 8, cudaMemcpyDeviceToHost));
+    std::vector<double> htl(N);
+    CK(cudaMemcpy(htl.data(), tl, N * 8, cudaMemcpyDeviceToHost));
+    for (int k = 0; k < K; k++)
+      for (int i = 0; i < N; i++)
+        for (int c = 0; c < 4; c++) {
+          double v = h[(size_t)(4 * i + c) * K + k];
+          if (c < 2) v += h[(size_t)(4 * i + c + 2) * K + k] * (t - htl[i]);
+          tangent_io[(size_t)k * 4 * N + 4 * i + c] = v;
+        }
+  }
+  return EDMD_OK;
+}
+
+// ==================================================================== adjoint driver
+
+extern "C" int edmd_msd_gradient(edmd_ctx* ctx, int32_t s, int64_t n_coll, int64_t ckpt_every,
+                                 double t_obs, double* msd_out, double* g_vx, double* g_vy,
+                                 double* g_x, double* g_y) {
+  if (!ctx || s < 0 || s >= ctx->nsys || n_coll < 1 || ckpt_every < 1) return EDMD_ERR_ARG;
+  if (ctx->engine != EDMD_ENGINE_WARP) return set_err(ctx, EDMD_ERR_ARG, "adjoints need the warp engine");
+  const int N = ctx->hs[s].B.N;
+  const double Lx = ctx->hs[s].B.Lx, Ly = ctx->hs[s].B.Ly;
+  int rc = edmd_set_log_capacity(ctx, ckpt_every + 16);
+  if (rc) return rc;
+  double *A = nullptr, *ta = nullptr, *px = nullptr, *py = nullptr;
+  CK(dalloc(&A, 4 * (size_t)N));
+  CK(dalloc(&ta, N));
+  CK(dalloc(&px, N));
+  CK(dalloc(&py, N));
+  struct Free { void* p[4]; ~Free() { for (void* q : p) if (q) cudaFree(q); } } guard{{A, ta, px, py}};
+  double t0, T;
+  if ((rc = current_time(ctx, s, &t0))) return rc;
+  std::vector<double> x0(N), y0(N), x1(N), y1(N);
+  k_positions_at<<<(N + 127) / 128, 128, 0, ctx->stream>>>(ctx->hs[s].d, N, t0, px, py);
+  CK(cudaMemcpyAsync(x0.data(), px, N * 8, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(y0.data(), py, N * 8, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  // forward sweep: exact engine checkpoints at every segment boundary
+  const int64_t nseg = (n_coll + ckpt_every - 1) / ckpt_every;
+  std::vector<int64_t> seglen(nseg);
+  for (int64_t g = 0; g < nseg; g++) {
+    if ((rc = edmd_checkpoint_save(ctx, (int32_t)g))) return rc;
+    seglen[g] = (g == nseg - 1) ? n_coll - g * ckpt_every : ckpt_every;
+    rc = edmd_advance(ctx, seglen[g], INFINITY, EDMD_F_COUNT_NORMAL, (int64_t)1 << 60, nullptr);
+    if (rc) return rc;
+  }
+  if ((rc = edmd_checkpoint_save(ctx, (int32_t)nseg))) return rc;
+  if ((rc = current_time(ctx, s, &T))) return rc;
+  if (t_obs >= 0) {
+    if (t_obs < T) return set_err(ctx, EDMD_ERR_ARG, "t_obs precedes the last processed event");
+    T = t_obs;
+  }
+  k_positions_at<<<(N + 127) / 128, 128, 0, ctx->stream>>>(ctx->hs[s].d, N, T, px, py);
+  CK(cudaMemcpyAsync(x1.data(), px, N * 8, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(y1.data(), py, N * 8, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  // MSD = (1/N) sum |u_i - mean(u)|^2, u = minimum-image displacement
+  std::vector<double> ux(N), uy(N);
+  double mx = 0, my = 0;
+  for (int i = 0; i < N; i++) {
+    double dx = x1[i] - x0[i], dy = y1[i] - y0[i];
+    dx -= Lx * std::nearbyint(dx / Lx);
+    dy -= Ly * std::nearbyint(dy / Ly);
+    ux[i] = dx; uy[i] = dy; mx += dx; my += dy;
+  }
+  mx /= N; my /= N;
+  double msd = 0;
+  std::vector<double> hA(4 * (size_t)N, 0.0);
+  for (int i = 0; i < N; i++) {
+    double a = ux[i] - mx, b = uy[i] - my;
+    msd += a * a + b * b;
+    hA[4 * i + 0] = 2.0 * a / N;
+    hA[4 * i + 1] = 2.0 * b / N;
+  }
+  msd /= N;
+  CK(cudaMemcpyAsync(A, hA.data(), hA.size() * 8, cudaMemcpyHostToDevice, ctx->stream));
+  k_fill<<<(N + 255) / 256, 256, 0, ctx->stream>>>(ta, N, T);
+  // reverse sweep: recompute each segment from its checkpoint, then its adjoint
+  for (int64_t g = nseg - 1; g >= 0; g--) {
+    if ((rc = edmd_checkpoint_restore(ctx, (int32_t)g))) return rc;
+    int64_t nl = 0;
+    if ((rc = advance_logged(ctx, s, seglen[g], &nl))) return rc;
+    k_adjoint_segment<<<1, 1, 0, ctx->stream>>>((const edmd_log_entry*)ctx->hs[s].log, nl, ctx->hs[s].d, A, ta);
+    CK(cudaGetLastError());
+  }
+  k_adjoint_finish<<<(N + 127) / 128, 128, 0, ctx->stream>>>(N, A, ta, t0);
+  CK(cudaMemcpyAsync(hA.data(), A, hA.size() * 8, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  // leave the engine at the end of the run
+  if ((rc = edmd_checkpoint_restore(ctx, (int32_t)nseg))) return rc;
+  for (int i = 0; i < N; i++) {
+    if (g_x) g_x[i] = hA[4 * i + 0];
+    if (g_y) g_y[i] = hA[4 * i + 1];
+    if (g_vx) g_vx[i] = hA[4 * i + 2];
+    if (g_vy) g_vy[i] = hA[4 * i + 3];
+  }
+  if (msd_out) *msd_out = msd;
+  return EDMD_OK;
+}

@@ -21,7 +21,7 @@ LIB_PATH = os.path.join(HERE, "libedmd_gpu.so")
 
 OK, ERR_ARG, ERR_CUDA, ERR_OVERLAP, ERR_BUDGET, ERR_CAPACITY, ERR_NODEV = range(7)
 STOP_COLL, STOP_TIME, STOP_TMAX, STOP_SCREEN, STOP_GROW = 1, 2, 3, 4, 5
-F_STOP_AT_SCREEN, F_STOP_AT_GROW, F_TRACE, F_COUNT_NORMAL = 1, 2, 4, 8
+F_STOP_AT_SCREEN, F_STOP_AT_GROW, F_TRACE, F_COUNT_NORMAL, F_LOG = 1, 2, 4, 8, 16
 ENGINE_AUTO, ENGINE_WARP, ENGINE_LANE = 0, 1, 2
 
 
@@ -36,6 +36,9 @@ class Collision(C.Structure):
     _fields_ = [("i", C.c_int32), ("j", C.c_int32), ("cell_i", C.c_int32), ("cell_j", C.c_int32),
                 ("t", C.c_double)]
 
+
+LOG_DTYPE = np.dtype([("i", "<i4"), ("j", "<i4"), ("t", "<f8"), ("dx", "<f8"), ("dy", "<f8"),
+                      ("dvx", "<f8"), ("dvy", "<f8"), ("f", "<f8")])
 
 COLLISION_DTYPE = np.dtype([("i", "<i4"), ("j", "<i4"), ("cell_i", "<i4"), ("cell_j", "<i4"),
                             ("t", "<f8")])
@@ -54,7 +57,8 @@ EXPORTS = [
     "edmd_get_states", "edmd_get_counters", "edmd_get_all_counters", "edmd_get_virial",
     "edmd_get_thermo", "edmd_get_trace", "edmd_set_engine", "edmd_set_lane_threads",
     "edmd_get_engine", "edmd_set_device", "edmd_host_alloc", "edmd_host_free", "edmd_run_noalloc",
-    "edmd_destroy",
+    "edmd_set_log_capacity", "edmd_clear_log", "edmd_get_log", "edmd_checkpoint_save",
+    "edmd_checkpoint_restore", "edmd_tangent_run", "edmd_msd_gradient", "edmd_destroy",
     "edmd_last_error", "edmd_device_info",
     "edmd_mt_seed", "edmd_mt_u32", "edmd_mt_double", "edmd_hex_size", "edmd_random_size",
     "edmd_grow_rate", "edmd_normalize", "edmd_init_hex", "edmd_init_grow", "edmd_default_desc",
@@ -85,6 +89,14 @@ def load(path=LIB_PATH):
     L.edmd_host_free.argtypes = [C.c_void_p]
     L.edmd_set_device.argtypes = [C.c_int32]
     L.edmd_set_engine.argtypes = [C.c_int32]
+    L.edmd_set_log_capacity.argtypes = [C.c_void_p, C.c_int64]
+    L.edmd_clear_log.argtypes = [C.c_void_p]
+    L.edmd_get_log.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_int64, C.POINTER(C.c_int64)]
+    L.edmd_checkpoint_save.argtypes = [C.c_void_p, C.c_int32]
+    L.edmd_checkpoint_restore.argtypes = [C.c_void_p, C.c_int32]
+    L.edmd_tangent_run.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int64, C.c_int64, C.c_uint64,
+                                   C.c_void_p, C.c_void_p]
+    L.edmd_msd_gradient.argtypes = [C.c_void_p, C.c_int32, C.c_int64, C.c_int64, C.c_double] + [C.c_void_p] * 5
     L.edmd_run_noalloc.argtypes = [C.POINTER(SystemDesc)] + [C.c_void_p] * 6 + [
         C.c_int64, C.c_double, C.POINTER(C.c_int64), C.POINTER(C.c_double), C.c_void_p]
     L.edmd_set_lane_threads.argtypes = [C.c_int32]
@@ -248,6 +260,39 @@ class Engine:
         arr = (Counters * self.n)()
         self._ck(self._L.edmd_get_all_counters(self.h, C.cast(arr, C.c_void_p)))
         return {k: np.array([getattr(c, k) for c in arr]) for k, _ in Counters._fields_}
+
+    # ---- differentiation
+    def checkpoint_save(self, slot):
+        self._ck(self._L.edmd_checkpoint_save(self.h, slot))
+
+    def checkpoint_restore(self, slot):
+        self._ck(self._L.edmd_checkpoint_restore(self.h, slot))
+
+    def log(self, s=0, cap=1 << 20):
+        out = np.zeros(cap, LOG_DTYPE)
+        n = C.c_int64()
+        rc = self._L.edmd_get_log(self.h, s, _ptr(out), cap, C.byref(n))
+        if rc not in (OK, ERR_CAPACITY):
+            self._ck(rc)
+        return out[: min(n.value, cap)]
+
+    def tangent(self, K, n_coll, qr_every=0, vectors=None, seed=1, s=0):
+        """Propagate K tangent vectors ([K][N][4] array or random); returns (vectors, exponents)."""
+        N = self.N[s]
+        vec = None if vectors is None else np.ascontiguousarray(vectors, np.float64).reshape(K, N, 4).copy()
+        lyap = np.zeros(K)
+        self._ck(self._L.edmd_tangent_run(self.h, s, K, int(n_coll), int(qr_every), int(seed),
+                                          _ptr(vec), _ptr(lyap)))
+        return vec, lyap
+
+    def msd_gradient(self, n_coll, ckpt_every=500, t_obs=-1.0, s=0):
+        """Final MSD and its gradient w.r.t. the current velocities and positions."""
+        N = self.N[s]
+        g = {k: np.zeros(N) for k in ("vx", "vy", "x", "y")}
+        msd = C.c_double()
+        self._ck(self._L.edmd_msd_gradient(self.h, s, int(n_coll), int(ckpt_every), float(t_obs), C.byref(msd),
+                                           _ptr(g["vx"]), _ptr(g["vy"]), _ptr(g["x"]), _ptr(g["y"])))
+        return msd.value, g
 
     def counters(self, s=0):
         c = Counters()

@@ -55,6 +55,7 @@ extern "C" {
 #define EDMD_F_STOP_AT_GROW    2u  /* return after the growth-stop event      */
 #define EDMD_F_TRACE           4u  /* record accepted collisions              */
 #define EDMD_F_COUNT_NORMAL    8u  /* max_coll counts normal-phase only       */
+#define EDMD_F_LOG            16u  /* record collision geometry (edmd_log_entry) */
 
 /*
  * One periodic 2D system.  Replaces the globals that constantInit
@@ -79,6 +80,16 @@ typedef struct edmd_collision {
 	int32_t cell_i, cell_j;/* linear cells Y*Nxcells+X                         */
 	double  t;
 } edmd_collision;
+
+/* geometry of one accepted normal-phase collision, enough to differentiate
+ * the elastic map of doTheCollisionNormal (src/EDMD.c:3587-3827) */
+typedef struct edmd_log_entry {
+	int32_t i, j;          /* owner and partner                               */
+	double  t;             /* collision time                                  */
+	double  dx, dy;        /* r_j - r_i at contact (nearest periodic image)   */
+	double  dvx, dvy;      /* v_j - v_i before the collision                  */
+	double  f;             /* funkyFactor: v_i += f m_j (dx,dy), v_j -= f m_i (dx,dy) */
+} edmd_log_entry;
 
 /* per-system counters, cumulative since creation */
 typedef struct edmd_counters {
@@ -160,6 +171,44 @@ int edmd_get_engine(const edmd_ctx* ctx);
 /* Select the CUDA device used by contexts created afterwards in this thread
  * (one process per GPU). */
 int edmd_set_device(int32_t dev);
+
+/* ---- differentiation (no counterpart in the reference, which has no derivatives) */
+
+/* Per-system capacity of the collision-geometry log written under
+ * EDMD_F_LOG; edmd_clear_log resets the logs, edmd_get_log reads one. */
+int edmd_set_log_capacity(edmd_ctx* ctx, int64_t cap);
+int edmd_clear_log(edmd_ctx* ctx);
+int edmd_get_log(edmd_ctx* ctx, int32_t sys, edmd_log_entry* out, int64_t cap, int64_t* n);
+
+/* Exact binary checkpoints of the whole engine state of every system (disks,
+ * cell lists, queue, counters): restoring and advancing again reproduces the
+ * same events bit for bit. */
+int edmd_checkpoint_save(edmd_ctx* ctx, int32_t slot);
+int edmd_checkpoint_restore(edmd_ctx* ctx, int32_t slot);
+
+/* Tangent-linear run.  Advances the context n_coll accepted collisions while
+ * propagating K <= 32 tangent vectors of system `sys` through the free
+ * flights and collisions (the Dellago-Posch-Hoover map).  tangent_io, if not
+ * NULL, holds K vectors [K][N][4] (dx, dy, dvx, dvy per disk) on entry and
+ * the propagated vectors at the final time on return; if NULL, random
+ * orthonormal vectors from `seed` are used.  With qr_every > 0 the vectors are
+ * re-orthonormalised every qr_every collisions (Cholesky QR, twice) and
+ * lyap_out (K entries, may be NULL) receives the Lyapunov exponents
+ * sum(log R_kk) / elapsed time.  Single-system contexts; warp engine. */
+int edmd_tangent_run(edmd_ctx* ctx, int32_t sys, int32_t K, int64_t n_coll, int64_t qr_every,
+                     uint64_t seed, double* tangent_io, double* lyap_out);
+
+/* Adjoint of the final mean-square displacement.  Advances n_coll accepted
+ * collisions from the current state, with exact engine checkpoints every
+ * ckpt_every collisions; the reverse pass recomputes each segment from its
+ * checkpoint and applies the transposed collision and free-flight maps.
+ * The observable is taken at t_obs (>= the time of the last processed event;
+ * t_obs < 0 means that time): msd_out = (1/N) sum |u_i - <u>|^2 with u the
+ * minimum-image displacement; g_vx, g_vy (g_x, g_y) receive d MSD / d v(0)
+ * (d r(0)) at fixed t_obs; any may be NULL.  The context is left at the end
+ * of the run.  Single-system contexts; warp engine. */
+int edmd_msd_gradient(edmd_ctx* ctx, int32_t sys, int64_t n_coll, int64_t ckpt_every, double t_obs,
+                      double* msd_out, double* g_vx, double* g_vy, double* g_x, double* g_y);
 
 /* Page-locked host buffers for fast host<->device staging. */
 int edmd_host_alloc(void** p, int64_t bytes);
