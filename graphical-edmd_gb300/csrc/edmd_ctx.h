@@ -38,8 +38,18 @@ struct edmd_ctx {
   uint16_t* mask = nullptr;
   int engine = 0;                   // EDMD_ENGINE_WARP or EDMD_ENGINE_LANE
   int64_t total_C = 0;
+  void* round = nullptr;            // buffers of the round-parallel engine (edmd_round.cu)
+  bool round_dirty = false;         // queue order lost: set by the round engine, cleared by a restage
+  std::vector<char> ckpt_dirty;     // round_dirty of each checkpoint
   std::string err;
 };
+
+void round_free(edmd_ctx* ctx);
+// device copies of the whole engine state (edmd_tangent.cu); slots above the
+// public range are internal
+constexpr int32_t CKPT_PUBLIC_MAX = 4096, CKPT_ROUND = 4097;
+int ckpt_save(edmd_ctx* ctx, int32_t slot);
+int ckpt_restore(edmd_ctx* ctx, int32_t slot);
 
 static inline int set_err(edmd_ctx* c, int code, const std::string& m) {
   if (c) c->err = m;

@@ -829,6 +829,7 @@ extern "C" int edmd_device_info(char* name, int32_t cap, int32_t* sm_count) {
 static int stage_all(edmd_ctx* ctx, const double* x, const double* y, const double* vx,
                      const double* vy, const double* rad, const double* m, const double* vr,
                      bool restart) {
+  ctx->round_dirty = false;
   const int64_t TN = ctx->total_N;
   std::vector<Disk> hd(TN);
   std::vector<int32_t> hcx(TN), hcy(TN), hprv(TN);
@@ -1005,6 +1006,8 @@ extern "C" int edmd_advance(edmd_ctx* ctx, int64_t max_coll, double t_stop, uint
                             int64_t max_events, float* elapsed_ms) {
   if (!ctx) return EDMD_ERR_ARG;
   if (max_coll < 0 || max_events <= 0) return set_err(ctx, EDMD_ERR_ARG, "bad advance limits");
+  if (ctx->round_dirty)
+    return set_err(ctx, EDMD_ERR_ARG, "advanced by the round engine: reload the state with edmd_load_state");
   RunArgs A;
   A.max_coll = max_coll; A.t_stop = t_stop; A.flags = flags; A.max_events = max_events;
   A.nsys = ctx->nsys; A.work = ctx->work;
@@ -1157,11 +1160,15 @@ extern "C" int edmd_host_free(void* p) {
 extern "C" int edmd_destroy(edmd_ctx* ctx) {
   if (!ctx) return EDMD_OK;
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  round_free(ctx);
   void* ptrs[] = {ctx->d, ctx->vr, ctx->cx, ctx->cy, ctx->prv, ctx->crossX, ctx->crossY, ctx->head,
                   ctx->ev, ctx->on, ctx->op, ctx->tree, ctx->st, ctx->trace, ctx->rows, ctx->stage,
                   ctx->work, ctx->ds, ctx->cal, ctx->mask};
   for (void* p : ptrs)
     if (p) cudaFree(p);
+  for (void* p : ctx->ckpt)
+    if (p) cudaFree(p);
+  if (ctx->logbuf) cudaFree(ctx->logbuf);
   if (ctx->e0) cudaEventDestroy(ctx->e0);
   if (ctx->e1) cudaEventDestroy(ctx->e1);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);

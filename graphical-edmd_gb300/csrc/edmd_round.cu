@@ -1,0 +1,1034 @@
+// edmd_round.cu -- round-parallel event engine: the causally independent events
+// of one large system, or of a whole batch, processed at once, one thread per
+// event.
+//
+// Every disk has one pending event: the earlier of its crossing event
+// (crossingEventNormal, src/EDMD.c:2405) and its collision event
+// (collisionEventNormal, src/EDMD.c:2829).  The event's footprint is the
+// owner's cell plus the target cell (crossing) or the partner's cell at
+// prediction time (collision; the partner stays in the owner's 3x3 block until
+// the contact unless it collides first, which makes the event stale).
+// Processing writes disks, lists and events of the owner's cell and the
+// partner's current cell (a neighbour of the owner's), and reads the 3x3
+// cells around them: everything lies within two cells of the owner's cell and
+// the writes within one, so events whose footprints are more than three cells
+// apart never touch the same data (window radius r >= 3).  Each round:
+//   1. per cell, the minimum (time key, owner) of the events attributed to it
+//      is kept up to date incrementally;
+//   2. a tile kernel reduces those minima over square windows of radius r in
+//      shared memory and selects every eligible event (before the system's
+//      next screenshot, t_stop and its collision budget) that is the window
+//      minimum at both of its footprint cells: no earlier pending event lies
+//      within r cells, and selected events are more than r cells apart;
+//   3. the selected events are processed, one thread each, with the
+//      arithmetic of the serial engines;
+//   4. the cell minima around them are recomputed, and systems with nothing
+//      left before their screenshot pass it (every disk free-flown to it).
+// Events created inside a round can still precede a processed event (a chain
+// of new events crossing r cells faster than the time gap).  That is detected,
+// never silently accepted: each event carries the serial engine's pop clock
+// at its processing (max of its time and its creator's clock), every cell
+// keeps the largest clock of the events that wrote it (lw) and read it (lr),
+// and an event that writes a cell with a later lw or lr, or reads one with a
+// later lw, is counted as a causality violation.  With none, every disk sees
+// the serial sequence of events, so the state is the reference's; only the
+// summation order of the virial and the order of the trace differ.  Mutual
+// equal-time predictions (a->b and b->a) resolve to the smaller owner; both
+// orders give bit-identical velocities since the collision rule is odd in
+// (dx, dy) and in (dvx, dvy).
+#include <cstdio>
+#include <cstring>
+#include "edmd_ctx.h"
+
+namespace {
+
+constexpr uint64_t KINF = ~0ull;
+constexpr int32_t IINF = 0x7fffffff;
+constexpr unsigned FULLM = 0xffffffffu;
+constexpr int TX = 32, TY = 8;        // selection tile (cells)
+constexpr int RTILE = 12;             // largest window radius of the tile kernel
+constexpr int MAXDIRTY = 8;           // cells whose minimum one event can change
+constexpr int MAXC = 8;               // candidates buffered per cell list per lane
+constexpr int WPB = 8;                // warps per block of the processing kernel
+constexpr int NSTRIPE = 32;           // copies of each system's counters
+// counters of the round engine, per system and stripe (u64 slots)
+enum { C_CT0, C_CT1, C_CT2, C_CT3, C_NCOL, C_NCROSS, C_NSTALE, C_NPAIR, C_NPRED, C_NEV, C_TLAST, NCNT };
+
+struct RoundArgs {
+  int32_t nsys;
+  int32_t radius;
+  int64_t TN;
+  uint32_t flags;
+  uint64_t tstop_key;
+  const int32_t* dsys;           // system of each disk
+  const int64_t* doff;           // disk offset of each system
+  const int64_t* coff;           // cell offset of each system
+  uint64_t* dkey;                // time key of each disk's next event (KINF: none)
+  int32_t* fc;                   // its two footprint cells (local), 2 per disk
+  uint64_t* cmt; int32_t* cmi;   // attributed minimum per cell
+  uint64_t* lw; uint64_t* lr;    // causality stamps per cell
+  int32_t* safe; int32_t* nsafe; // selected events of the round
+  int32_t* dcell;                // cells to recompute, MAXDIRTY per selected event
+  int32_t* selflag;              // some event of the system was selected
+  int32_t* active;               // systems still running after the round
+  uint64_t* lim;                 // per-system bound on eligible keys for the round
+  const uint64_t* target;        // per-system ncol at which the budget is met
+  uint64_t* freeze;              // per-system key bound once the budget is met
+  uint64_t* tlast;               // per-system largest screenshot key passed
+  uint64_t* cnt;                 // [nsys][NSTRIPE][NCNT] counters of this call
+  const int32_t* tsys;           // tiles: system, first cell x, first cell y
+  const int32_t* tx0;
+  const int32_t* ty0;
+  unsigned long long* violations;
+};
+
+__device__ __forceinline__ bool pair_less(uint64_t t1, int32_t i1, uint64_t t2, int32_t i2) {
+  return t1 < t2 || (t1 == t2 && i1 < i2);
+}
+
+__device__ __forceinline__ double key_time(uint64_t k) {
+  uint64_t u = (k >> 63) ? (k & 0x7fffffffffffffffull) : ~k;
+  return __longlong_as_double((long long)u);
+}
+
+__device__ __forceinline__ uint64_t kmax(uint64_t a, uint64_t b) { return a > b ? a : b; }
+
+// disk i's next event slot (the crossing wins an exact tie) and its key
+__device__ __forceinline__ int next_slot(const SysDev& S, int i, uint64_t* key) {
+  const int N = S.B.N;
+  const Ev c = S.ev[i], k = S.ev[N + i];
+  uint64_t kc = (c.st & 3u) ? time_key(c.t) : KINF;
+  uint64_t kk = (k.st & 3u) ? time_key(k.t) : KINF;
+  if (kk < kc) { *key = kk; return N + i; }
+  *key = kc;
+  return kc == KINF ? -1 : i;
+}
+
+__device__ __forceinline__ int cell_of(const Box& B, int cx, int cy) { return cy * B.Nxc + cx; }
+
+// target cell of a crossing in direction dir (1..4) from (cx, cy)
+__device__ __forceinline__ int target_cell(const Box& B, int cx, int cy, int dir) {
+  switch (dir) {
+    case 1: cx = cx - 1 < 0 ? B.Nxc - 1 : cx - 1; break;
+    case 2: cx = cx + 1 >= B.Nxc ? 0 : cx + 1; break;
+    case 3: cy = cy - 1 < 0 ? B.Nyc - 1 : cy - 1; break;
+    default: cy = cy + 1 >= B.Nyc ? 0 : cy + 1; break;
+  }
+  return cell_of(B, cx, cy);
+}
+
+// cells a and b are equal or neighbours (periodic)
+__device__ __forceinline__ bool adjacent(const Box& B, int a, int b) {
+  int dx = a % B.Nxc - b % B.Nxc, dy = a / B.Nxc - b / B.Nxc;
+  if (dx > 1) dx -= B.Nxc;
+  if (dx < -1) dx += B.Nxc;
+  if (dy > 1) dy -= B.Nyc;
+  if (dy < -1) dy += B.Nyc;
+  return dx >= -1 && dx <= 1 && dy >= -1 && dy <= 1;
+}
+
+// next event key and footprint of disk i; the collision slot's `b` field holds
+// the partner's cell at prediction time
+__device__ __forceinline__ void attribution(const SysDev& S, int i, uint64_t* key, int* c1, int* c2) {
+  const int slot = next_slot(S, i, key);
+  const Box& B = S.B;
+  const int cx = S.cx[i], cy = S.cy[i];
+  *c1 = cell_of(B, cx, cy);
+  if (slot < 0) *c2 = *c1;
+  else if (slot >= B.N) *c2 = (int)S.ev[slot].b;
+  else *c2 = target_cell(B, cx, cy, S.ev[slot].j);
+}
+
+// ---------------------------------------------------------------- per call
+
+// serial pop clock and stored partner cell of every pending event, then the
+// attribution of every disk
+__global__ void k_prep(const SysDev* __restrict__ sys, RoundArgs A) {
+  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= A.TN) return;
+  const int s = A.dsys[g];
+  const SysDev& S = sys[s];
+  const Box& B = S.B;
+  const int N = B.N;
+  const int i = (int)(g - A.doff[s]);
+  const uint64_t clock = time_key(S.st->t);
+  for (int k = 0; k < 2; k++) {
+    Ev& e = S.ev[k * N + i];
+    if (!(e.st & 3u)) continue;
+    e.tie = kmax(time_key(e.t), clock);
+    if (k == 1) {
+      const int own = cell_of(B, S.cx[i], S.cy[i]);
+      const int p = e.j;
+      const int pc = cell_of(B, S.cx[p], S.cy[p]);
+      e.b = (uint32_t)(adjacent(B, own, pc) ? pc : own);
+    }
+  }
+  uint64_t key;
+  int c1, c2;
+  attribution(S, i, &key, &c1, &c2);
+  A.dkey[g] = key;
+  A.fc[2 * g] = c1;
+  A.fc[2 * g + 1] = c2;
+  if (key != KINF) {
+    atomicMin((unsigned long long*)&A.cmt[A.coff[s] + c1], (unsigned long long)key);
+    if (c2 != c1) atomicMin((unsigned long long*)&A.cmt[A.coff[s] + c2], (unsigned long long)key);
+  }
+}
+
+__global__ void k_prep_owner(RoundArgs A) {
+  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= A.TN) return;
+  const uint64_t key = A.dkey[g];
+  if (key == KINF) return;
+  const int64_t base = A.coff[A.dsys[g]];
+  const int64_t a = base + A.fc[2 * g], b = base + A.fc[2 * g + 1];
+  if (A.cmt[a] == key) atomicMin(&A.cmi[a], (int32_t)g);
+  if (b != a && A.cmt[b] == key) atomicMin(&A.cmi[b], (int32_t)g);
+}
+
+// eligibility bound of every system for the next round
+__device__ __forceinline__ uint64_t system_limit(const SysDev& S, const RoundArgs& A, int s) {
+  if (S.st->status != EDMD_OK) return 0;
+  uint64_t lim = time_key(S.ev[2 * S.B.N + SP_SCREEN].t);
+  if (A.tstop_key < lim) lim = A.tstop_key;
+  if (A.freeze[s] < lim) lim = A.freeze[s];
+  return lim;
+}
+
+__global__ void k_limits(const SysDev* __restrict__ sys, RoundArgs A) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < A.nsys) A.lim[s] = system_limit(sys[s], A, s);
+}
+
+// ---------------------------------------------------------------- per round
+
+__global__ void k_round_begin(RoundArgs A) {
+  *A.nsafe = 0;
+  *A.active = 0;
+}
+
+__device__ __forceinline__ int wrapi(int v, int n) {
+  v %= n;
+  return v < 0 ? v + n : v;
+}
+
+// window minima of one tile in shared memory and selection of its events
+__global__ void __launch_bounds__(256) k_select(const SysDev* __restrict__ sys, RoundArgs A) {
+  extern __shared__ unsigned char smem[];
+  const int t = blockIdx.x;
+  const int s = A.tsys[t];
+  const uint64_t lim = A.lim[s];
+  if (lim == 0) return;
+  const Box& B = sys[s].B;
+  const int Nxc = B.Nxc, Nyc = B.Nyc;
+  const int x0 = A.tx0[t], y0 = A.ty0[t];
+  const int r = A.radius, H = r + 1;
+  const int CW = TX + 2 * H, CH = TY + 2 * H;    // cell minima, halo H
+  const int HW = TX + 2;                          // horizontal minima: cols -1..TX
+  uint64_t* ck = (uint64_t*)smem;
+  uint64_t* hk = ck + CW * CH;
+  uint64_t* wk = hk + HW * CH;
+  int32_t* ci = (int32_t*)(wk + HW * (TY + 2));
+  int32_t* hi = ci + CW * CH;
+  int32_t* wi = hi + HW * CH;
+  const int64_t base = A.coff[s];
+  for (int q = threadIdx.x; q < CW * CH; q += blockDim.x) {
+    const int lx = q % CW, ly = q / CW;
+    const int gx = wrapi(x0 + lx - H, Nxc), gy = wrapi(y0 + ly - H, Nyc);
+    const int64_t c = base + (int64_t)gy * Nxc + gx;
+    ck[q] = A.cmt[c];
+    ci[q] = A.cmi[c];
+  }
+  __syncthreads();
+  for (int q = threadIdx.x; q < HW * CH; q += blockDim.x) {
+    const int hx = q % HW, ly = q / HW;
+    const int lx = hx - 1 + H;
+    uint64_t bk = KINF;
+    int32_t bi = IINF;
+    for (int d = -r; d <= r; d++) {
+      const int o = ly * CW + lx + d;
+      if (pair_less(ck[o], ci[o], bk, bi)) { bk = ck[o]; bi = ci[o]; }
+    }
+    hk[q] = bk;
+    hi[q] = bi;
+  }
+  __syncthreads();
+  for (int q = threadIdx.x; q < HW * (TY + 2); q += blockDim.x) {
+    const int wx = q % HW, wy = q / HW;
+    const int ly = wy - 1 + H;
+    uint64_t bk = KINF;
+    int32_t bi = IINF;
+    for (int d = -r; d <= r; d++) {
+      const int o = (ly + d) * HW + wx;
+      if (pair_less(hk[o], hi[o], bk, bi)) { bk = hk[o]; bi = hi[o]; }
+    }
+    wk[q] = bk;
+    wi[q] = bi;
+  }
+  __syncthreads();
+  const int ix = threadIdx.x % TX, iy = threadIdx.x / TX;
+  const int cx = x0 + ix, cy = y0 + iy;
+  bool sel = false;
+  int32_t g = 0;
+  if (cx < Nxc && cy < Nyc) {
+    const int o = (iy + H) * CW + ix + H;
+    const uint64_t k = ck[o];
+    g = ci[o];
+    const int w = (iy + 1) * HW + ix + 1;
+    if (k < lim && wk[w] == k && wi[w] == g) {
+      const int c = cy * Nxc + cx;
+      if (A.fc[2 * (int64_t)g] == c) {
+        const int c2 = A.fc[2 * (int64_t)g + 1];
+        if (c2 == c) {
+          sel = true;
+        } else {
+          int dx = c2 % Nxc - cx, dy = c2 / Nxc - cy;
+          if (dx > 1) dx -= Nxc;
+          if (dx < -1) dx += Nxc;
+          if (dy > 1) dy -= Nyc;
+          if (dy < -1) dy += Nyc;
+          if (dx >= -1 && dx <= 1 && dy >= -1 && dy <= 1) {
+            const int w2 = (iy + 1 + dy) * HW + ix + 1 + dx;
+            sel = wk[w2] == k && wi[w2] == g;
+          }
+        }
+      }
+    }
+  }
+  const unsigned m = __ballot_sync(FULLM, sel);
+  if (m) {
+    const int lane = threadIdx.x & 31;
+    const int lead = __ffs(m) - 1;
+    int pos = 0;
+    if (lane == lead) pos = atomicAdd(A.nsafe, __popc(m));
+    pos = __shfl_sync(FULLM, pos, lead);
+    if (sel) A.safe[pos + __popc(m & ((1u << lane) - 1))] = g;
+    if (lane == lead) A.selflag[s] = 1;
+  }
+}
+
+// causality stamp of a write of local cell c
+__device__ bool stamp_write(const RoundArgs& A, int64_t base, int c, uint64_t clk) {
+  const int64_t gc = base + c;
+  const bool bad = A.lw[gc] > clk || A.lr[gc] > clk;
+  atomicMax((unsigned long long*)&A.lw[gc], (unsigned long long)clk);
+  return bad;
+}
+
+// collisionEventNormal (src/EDMD.c:2829-2905) for disks a0 and a1 (a1 may be
+// -1), each current at time t, by one warp: lanes 0..8 walk a0's 3x3 cells and
+// lanes 16..24 a1's (dy outer, dx inner), the candidates are packed over the
+// warp and each lane solves a share of the pairs; the result is the first
+// strict minimum below NEVER in the reference's scan order (lexicographic
+// (time, scan position)); with none the partner stays 0 and collActual is
+// disk 0's counter.
+struct Pred {
+  double dt;
+  int partner;
+  uint32_t ca;
+  int pcell;     // partner's cell, or the owner's when there is none
+};
+struct WarpScratch {
+  int32_t reg[32 * MAXC];
+  int32_t comp[2 * 9 * MAXC];
+  int16_t ord[2 * 9 * MAXC];
+};
+
+__device__ __forceinline__ void merge(double& bd, uint64_t& bk, int& bo, int& bp, uint32_t& bc,
+                                      double d, uint64_t kd, int o, int p, uint32_t c) {
+  if (kd < bk || (kd == bk && o < bo)) { bd = d; bk = kd; bo = o; bp = p; bc = c; }
+}
+
+__device__ void predict_warp(const SysDev& S, int a0, const Disk& A0, int X0, int Y0, int a1,
+                             const Disk& A1, int X1, int Y1, double t, Pred& r0, Pred& r1,
+                             WarpScratch* W, int lane, unsigned long long* npair, bool* ovl, int* ob) {
+  const Box& B = S.B;
+  const int grp = lane >> 4, q = lane & 15;
+  const int a = grp ? a1 : a0;
+  const int X = grp ? X1 : X0, Y = grp ? Y1 : Y0;
+  int cnt = 0;
+  int32_t* reg = W->reg + lane * MAXC;
+  if (a >= 0 && q < 9) {
+    int p = S.head[pbc_cy(B, Y + q / 3 - 1) * B.Nxc + pbc_cx(B, X + q % 3 - 1)];
+    int guard = 0;                   // a list is never longer than N
+    while (p != NIL && guard++ < B.N) {
+      if (p != a) {
+        if (cnt < MAXC) reg[cnt] = p;
+        cnt++;
+      }
+      p = S.d[p].nxt;
+    }
+  }
+  const bool spill = __any_sync(FULLM, cnt > MAXC);
+  const uint64_t knever = time_key(NEVER);
+  double bd0 = NEVER, bd1 = NEVER;
+  uint64_t bk0 = knever, bk1 = knever;
+  int bo0 = -1, bo1 = -1, bp0 = 0, bp1 = 0;
+  uint32_t bc0 = 0, bc1 = 0;
+  bool lovl = false;
+  int lb = -1;
+  unsigned long long tot;
+  if (!spill) {
+    int incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 16; o <<= 1) {
+      const int v = __shfl_up_sync(FULLM, incl, o, 16);
+      if (q >= o) incl += v;
+    }
+    const int excl = incl - cnt;
+    const int tot0 = __shfl_sync(FULLM, incl, 15), tot1 = __shfl_sync(FULLM, incl, 31);
+    const int bse = grp ? tot0 : 0;
+    for (int k = 0; k < cnt; k++) {
+      W->comp[bse + excl + k] = reg[k];
+      W->ord[bse + excl + k] = (int16_t)(q * MAXC + k);
+    }
+    __syncwarp();
+    tot = (unsigned long long)(tot0 + tot1);
+    for (int f = lane; f < tot0 + tot1; f += 32) {
+      const int p = W->comp[f];
+      const int o = W->ord[f];
+      const Disk P = S.d[p];
+      const bool g1 = f >= tot0;
+      bool ov = false;
+      const double d = coll_time_normal_i(B, g1 ? A1 : A0, P, t, &ov);
+      if (ov) { lovl = true; lb = p; }
+      const uint64_t kd = time_key(d);
+      if (g1) merge(bd1, bk1, bo1, bp1, bc1, d, kd, o, p, P.coll);
+      else merge(bd0, bk0, bo0, bp0, bc0, d, kd, o, p, P.coll);
+    }
+    __syncwarp();
+  } else {
+    // a list longer than MAXC: every lane walks and solves its own list
+    unsigned long long mine = 0;
+    if (a >= 0 && q < 9) {
+      const Disk& AA = grp ? A1 : A0;
+      int p = S.head[pbc_cy(B, Y + q / 3 - 1) * B.Nxc + pbc_cx(B, X + q % 3 - 1)];
+      int k = 0, guard = 0;
+      while (p != NIL && guard++ < B.N) {
+        const Disk P = S.d[p];
+        if (p != a) {
+          bool ov = false;
+          const double d = coll_time_normal_i(B, AA, P, t, &ov);
+          if (ov) { lovl = true; lb = p; }
+          const uint64_t kd = time_key(d);
+          if (grp) merge(bd1, bk1, bo1, bp1, bc1, d, kd, q * (1 << 20) + k, p, P.coll);
+          else merge(bd0, bk0, bo0, bp0, bc0, d, kd, q * (1 << 20) + k, p, P.coll);
+          k++;
+          mine++;
+        }
+        p = P.nxt;
+      }
+    }
+    for (int o = 16; o > 0; o >>= 1) mine += __shfl_xor_sync(FULLM, mine, o);
+    tot = mine;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    double d = __shfl_xor_sync(FULLM, bd0, o);
+    uint64_t kd = __shfl_xor_sync(FULLM, bk0, o);
+    int oo = __shfl_xor_sync(FULLM, bo0, o), pp = __shfl_xor_sync(FULLM, bp0, o);
+    uint32_t cc = __shfl_xor_sync(FULLM, bc0, o);
+    merge(bd0, bk0, bo0, bp0, bc0, d, kd, oo, pp, cc);
+    d = __shfl_xor_sync(FULLM, bd1, o);
+    kd = __shfl_xor_sync(FULLM, bk1, o);
+    oo = __shfl_xor_sync(FULLM, bo1, o);
+    pp = __shfl_xor_sync(FULLM, bp1, o);
+    cc = __shfl_xor_sync(FULLM, bc1, o);
+    merge(bd1, bk1, bo1, bp1, bc1, d, kd, oo, pp, cc);
+  }
+  const int div = spill ? (1 << 20) : MAXC;
+  r0.dt = bd0; r0.partner = bp0; r0.ca = bo0 < 0 ? S.d[0].coll : bc0;
+  {
+    const int qq = bo0 < 0 ? 4 : bo0 / div;
+    r0.pcell = pbc_cy(B, Y0 + qq / 3 - 1) * B.Nxc + pbc_cx(B, X0 + qq % 3 - 1);
+  }
+  if (a1 >= 0) {
+    r1.dt = bd1; r1.partner = bp1; r1.ca = bo1 < 0 ? S.d[0].coll : bc1;
+    const int qq = bo1 < 0 ? 4 : bo1 / div;
+    r1.pcell = pbc_cy(B, Y1 + qq / 3 - 1) * B.Nxc + pbc_cx(B, X1 + qq % 3 - 1);
+  }
+  *npair += tot;
+  const unsigned m = __ballot_sync(FULLM, lovl);
+  if (m) {
+    *ovl = true;
+    *ob = __shfl_sync(FULLM, lb, __ffs(m) - 1);
+  }
+}
+
+__device__ __forceinline__ void set_event(const SysDev& S, int slot, double t, int j, uint32_t ca,
+                                          uint32_t pcell, uint64_t clock) {
+  Ev e;
+  e.t = t; e.tie = kmax(time_key(t), clock); e.b = pcell; e.j = j; e.ca = ca; e.st = ST_QUEUED;
+  S.ev[slot] = e;
+}
+
+// new attribution of disk i (global index g); its cells join the dirty list
+__device__ __forceinline__ void reattribute(const SysDev& S, const RoundArgs& A, int i, int64_t g,
+                                            int64_t base, int32_t* dc, int* nd) {
+  uint64_t key;
+  int c1, c2;
+  attribution(S, i, &key, &c1, &c2);
+  A.dkey[g] = key;
+  A.fc[2 * g] = c1;
+  A.fc[2 * g + 1] = c2;
+  dc[(*nd)++] = (int32_t)(base + c1);
+  if (c2 != c1) dc[(*nd)++] = (int32_t)(base + c2);
+}
+
+// read stamps of the 3x3 cells around c by lanes l0..l0+8 (warp-wide result)
+__device__ __forceinline__ bool stamp_read_warp(const Box& B, const RoundArgs& A, int64_t base, int c,
+                                                uint64_t clk, int lane, int l0) {
+  bool bad = false;
+  const int q = lane - l0;
+  if (q >= 0 && q < 9) {
+    const int x = c % B.Nxc, y = c / B.Nxc;
+    const int64_t gc = base + pbc_cy(B, y + q / 3 - 1) * B.Nxc + pbc_cx(B, x + q % 3 - 1);
+    if (A.lw[gc] > clk) bad = true;
+    if (A.lr[gc] < clk) atomicMax((unsigned long long*)&A.lr[gc], (unsigned long long)clk);
+  }
+  return __any_sync(FULLM, bad);
+}
+
+__device__ __forceinline__ void cnt_add(const RoundArgs& A, int s, int stripe, int k, unsigned long long v) {
+  if (v) atomicAdd((unsigned long long*)&A.cnt[((int64_t)s * NSTRIPE + stripe) * NCNT + k], v);
+}
+__device__ __forceinline__ void cnt_addf(const RoundArgs& A, int s, int stripe, int k, double v) {
+  atomicAdd((double*)&A.cnt[((int64_t)s * NSTRIPE + stripe) * NCNT + k], v);
+}
+
+// process the selected events, one warp each: doTheCollisionNormal
+// (src/EDMD.c:3542, elastic rule 3802-3827), its stale branch (3553-3556) or
+// doTheCrossing (2501).  The scalar work is repeated by every lane (same
+// values), stores are made by lane 0, predictions are shared by the warp.
+// Per-system counters go to one of NSTRIPE stripes to spread the atomics.
+__global__ void __launch_bounds__(32 * WPB) k_process(const SysDev* __restrict__ sys, RoundArgs A) {
+  __shared__ WarpScratch scr[WPB];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  WarpScratch* W = &scr[wid];
+  const int nsafe = *A.nsafe;
+  const int gw = blockIdx.x * WPB + wid, nw = gridDim.x * WPB;
+  const int stripe = gw & (NSTRIPE - 1);
+  for (int n = gw; n < nsafe; n += nw) {
+    const int64_t g = A.safe[n];
+    const int s = A.dsys[g];
+    const SysDev& S = sys[s];
+    const Box& B = S.B;
+    const int N = B.N;
+    const int64_t base = A.coff[s], dbase = A.doff[s];
+    const int a = (int)(g - dbase);
+    uint64_t key;
+    const int slot = next_slot(S, a, &key);
+    const Ev E = S.ev[slot];
+    const double t = E.t;
+    const uint64_t clk = E.tie;        // serial pop clock of this event
+    int32_t dc[MAXDIRTY];
+    int nd = 0;
+    dc[nd++] = (int32_t)(base + A.fc[2 * g]);
+    if (A.fc[2 * g + 1] != A.fc[2 * g]) dc[nd++] = (int32_t)(base + A.fc[2 * g + 1]);
+    Disk Da = S.d[a];
+    free_fly_i(B, Da, t);
+    const int ax = S.cx[a], ay = S.cy[a];
+    const int ca = cell_of(B, ax, ay);
+    unsigned long long npair = 0, npred = 0, ncol = 0, ncross = 0, nstale = 0;
+    double ct[4] = {0, 0, 0, 0};
+    bool ovl = false, bad = false;
+    int ob = -1;
+    if (slot >= N) {
+      const int b = E.j;
+      Disk Db = S.d[b];
+      if (E.ca != Db.coll) {
+        __syncwarp();
+        if (lane == 0) S.d[a] = Da;
+        bad |= lane == 0 && stamp_write(A, base, ca, clk);
+        bad |= stamp_read_warp(B, A, base, ca, clk, lane, 0);
+        __syncwarp();
+        Pred p0, p1;
+        predict_warp(S, a, Da, ax, ay, -1, Da, ax, ay, t, p0, p1, W, lane, &npair, &ovl, &ob);
+        npred = 1;
+        nstale = 1;
+        if (lane == 0) {
+          set_event(S, N + a, t + p0.dt, p0.partner, p0.ca, p0.pcell, clk);
+          reattribute(S, A, a, g, base, dc, &nd);
+        }
+      } else {
+        const int64_t gb = dbase + b;
+        dc[nd++] = (int32_t)(base + A.fc[2 * gb]);
+        if (A.fc[2 * gb + 1] != A.fc[2 * gb]) dc[nd++] = (int32_t)(base + A.fc[2 * gb + 1]);
+        const int bx = S.cx[b], by = S.cy[b];
+        const int cb = cell_of(B, bx, by);
+        free_fly_i(B, Db, t);
+        Da.coll++;
+        Db.coll++;
+        double dx = Db.x - Da.x, dy = Db.y - Da.y;
+        const double dvx = Db.vx - Da.vx, dvy = Db.vy - Da.vy;
+        const double msum = Da.m + Db.m;
+        const double invMass = msum == 2.0 ? 0.5 : 1 / msum;
+        pbc_i(B, dx, dy);
+        const double collKernel = invMass * (1 + S.res) * (dx * dvx + dy * dvy);
+        const double distSquared = 4 * Da.rad * Db.rad;
+        const double f = distSquared == 4.0 ? collKernel * 0.25 : collKernel / distSquared;
+        const double cf = Da.m * Db.m * f;
+        ct[0] = cf * dx * dx;
+        ct[1] = cf * dy * dy;
+        ct[2] = cf * dx * dy;
+        ct[3] = cf * dy * dx;
+        Da.vx += f * Db.m * dx;
+        Da.vy += f * Db.m * dy;
+        Db.vx -= f * Da.m * dx;
+        Db.vy -= f * Da.m * dy;
+        __syncwarp();
+        if (lane == 0) {
+          S.d[a] = Da;
+          S.d[b] = Db;
+          if ((A.flags & EDMD_F_TRACE) && S.trace) {
+            const unsigned long long k = atomicAdd((unsigned long long*)&S.st->ntrace, 1ull);
+            if ((int64_t)k < S.trace_cap) {
+              edmd_collision* tr = (edmd_collision*)S.trace + k;
+              tr->i = a; tr->j = b; tr->cell_i = ca; tr->cell_j = cb; tr->t = t;
+            }
+          }
+        }
+        bad |= lane == 0 && (stamp_write(A, base, ca, clk) | stamp_write(A, base, cb, clk));
+        bad |= stamp_read_warp(B, A, base, ca, clk, lane, 0);
+        bad |= stamp_read_warp(B, A, base, cb, clk, lane, 16);
+        __syncwarp();
+        Pred p0, p1;
+        predict_warp(S, a, Da, ax, ay, b, Db, bx, by, t, p0, p1, W, lane, &npair, &ovl, &ob);
+        npred = 2;
+        ncol = 1;
+        if (lane == 0) {
+          int dir;
+          double tc = crossing_time_i(B, Da, ax, ay, t, &dir);
+          set_event(S, a, tc, dir, 0, 0, clk);
+          tc = crossing_time_i(B, Db, bx, by, t, &dir);
+          set_event(S, b, tc, dir, 0, 0, clk);
+          set_event(S, N + a, t + p0.dt, p0.partner, p0.ca, p0.pcell, clk);
+          set_event(S, N + b, t + p1.dt, p1.partner, p1.ca, p1.pcell, clk);
+          reattribute(S, A, a, g, base, dc, &nd);
+          reattribute(S, A, b, gb, base, dc, &nd);
+        }
+      }
+    } else {
+      int cx = ax, cy = ay;
+      int wrapx = 0, wrapy = 0;
+      switch (E.j) {
+        case 1: if (cx - 1 == -1) { cx = B.Nxc - 1; wrapx = -1; } else cx -= 1; break;
+        case 2: if (cx + 1 == B.Nxc) { cx = 0; wrapx = 1; } else cx += 1; break;
+        case 3: if (cy - 1 == -1) { cy = B.Nyc - 1; wrapy = -1; } else cy -= 1; break;
+        default: if (cy + 1 == B.Nyc) { cy = 0; wrapy = 1; } else cy += 1; break;
+      }
+      const int c = cell_of(B, cx, cy);
+      __syncwarp();
+      if (lane == 0) {
+        // unlink from the old cell, relink at the head of the new one
+        const int pv = S.prv[a], nx = Da.nxt;
+        if (pv == NIL) S.head[ca] = nx;
+        else S.d[pv].nxt = nx;
+        if (nx != NIL) S.prv[nx] = pv;
+        if (wrapx) S.crossX[a] += wrapx;
+        if (wrapy) S.crossY[a] += wrapy;
+        const int h = S.head[c];
+        S.cx[a] = cx;
+        S.cy[a] = cy;
+        S.prv[a] = NIL;
+        Da.nxt = h;
+        S.d[a] = Da;
+        S.head[c] = a;
+        if (h != NIL) S.prv[h] = a;
+      }
+      bad |= lane == 0 && (stamp_write(A, base, ca, clk) | stamp_write(A, base, c, clk));
+      bad |= stamp_read_warp(B, A, base, c, clk, lane, 0);
+      __syncwarp();
+      Pred p0, p1;
+      predict_warp(S, a, Da, cx, cy, -1, Da, cx, cy, t, p0, p1, W, lane, &npair, &ovl, &ob);
+      npred = 1;
+      ncross = 1;
+      if (lane == 0) {
+        int dir;
+        const double tc = crossing_time_i(B, Da, cx, cy, t, &dir);
+        set_event(S, a, tc, dir, 0, 0, clk);
+        set_event(S, N + a, t + p0.dt, p0.partner, p0.ca, p0.pcell, clk);
+        reattribute(S, A, a, g, base, dc, &nd);
+      }
+    }
+    if (lane == 0) {
+      for (int k = 0; k < MAXDIRTY; k++) A.dcell[(int64_t)n * MAXDIRTY + k] = k < nd ? dc[k] : -1;
+      if (ncol) {
+        cnt_addf(A, s, stripe, C_CT0, ct[0]);
+        cnt_addf(A, s, stripe, C_CT1, ct[1]);
+        cnt_addf(A, s, stripe, C_CT2, ct[2]);
+        cnt_addf(A, s, stripe, C_CT3, ct[3]);
+      }
+      cnt_add(A, s, stripe, C_NCOL, ncol);
+      cnt_add(A, s, stripe, C_NCROSS, ncross);
+      cnt_add(A, s, stripe, C_NSTALE, nstale);
+      cnt_add(A, s, stripe, C_NPAIR, npair);
+      cnt_add(A, s, stripe, C_NPRED, npred);
+      cnt_add(A, s, stripe, C_NEV, 1ull);
+      atomicMax((unsigned long long*)&A.cnt[((int64_t)s * NSTRIPE + stripe) * NCNT + C_TLAST],
+                (unsigned long long)key);
+      if (bad) atomicAdd(A.violations, 1ull);
+      if (ovl) {
+        SysState* R = S.st;
+        R->err_a = a;
+        R->err_b = ob;
+        R->status = EDMD_ERR_OVERLAP;
+      }
+    }
+    __syncwarp();
+  }
+}
+
+// minimum (key, owner) of the events attributed to each dirty cell: one warp
+// per cell, lanes 0..8 walk the lists of the 3x3 block around it
+__global__ void __launch_bounds__(256) k_recompute(const SysDev* __restrict__ sys, RoundArgs A) {
+  const int lane = threadIdx.x & 31;
+  const int64_t total = (int64_t)(*A.nsafe) * MAXDIRTY;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < total; w += nwarps) {
+    const int32_t gc = A.dcell[w];
+    if (gc < 0) continue;
+    const int s = A.dsys[A.safe[w / MAXDIRTY]];
+    const SysDev& S = sys[s];
+    const Box& B = S.B;
+    const int64_t base = A.coff[s], dbase = A.doff[s];
+    const int c = (int)(gc - base);
+    uint64_t bk = KINF;
+    int32_t bi = IINF;
+    if (lane < 9) {
+      const int x = c % B.Nxc, y = c / B.Nxc;
+      int p = S.head[pbc_cy(B, y + lane / 3 - 1) * B.Nxc + pbc_cx(B, x + lane % 3 - 1)];
+      int guard = 0;
+      while (p != NIL && guard++ < B.N) {
+        const int64_t g = dbase + p;
+        const uint64_t k = A.dkey[g];
+        if (k != KINF && (A.fc[2 * g] == c || A.fc[2 * g + 1] == c) && pair_less(k, (int32_t)g, bk, bi)) {
+          bk = k;
+          bi = (int32_t)g;
+        }
+        p = S.d[p].nxt;
+      }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      const uint64_t k2 = __shfl_xor_sync(FULLM, bk, o);
+      const int32_t i2 = __shfl_xor_sync(FULLM, bi, o);
+      if (pair_less(k2, i2, bk, bi)) { bk = k2; bi = i2; }
+    }
+    if (lane == 0) {
+      A.cmt[gc] = bk;
+      A.cmi[gc] = bi;
+    }
+  }
+}
+
+// per system, after the round: a system that has met its collision budget
+// stops taking events later than the latest one it processed (the earlier
+// ones still pending are drained, so the call ends on a state of the serial
+// run); a system with nothing eligible left before its screenshot time
+// free-flies every disk to it (takeAScreenshot, src/EDMD.c:4657-4661) and
+// reschedules it; then the eligibility bound of the next round
+__global__ void k_barrier(const SysDev* __restrict__ sys, RoundArgs A) {
+  const int s = blockIdx.x;
+  const SysDev& S = sys[s];
+  const int N = S.B.N;
+  __shared__ int go;
+  if (threadIdx.x < 32) {
+    const int l = threadIdx.x;
+    const uint64_t* c = A.cnt + ((int64_t)s * NSTRIPE + l) * NCNT;
+    unsigned long long nc = c[C_NCOL];
+    uint64_t tl = c[C_TLAST];
+    for (int o = 16; o > 0; o >>= 1) {
+      nc += __shfl_xor_sync(FULLM, nc, o);
+      const uint64_t t2 = __shfl_xor_sync(FULLM, tl, o);
+      tl = t2 > tl ? t2 : tl;
+    }
+    if (l == 0) {
+      const SysState* R = S.st;
+      const bool ok = R->status == EDMD_OK;
+      uint64_t fz = A.freeze[s];
+      if (ok && fz == KINF && R->ncol + nc >= A.target[s]) {
+        fz = kmax(tl, A.tlast[s]) + 1;
+        A.freeze[s] = fz;
+      }
+      const uint64_t lim = A.tstop_key < fz ? A.tstop_key : fz;
+      const int selected = A.selflag[s];
+      go = (ok && !selected && time_key(S.ev[2 * N + SP_SCREEN].t) < lim) ? 1 : 0;
+      if (ok && (selected || go)) atomicAdd(A.active, 1);
+      A.selflag[s] = 0;
+    }
+  }
+  __syncthreads();
+  if (go) {
+    const double tbar = S.ev[2 * N + SP_SCREEN].t;
+    for (int i = threadIdx.x; i < N; i += blockDim.x) {
+      Disk p = S.d[i];
+      free_fly_i(S.B, p, tbar);
+      S.d[i] = p;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      S.ev[2 * N + SP_SCREEN].t = tbar + S.dtime;
+      A.tlast[s] = kmax(A.tlast[s], time_key(tbar));
+    }
+  }
+  if (threadIdx.x == 0) A.lim[s] = system_limit(S, A, s);
+}
+
+// fold the call's counters into each system's state; its time is the last
+// processed event or screenshot
+__global__ void k_round_finish(const SysDev* __restrict__ sys, RoundArgs A) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= A.nsys) return;
+  SysState* R = sys[s].st;
+  unsigned long long v[NCNT];
+  double ct[4] = {0, 0, 0, 0};
+  for (int k = 0; k < NCNT; k++) v[k] = 0;
+  uint64_t tl = A.tlast[s];
+  for (int l = 0; l < NSTRIPE; l++) {
+    const uint64_t* c = A.cnt + ((int64_t)s * NSTRIPE + l) * NCNT;
+    for (int k = 0; k < 4; k++) ct[k] += __longlong_as_double((long long)c[k]);
+    for (int k = C_NCOL; k <= C_NEV; k++) v[k] += c[k];
+    tl = kmax(tl, c[C_TLAST]);
+  }
+  for (int k = 0; k < 4; k++) R->collT[k] += ct[k];
+  R->ncol += v[C_NCOL];
+  R->ncol_total += v[C_NCOL];
+  R->ncross += v[C_NCROSS];
+  R->nstale += v[C_NSTALE];
+  R->npair += v[C_NPAIR];
+  R->npred += v[C_NPRED];
+  R->nevents += v[C_NEV];
+  if (tl != 0) {
+    const double t = key_time(tl);
+    if (t > R->t) R->t = t;
+  }
+  R->stop_reason = A.freeze[s] != KINF ? EDMD_STOP_COLL : EDMD_STOP_TIME;
+}
+
+__global__ void k_round_setup(const int64_t* __restrict__ doff, const SysDev* __restrict__ sys,
+                              int32_t* dsys) {
+  const int s = blockIdx.y;
+  const int N = sys[s].B.N;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x)
+    dsys[doff[s] + i] = s;
+}
+
+struct RoundBufs {
+  int32_t *dsys = nullptr, *fc = nullptr, *cmi = nullptr, *safe = nullptr, *nsafe = nullptr;
+  int32_t *dcell = nullptr, *selflag = nullptr, *active = nullptr;
+  int32_t *tsys = nullptr, *tx0 = nullptr, *ty0 = nullptr;
+  int64_t *doff = nullptr, *coff = nullptr;
+  uint64_t *dkey = nullptr, *cmt = nullptr, *lw = nullptr, *lr = nullptr;
+  uint64_t *lim = nullptr, *target = nullptr, *freeze = nullptr, *tlast = nullptr, *cnt = nullptr;
+  unsigned long long* viol = nullptr;
+  int64_t ntiles = 0;
+};
+
+int round_init(edmd_ctx* ctx) {
+  if (ctx->round) return EDMD_OK;
+  for (const SysDev& S : ctx->hs)
+    if (S.B.Nxc < 3 || S.B.Nyc < 3) return set_err(ctx, EDMD_ERR_ARG, "the round engine needs at least 3x3 cells");
+  RoundBufs* R = new RoundBufs();
+  ctx->round = R;
+  const int64_t TN = ctx->total_N, TC = ctx->total_C;
+  std::vector<int32_t> tsys, tx0, ty0;
+  for (int s = 0; s < ctx->nsys; s++) {
+    const Box& B = ctx->hs[s].B;
+    for (int y = 0; y < B.Nyc; y += TY)
+      for (int x = 0; x < B.Nxc; x += TX) {
+        tsys.push_back(s);
+        tx0.push_back(x);
+        ty0.push_back(y);
+      }
+  }
+  R->ntiles = (int64_t)tsys.size();
+  CK(dalloc(&R->dsys, TN)); CK(dalloc(&R->fc, 2 * TN)); CK(dalloc(&R->dkey, TN));
+  CK(dalloc(&R->cmi, TC)); CK(dalloc(&R->cmt, TC)); CK(dalloc(&R->lw, TC)); CK(dalloc(&R->lr, TC));
+  CK(dalloc(&R->safe, TN)); CK(dalloc(&R->nsafe, 1)); CK(dalloc(&R->dcell, TN * MAXDIRTY));
+  CK(dalloc(&R->selflag, ctx->nsys)); CK(dalloc(&R->active, 1));
+  CK(dalloc(&R->doff, ctx->nsys)); CK(dalloc(&R->coff, ctx->nsys));
+  CK(dalloc(&R->lim, ctx->nsys)); CK(dalloc(&R->target, ctx->nsys)); CK(dalloc(&R->freeze, ctx->nsys));
+  CK(dalloc(&R->tlast, ctx->nsys)); CK(dalloc(&R->viol, 1));
+  CK(dalloc(&R->cnt, (int64_t)ctx->nsys * NSTRIPE * NCNT));
+  CK(dalloc(&R->tsys, R->ntiles)); CK(dalloc(&R->tx0, R->ntiles)); CK(dalloc(&R->ty0, R->ntiles));
+  CK(cudaMemcpy(R->doff, ctx->disk_off.data(), ctx->nsys * 8, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(R->coff, ctx->cell_off.data(), ctx->nsys * 8, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(R->tsys, tsys.data(), R->ntiles * 4, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(R->tx0, tx0.data(), R->ntiles * 4, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(R->ty0, ty0.data(), R->ntiles * 4, cudaMemcpyHostToDevice));
+  CK(cudaMemset(R->selflag, 0, ctx->nsys * 4));
+  k_round_setup<<<dim3(64, ctx->nsys), 256, 0, ctx->stream>>>(R->doff, ctx->ds, R->dsys);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(ctx->stream));
+  return EDMD_OK;
+}
+
+size_t select_smem(int r) {
+  const int H = r + 1, CW = TX + 2 * H, CH = TY + 2 * H, HW = TX + 2;
+  return (size_t)(CW * CH + HW * CH + HW * (TY + 2)) * 12;
+}
+
+// one round: selection, processing, minima, barriers
+cudaError_t enqueue_round(edmd_ctx* ctx, const RoundBufs* R, const RoundArgs& A, int nsm) {
+  cudaStream_t st = ctx->stream;
+  k_round_begin<<<1, 1, 0, st>>>(A);
+  k_select<<<(unsigned)R->ntiles, TX * TY, select_smem(A.radius), st>>>(ctx->ds, A);
+  k_process<<<nsm * 16, 32 * WPB, 0, st>>>(ctx->ds, A);
+  k_recompute<<<nsm * 8, 256, 0, st>>>(ctx->ds, A);
+  k_barrier<<<ctx->nsys, 256, 0, st>>>(ctx->ds, A);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+void round_free(edmd_ctx* ctx) {
+  RoundBufs* R = (RoundBufs*)ctx->round;
+  if (!R) return;
+  void* p[] = {R->dsys, R->fc, R->cmi, R->safe, R->nsafe, R->dcell, R->selflag, R->active,
+               R->tsys, R->tx0, R->ty0, R->doff, R->coff, R->dkey, R->cmt, R->lw, R->lr,
+               R->lim, R->target, R->freeze, R->tlast, R->cnt, R->viol};
+  for (void* q : p)
+    if (q) cudaFree(q);
+  delete R;
+  ctx->round = nullptr;
+}
+
+// rounds until every system has stopped
+static int run_rounds(edmd_ctx* ctx, const std::vector<uint64_t>& tgt, double t_stop, uint32_t flags,
+                      int32_t radius, int64_t max_rounds, int64_t* rounds_out, int32_t* active_out,
+                      unsigned long long* viol_out) {
+  const RoundBufs* R = (const RoundBufs*)ctx->round;
+  cudaStream_t st = ctx->stream;
+  const int64_t TN = ctx->total_N, TC = ctx->total_C;
+  CK(cudaMemcpyAsync(R->target, tgt.data(), ctx->nsys * 8, cudaMemcpyHostToDevice, st));
+  CK(cudaMemsetAsync(R->freeze, 0xff, ctx->nsys * 8, st));
+  CK(cudaMemsetAsync(R->tlast, 0, ctx->nsys * 8, st));
+  CK(cudaMemsetAsync(R->cnt, 0, (size_t)ctx->nsys * NSTRIPE * NCNT * 8, st));
+  CK(cudaMemsetAsync(R->viol, 0, 8, st));
+  CK(cudaMemsetAsync(R->lw, 0, TC * 8, st));
+  CK(cudaMemsetAsync(R->lr, 0, TC * 8, st));
+  CK(cudaMemsetAsync(R->cmt, 0xff, TC * 8, st));
+  CK(cudaMemsetAsync(R->cmi, 0x7f, TC * 4, st));
+  RoundArgs A;
+  A.nsys = ctx->nsys; A.radius = radius; A.TN = TN; A.flags = flags;
+  {
+    // the order-preserving integer image of t_stop (time_key on the host)
+    uint64_t u;
+    memcpy(&u, &t_stop, 8);
+    if (u == 0x8000000000000000ull) u = 0;
+    A.tstop_key = (u >> 63) ? ~u : (u | 0x8000000000000000ull);
+  }
+  A.dsys = R->dsys; A.doff = R->doff; A.coff = R->coff;
+  A.dkey = R->dkey; A.fc = R->fc; A.cmt = R->cmt; A.cmi = R->cmi; A.lw = R->lw; A.lr = R->lr;
+  A.safe = R->safe; A.nsafe = R->nsafe; A.dcell = R->dcell; A.selflag = R->selflag;
+  A.active = R->active; A.lim = R->lim; A.target = R->target; A.freeze = R->freeze;
+  A.tlast = R->tlast; A.cnt = R->cnt; A.tsys = R->tsys; A.tx0 = R->tx0; A.ty0 = R->ty0; A.violations = R->viol;
+  const unsigned gd = (unsigned)((TN + 255) / 256);
+  k_prep<<<gd, 256, 0, st>>>(ctx->ds, A);
+  k_prep_owner<<<gd, 256, 0, st>>>(A);
+  k_limits<<<(ctx->nsys + 127) / 128, 128, 0, st>>>(ctx->ds, A);
+  CK(cudaGetLastError());
+  int dev = 0, nsm = 0;
+  CK(cudaGetDevice(&dev));
+  CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  // a block of rounds is captured once into a graph and replayed until every
+  // system has stopped; the host polls the active count between blocks
+  const int per_graph = 16;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+  cudaError_t ce = cudaSuccess;
+  for (int k = 0; k < per_graph && ce == cudaSuccess; k++) ce = enqueue_round(ctx, R, A, nsm);
+  cudaError_t ee = cudaStreamEndCapture(st, &graph);
+  if (ce != cudaSuccess || ee != cudaSuccess) {
+    if (graph) cudaGraphDestroy(graph);
+    return set_err(ctx, EDMD_ERR_CUDA, std::string("round capture: ") +
+                                           cudaGetErrorString(ce != cudaSuccess ? ce : ee));
+  }
+  ce = cudaGraphInstantiate(&exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (ce != cudaSuccess) return set_err(ctx, EDMD_ERR_CUDA, std::string("round graph: ") + cudaGetErrorString(ce));
+  int32_t* active_h = nullptr;
+  ce = cudaMallocHost((void**)&active_h, sizeof(int32_t));
+  if (ce != cudaSuccess) {
+    cudaGraphExecDestroy(exec);
+    CK(ce);
+  }
+  int64_t rounds = 0;
+  int32_t active = 1;
+  while (active && rounds < max_rounds) {
+    ce = cudaGraphLaunch(exec, st);
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(active_h, R->active, 4, cudaMemcpyDeviceToHost, st);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
+    if (ce != cudaSuccess) break;
+    rounds += per_graph;
+    active = *active_h;
+  }
+  cudaGraphExecDestroy(exec);
+  cudaFreeHost(active_h);
+  CK(ce);
+  k_round_finish<<<(ctx->nsys + 127) / 128, 128, 0, st>>>(ctx->ds, A);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(viol_out, R->viol, 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  *rounds_out += rounds;
+  *active_out = active;
+  return EDMD_OK;
+}
+
+extern "C" int edmd_advance_rounds(edmd_ctx* ctx, int64_t max_coll, double t_stop, uint32_t flags,
+                                   int32_t radius, int64_t max_rounds, float* elapsed_ms,
+                                   int64_t* rounds_out, int64_t* violations_out) {
+  if (!ctx) return EDMD_ERR_ARG;
+  if (max_coll < 0 || radius < 3 || radius > RTILE || max_rounds < 1)
+    return set_err(ctx, EDMD_ERR_ARG, "bad round-engine limits (radius 3..12)");
+  int rc = round_init(ctx);
+  if (rc) return rc;
+  std::vector<SysState> st(ctx->nsys);
+  CK(cudaMemcpy(st.data(), ctx->st, ctx->nsys * sizeof(SysState), cudaMemcpyDeviceToHost));
+  std::vector<uint64_t> tgt(ctx->nsys);
+  for (int s = 0; s < ctx->nsys; s++) {
+    if (st[s].grow) return set_err(ctx, EDMD_ERR_ARG, "the round engine runs the constant-radius phase only");
+    if (st[s].status != EDMD_OK) return set_err(ctx, st[s].status, "system is in an error state");
+    tgt[s] = st[s].ncol + (uint64_t)max_coll;
+  }
+  const bool exact = (flags & EDMD_F_EXACT) != 0;
+  if (exact) {
+    rc = ckpt_save(ctx, CKPT_ROUND);
+    if (rc) return rc;
+  }
+  ctx->round_dirty = true;
+  CK(cudaEventRecord(ctx->e0, ctx->stream));
+  int64_t rounds = 0, viol_total = 0;
+  int32_t active = 0;
+  int32_t r = radius;
+  for (;;) {
+    unsigned long long v = 0;
+    rc = run_rounds(ctx, tgt, t_stop, flags, r, max_rounds, &rounds, &active, &v);
+    if (rc) return rc;
+    viol_total += (int64_t)v;
+    if (!exact || v == 0 || active) break;
+    // a violation: replay the whole call from its start with a wider window
+    if (r >= RTILE) return set_err(ctx, EDMD_ERR_BUDGET, "round engine: violation at the widest window");
+    rc = ckpt_restore(ctx, CKPT_ROUND);
+    if (rc) return rc;
+    ctx->round_dirty = true;
+    r = r * 2 < RTILE ? r * 2 : RTILE;
+  }
+  CK(cudaEventRecord(ctx->e1, ctx->stream));
+  CK(cudaEventSynchronize(ctx->e1));
+  if (elapsed_ms) CK(cudaEventElapsedTime(elapsed_ms, ctx->e0, ctx->e1));
+  if (rounds_out) *rounds_out = rounds;
+  if (violations_out) *violations_out = viol_total;
+  std::vector<int32_t> status(ctx->nsys);
+  CK(cudaMemcpy2D(status.data(), 4, &ctx->st[0].status, sizeof(SysState), 4, ctx->nsys,
+                  cudaMemcpyDeviceToHost));
+  for (int s = 0; s < ctx->nsys; s++)
+    if (status[s] != EDMD_OK) {
+      char b[128];
+      snprintf(b, sizeof b, "system %d stopped with status %d", s, status[s]);
+      return set_err(ctx, status[s], b);
+    }
+  if (active) return set_err(ctx, EDMD_ERR_BUDGET, "round budget exhausted");
+  return EDMD_OK;
+}

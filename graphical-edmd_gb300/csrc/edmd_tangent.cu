@@ -263,13 +263,14 @@ static void state_parts(edmd_ctx* ctx, std::vector<std::pair<void*, size_t>>& pa
   if (ctx->mask) parts.push_back({ctx->mask, TN * 2});
 }
 
-extern "C" int edmd_checkpoint_save(edmd_ctx* ctx, int32_t slot) {
-  if (!ctx || slot < 0 || slot > 4096) return EDMD_ERR_ARG;
+int ckpt_save(edmd_ctx* ctx, int32_t slot) {
   std::vector<std::pair<void*, size_t>> parts;
   state_parts(ctx, parts);
   size_t total = 0;
   for (auto& p : parts) total += align_up(p.second, 256);
   if ((int)ctx->ckpt.size() <= slot) ctx->ckpt.resize(slot + 1, nullptr);
+  if ((int)ctx->ckpt_dirty.size() <= slot) ctx->ckpt_dirty.resize(slot + 1, 0);
+  ctx->ckpt_dirty[slot] = ctx->round_dirty ? 1 : 0;
   if (!ctx->ckpt[slot]) CK(cudaMalloc(&ctx->ckpt[slot], total));
   char* dst = (char*)ctx->ckpt[slot];
   for (auto& p : parts) {
@@ -280,8 +281,8 @@ extern "C" int edmd_checkpoint_save(edmd_ctx* ctx, int32_t slot) {
   return EDMD_OK;
 }
 
-extern "C" int edmd_checkpoint_restore(edmd_ctx* ctx, int32_t slot) {
-  if (!ctx || slot < 0 || slot >= (int)ctx->ckpt.size() || !ctx->ckpt[slot]) return EDMD_ERR_ARG;
+int ckpt_restore(edmd_ctx* ctx, int32_t slot) {
+  if (slot >= (int)ctx->ckpt.size() || !ctx->ckpt[slot]) return EDMD_ERR_ARG;
   std::vector<std::pair<void*, size_t>> parts;
   state_parts(ctx, parts);
   const char* src = (const char*)ctx->ckpt[slot];
@@ -290,7 +291,18 @@ extern "C" int edmd_checkpoint_restore(edmd_ctx* ctx, int32_t slot) {
     src += align_up(p.second, 256);
   }
   CK(cudaStreamSynchronize(ctx->stream));
+  ctx->round_dirty = ctx->ckpt_dirty[slot] != 0;
   return EDMD_OK;
+}
+
+extern "C" int edmd_checkpoint_save(edmd_ctx* ctx, int32_t slot) {
+  if (!ctx || slot < 0 || slot > CKPT_PUBLIC_MAX) return EDMD_ERR_ARG;
+  return ckpt_save(ctx, slot);
+}
+
+extern "C" int edmd_checkpoint_restore(edmd_ctx* ctx, int32_t slot) {
+  if (!ctx || slot < 0 || slot > CKPT_PUBLIC_MAX) return EDMD_ERR_ARG;
+  return ckpt_restore(ctx, slot);
 }
 
 // ==================================================================== tangent driver

@@ -21,7 +21,7 @@ LIB_PATH = os.path.join(HERE, "libedmd_gpu.so")
 
 OK, ERR_ARG, ERR_CUDA, ERR_OVERLAP, ERR_BUDGET, ERR_CAPACITY, ERR_NODEV = range(7)
 STOP_COLL, STOP_TIME, STOP_TMAX, STOP_SCREEN, STOP_GROW = 1, 2, 3, 4, 5
-F_STOP_AT_SCREEN, F_STOP_AT_GROW, F_TRACE, F_COUNT_NORMAL, F_LOG = 1, 2, 4, 8, 16
+F_STOP_AT_SCREEN, F_STOP_AT_GROW, F_TRACE, F_COUNT_NORMAL, F_LOG, F_EXACT = 1, 2, 4, 8, 16, 32
 ENGINE_AUTO, ENGINE_WARP, ENGINE_LANE = 0, 1, 2
 
 
@@ -53,7 +53,8 @@ class Counters(C.Structure):
 
 # every symbol the public headers declare, in declaration order
 EXPORTS = [
-    "edmd_create", "edmd_load_state", "edmd_advance", "edmd_sync", "edmd_get_state",
+    "edmd_create", "edmd_load_state", "edmd_advance", "edmd_advance_rounds", "edmd_sync",
+    "edmd_get_state",
     "edmd_get_states", "edmd_get_counters", "edmd_get_all_counters", "edmd_get_virial",
     "edmd_get_thermo", "edmd_get_trace", "edmd_set_engine", "edmd_set_lane_threads",
     "edmd_get_engine", "edmd_set_device", "edmd_host_alloc", "edmd_host_free", "edmd_run_noalloc",
@@ -83,6 +84,9 @@ def load(path=LIB_PATH):
     L.edmd_advance.argtypes = [C.c_void_p, C.c_int64, C.c_double, C.c_uint32, C.c_int64,
                                C.POINTER(C.c_float)]
     L.edmd_load_state.argtypes = [C.c_void_p] + [C.c_void_p] * 6
+    L.edmd_advance_rounds.argtypes = [C.c_void_p, C.c_int64, C.c_double, C.c_uint32, C.c_int32,
+                                      C.c_int64, C.POINTER(C.c_float), C.POINTER(C.c_int64),
+                                      C.POINTER(C.c_int64)]
     L.edmd_get_states.argtypes = [C.c_void_p] + [C.c_void_p] * 6
     L.edmd_get_all_counters.argtypes = [C.c_void_p, C.c_void_p]
     L.edmd_host_alloc.argtypes = [C.POINTER(C.c_void_p), C.c_int64]
@@ -228,6 +232,18 @@ class Engine:
         if check:
             self._ck(rc)
         return rc, ms.value
+
+    def advance_rounds(self, max_coll=2**62, t_stop=float("inf"), flags=0, radius=3,
+                       max_rounds=2**24, check=True):
+        """Round-parallel advance; returns (status, ms, rounds, violations)."""
+        ms = C.c_float()
+        rounds = C.c_int64()
+        viol = C.c_int64()
+        rc = self._L.edmd_advance_rounds(self.h, int(max_coll), float(t_stop), int(flags), int(radius),
+                                         int(max_rounds), C.byref(ms), C.byref(rounds), C.byref(viol))
+        if check:
+            self._ck(rc)
+        return rc, ms.value, rounds.value, viol.value
 
     def sync(self):
         self._ck(self._L.edmd_sync(self.h))

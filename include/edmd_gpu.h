@@ -56,6 +56,7 @@ extern "C" {
 #define EDMD_F_TRACE           4u  /* record accepted collisions              */
 #define EDMD_F_COUNT_NORMAL    8u  /* max_coll counts normal-phase only       */
 #define EDMD_F_LOG            16u  /* record collision geometry (edmd_log_entry) */
+#define EDMD_F_EXACT          32u  /* edmd_advance_rounds: replay on a causality violation */
 
 /*
  * One periodic 2D system.  Replaces the globals that constantInit
@@ -133,6 +134,31 @@ int edmd_load_state(edmd_ctx* ctx, const double* x, const double* y, const doubl
  * CUDA events on the context's stream. */
 int edmd_advance(edmd_ctx* ctx, int64_t max_coll, double t_stop, uint32_t flags,
                  int64_t max_events, float* elapsed_ms);
+
+/* Round-parallel advance of the constant-radius phase (replaces the same loop
+ * body as edmd_advance, src/EDMD.c:523-618, for many events at once).  Each
+ * round processes, in every system, the pending events that are the earliest
+ * within `radius` cells (3..12) of their footprint (owner's cell plus partner's
+ * or target cell), one GPU thread per event; screenshot events act as barriers
+ * (every disk is free-flown to them, src/EDMD.c:4657-4661).  A system stops at
+ * t_stop, or once it has accepted max_coll collisions in this call: it then
+ * finishes the pending events earlier than the latest one it processed, so
+ * the call always ends on a state of the serial run (ncol may exceed max_coll
+ * by the events of that drain).  At most max_rounds rounds are run (rounded up
+ * to a multiple of 16).  Thermo rows are not produced.
+ * Collisions, crossings and the final state are those of the serial algorithm
+ * unless *violations_out > 0: events processed before an earlier event of the
+ * same region, detected exactly with per-cell time stamps (a larger radius
+ * makes them rarer).  With EDMD_F_EXACT the call keeps a device copy of the
+ * engine state and, after a violation, replays from it with a 2x wider window
+ * (up to radius 12; a violation there returns EDMD_ERR_BUDGET), so a successful
+ * call is always the serial result and *violations_out counts the discarded
+ * ones.
+ * EDMD_F_TRACE records collisions in processing order.  After this call
+ * edmd_advance refuses the context until edmd_load_state restages it. */
+int edmd_advance_rounds(edmd_ctx* ctx, int64_t max_coll, double t_stop, uint32_t flags,
+                        int32_t radius, int64_t max_rounds, float* elapsed_ms,
+                        int64_t* rounds_out, int64_t* violations_out);
 
 /* Free-fly every disk of every system to its current time, the first step of
  * takeAScreenshot (src/EDMD.c:4657-4661). */
