@@ -4,23 +4,31 @@
 Metric: accepted pair collisions per second on one GB300 (the reference's
 ``ncol`` increments, src/EDMD.c:3558; growth-phase collisions excluded).
 
-Default workload ("batched"): 4096 independent periodic systems, N uniform in
-[256, 4096], area fraction uniform in [0.30, 0.75], 50:50 bidisperse diameters
-1.0/1.4 (-x 0.5 -q 0.7142857), per-system seeds, the reference's growth start
-(untimed set-up), then one step = 10^5 accepted collisions per system in one
-persistent launch.  Data are synthetic (the reference has no dataset); the
-state (~1 GB) is far larger than L2, so no flush is needed between steps.
-
-``--workload plain_small`` runs the single 1980-disk Hex system (phi 0.70)
-instead, one step = 10^5 collisions.
+Workloads (``--workload``):
+  batched       (default) 4096 independent periodic systems, N uniform in
+                [256, 4096], area fraction uniform in [0.30, 0.75], 50:50
+                bidisperse diameters 1.0/1.4 (-x 0.5 -q 0.7142857), per-system
+                seeds, the reference's growth start (untimed set-up), then one
+                step = 10^5 accepted collisions per system.  Serial-exact warp
+                engine by default (one persistent launch per step).
+  single_large  one Hex system of 10^6 monodisperse disks at phi = 0.72,
+                10^5 equilibration collisions (untimed), one step = 2*10^7
+                collisions in the round-parallel engine (exact mode).
+  plain_small   one 1980-disk Hex system at phi = 0.70, one step = 10^5
+                collisions, serial-exact warp engine (the plain GPU path).
+Data are synthetic (the reference has no dataset).  The batched state
+(~1.4 GB) and the single_large state (~0.2 GB) are larger than L2, so no
+flush is needed between steps.
 
 The JSON line carries the device-resident throughput (``value``), the
 end-to-end throughput through the C ABI with host buffers (``e2e``: restart
 from pinned host state, run, read the state back), the roofline of the run
-kernel, the CPU baseline (the oracle on all host cores) and the SM clocks
-sampled during the timed region.  ``--impl reference`` times the reference
-algorithm on the host cores (the oracle restatement; the reference's own C
-cannot be compiled where the benchmark runs).
+kernels, the CPU baseline (the oracle restatement on the host cores) and the SM
+clocks sampled during the timed region.  The default run also measures the
+single_large workload and reports it under ``other_workloads``.
+``--impl reference`` times the reference algorithm on the host cores (the
+oracle restatement; the reference's own C cannot be compiled where the
+benchmark runs).
 """
 import argparse
 import json
@@ -37,9 +45,16 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
-METRIC = "collisions/s on 1 GB300 (batched systems)"
 UNIT = "collisions/s"
 XS, Q = 0.5, 0.7142857
+METRICS = {
+    "batched": "collisions/s on 1 GB300 (batched systems)",
+    "single_large": "collisions/s on 1 GB300 (single 10^6-disk system, round-parallel)",
+    "plain_small": "collisions/s on 1 GB300 (plain single system)",
+}
+DEFAULT_COLL = {"batched": 100000, "single_large": 20000000, "plain_small": 100000}
+DEFAULT_ENGINE = {"batched": "warp", "single_large": "round", "plain_small": "warp"}
+LARGE_N, LARGE_PHI, LARGE_EQUIL = 1000000, 0.72, 100000
 
 
 def _load_edmd():
@@ -67,9 +82,11 @@ def batched_params(nsys, seed, rank):
 def _cpu_worker(conn, params, coll):
     """One reference-semantics system per process (the oracle), single-threaded."""
     from oracle import oracle as orc
-    N, phi, seed, hex_ = params
-    if hex_:
+    N, phi, seed, kind = params
+    if kind == "hex":
         o = orc.Oracle(N=N, phi=phi, seed=seed, start=orc.HEX, tmax=1e30)
+        if N >= LARGE_N:
+            o.run(LARGE_EQUIL, cap=1)                          # equilibration, untimed
     else:
         o = orc.Oracle(N=N, phi=phi, seed=seed, start=orc.GROW, xs=XS, q=Q, tmax=1e30)
         vr = orc.load().orc_vr(o.h)
@@ -112,8 +129,14 @@ class CpuPool:
 
 def cpu_sample_params(workload, ncores, seed):
     if workload == "plain_small":
-        return [(2000, 0.70, seed + k, True) for k in range(ncores)]
-    return [(n, p, s, False) for n, p, s in batched_params(ncores, seed, 0)]
+        return [(2000, 0.70, seed + k, "hex") for k in range(ncores)]
+    if workload == "single_large":
+        return [(LARGE_N, LARGE_PHI, seed, "hex")]          # one system: one thread
+    return [(n, p, s, "grow") for n, p, s in batched_params(ncores, seed, 0)]
+
+
+def cpu_sample_coll(workload, a):
+    return a.cpu_coll if workload != "single_large" else 2000000
 
 
 # ------------------------------------------------------------------ clocks
@@ -199,8 +222,9 @@ def run_reference(a, rank, world, dist):
     if rank != 0:
         return 0
     ncores = os.cpu_count() or 1
-    coll = a.ref_coll
-    pool = CpuPool(cpu_sample_params(a.workload, ncores, a.seed), coll)
+    coll = a.ref_coll if a.workload != "single_large" else 2000000
+    params = cpu_sample_params(a.workload, ncores, a.seed)
+    pool = CpuPool(params, coll)
     for _ in range(a.warmup):
         pool.step()
     tot, wall = 0, 0.0
@@ -209,15 +233,14 @@ def run_reference(a, rank, world, dist):
         tot += n; wall += w
     pool.close()
     v = tot / wall
-    line = {"impl": "reference", "metric": METRIC if a.workload == "batched" else "collisions/s on 1 GB300 (plain single system)",
+    sample = (f"{len(params)} systems of the workload, one per process, {coll} collisions each per step, "
+              f"oracle restatement (-O2 IEEE), set-up untimed")
+    line = {"impl": "reference", "metric": METRICS[a.workload],
             "value": v, "unit": UNIT, "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup,
             "ms_per_step": 1000 * wall / a.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": a.workload, "sample": f"{ncores} systems, one per process, "
-                                                         f"{coll} collisions each per step"},
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": ncores, "kind": "port",
-                             "sample": f"{ncores} processes x {coll} collisions per step, oracle restatement "
-                                       f"(-O2 IEEE), growth untimed"},
+            "config": {"workload": a.workload, "sample": sample},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": len(params), "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
@@ -225,54 +248,71 @@ def run_reference(a, rank, world, dist):
 
 # ------------------------------------------------------------------ GPU arm
 
-def build_systems(edmd, a, rank):
+def build_systems(edmd, workload, nsys, seed, rank):
     systems = []
-    if a.workload == "plain_small":
-        for k in range(a.nsys):
-            s = edmd.hex_start(2000, 0.70, a.seed + rank * a.nsys + k)
+    if workload == "plain_small":
+        for k in range(nsys):
+            s = edmd.hex_start(2000, 0.70, seed + rank * nsys + k)
             s["desc"] = edmd.default_desc(s["N"], s["Lx"], s["Ly"], 0.0, 1e30)
             systems.append(s)
         return systems
-    for N, phi, seed in batched_params(a.nsys, a.seed, rank):
-        s = edmd.grow_start(N, phi, seed, xs=XS, q=Q)
+    if workload == "single_large":
+        s = edmd.hex_start(LARGE_N, LARGE_PHI, seed + rank)
+        s["desc"] = edmd.default_desc(s["N"], s["Lx"], s["Ly"], 0.0, 1e30)
+        return [s]
+    for N, phi, sd in batched_params(nsys, seed, rank):
+        s = edmd.grow_start(N, phi, sd, xs=XS, q=Q)
         s["desc"] = edmd.default_desc(N, s["Lx"], s["Ly"], s["vr_base"], 1e30)
         systems.append(s)
     return systems
 
 
-def run_ours(a, rank, world, dist):
-    cpu_pool = None
-    ncores = os.cpu_count() or 1
-    if rank == 0 and world == 1 and not a.no_cpu_baseline:
-        # spawn the CPU-baseline processes before the first GPU call
-        cpu_pool = CpuPool(cpu_sample_params(a.workload, ncores, a.seed), a.cpu_coll)
-    edmd = _load_edmd()
-    L = edmd.load()
-    dev = int(os.environ.get("LOCAL_RANK", "0"))
-    if world > 1:
-        L.edmd_set_device(dev)
-    systems = build_systems(edmd, a, rank)
-    eng = edmd.Engine(systems)
+class Stepper:
+    """One timed step of a workload through the engine selected for it."""
+
+    def __init__(self, edmd, eng, engine, coll, radius):
+        self.edmd, self.eng, self.engine, self.coll, self.radius = edmd, eng, engine, coll, radius
+        self.launches = 0
+
+    def step(self):
+        if self.engine == "round":
+            _, ms, rounds, _ = self.eng.advance_rounds(max_coll=self.coll, radius=self.radius,
+                                                       flags=self.edmd.F_EXACT)
+            self.launches += 5 * rounds + 4
+            return ms
+        _, ms = self.eng.advance(max_coll=self.coll, flags=self.edmd.F_COUNT_NORMAL)
+        self.launches += 1
+        return ms
+
+
+def measure(edmd, a, workload, engine, coll, steps, warmup, rank, world, dist, dev, e2e_steps):
+    nsys = a.nsys if a.nsys is not None else (4096 if workload == "batched" else 1)
+    systems = build_systems(edmd, workload, nsys, a.seed, rank)
+    eng = edmd.Engine(systems, engine=edmd.ENGINE_LANE if engine == "lane" else edmd.ENGINE_WARP)
     TN = sum(s["desc"].N for s in systems)
     TC = sum(int(s["desc"].Lx / 2) * int(s["desc"].Ly / 2) for s in systems)
-    # set-up: growth phase to completion (untimed), then warm-up steps
-    if a.workload == "batched":
+    # untimed set-up: growth phase, or equilibration of the large system
+    if workload == "batched":
         eng.advance(flags=edmd.F_STOP_AT_GROW)
         c = eng.all_counters()
         assert not c["growing"].any(), "growth did not finish"
-    for _ in range(a.warmup):
-        eng.advance(max_coll=a.coll, flags=edmd.F_COUNT_NORMAL)
+    elif workload == "single_large":
+        eng.advance_rounds(max_coll=LARGE_EQUIL, radius=a.radius, flags=edmd.F_EXACT)
+    st = Stepper(edmd, eng, engine, coll, a.radius)
+    for _ in range(warmup):
+        st.step()
     c0 = eng.all_counters()
     clk = ClockSampler(dev)
     barrier(dist)
     clk.start()
+    st.launches = 0
     kern_ms = []
     t0 = time.perf_counter()
-    for _ in range(a.steps):
-        _, ms = eng.advance(max_coll=a.coll, flags=edmd.F_COUNT_NORMAL)
-        kern_ms.append(ms)
+    for _ in range(steps):
+        kern_ms.append(st.step())
     wall = time.perf_counter() - t0
     clocks = clk.stop()
+    launches = st.launches
     c1 = eng.all_counters()
     ncoll = int((c1["ncol"] - c0["ncol"]).sum())
     npair = int((c1["npair"] - c0["npair"]).sum())
@@ -283,28 +323,74 @@ def run_ours(a, rank, world, dist):
     value = coll_all / t_max
     # ---- end to end through the C ABI with pinned host buffers
     eng.sync()
-    st = eng.states()
+    stt = eng.states()
     pin = {k: edmd.PinnedArray(TN) for k in ("x", "y", "vx", "vy", "rad", "m")}
     for k in pin:
-        pin[k].a[:] = st[k]
+        pin[k].a[:] = stt[k]
     outs = {k: pin[k].a for k in pin}
-    e2e_steps = max(1, min(a.steps, 3))
     barrier(dist)
     t0 = time.perf_counter()
     e2e_coll = 0
     for _ in range(e2e_steps):
+        ca = eng.all_counters()["ncol"].sum()
         eng.load_state(*(pin[k].a for k in ("x", "y", "vx", "vy", "rad", "m")))
-        eng.advance(max_coll=a.coll, flags=edmd.F_COUNT_NORMAL)
+        cb = eng.all_counters()["ncol"].sum()
+        st.step()
+        e2e_coll += int(eng.all_counters()["ncol"].sum() - cb)
         eng.sync()
         eng.states(outs)
-        e2e_coll += a.coll * len(systems)
     e2e_wall = max_over_ranks(dist, time.perf_counter() - t0)
     e2e = sum_over_ranks(dist, e2e_coll) / e2e_wall
     for p in pin.values():
         p.free()
-    h2d = TN * (64 + 12) + TC * 4 + len(systems) * 176
-    d2h = TN * 6 * 8 + len(systems) * 4
+    h2d = TN * 6 * 8
+    d2h = TN * 6 * 8
     eng.close()
+    # roofline: algorithmic bytes per collision B = P_pair*S + P_pred*(S+24) + 4*S,
+    # S = 48 B (x, y, vx, vy, t, r in FP64)
+    S = 48
+    p_pair = npair / max(ncoll, 1)
+    p_pred = npred / max(ncoll, 1)
+    Bcoll = p_pair * S + p_pred * (S + 24) + 4 * S
+    achieved = Bcoll * ncoll / t_dev / 1e9
+    peaks = json.load(open(PEAKS)) if os.path.exists(PEAKS) else {}
+    peak = peaks.get("hbm_gbs", 6800.0)
+    kernel = ("k_run (one persistent launch per step)" if engine == "warp" else
+              "k_lane_run" if engine == "lane" else
+              "round engine graph: k_select + k_process + k_recompute + k_barrier per round")
+    return dict(value=value, ms_per_step=1000 * t_max / steps, wall=wall, clocks=clocks, launches=launches,
+                systems=len(systems), TN=TN, e2e=e2e, h2d=h2d, d2h=d2h,
+                roofline={"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                          "frac": achieved / peak, "traffic": None, "kernel": kernel,
+                          "bytes_per_collision": Bcoll, "p_pair": p_pair, "p_pred": p_pred,
+                          "peak_source": "measured hbm_gbs" if "hbm_gbs" in peaks else "fallback"})
+
+
+def run_ours(a, rank, world, dist):
+    cpu_pool = None
+    ncores = os.cpu_count() or 1
+    workload = a.workload
+    engine = a.engine if a.engine != "auto" else DEFAULT_ENGINE[workload]
+    coll = a.coll if a.coll is not None else DEFAULT_COLL[workload]
+    if rank == 0 and world == 1 and not a.no_cpu_baseline:
+        # spawn the CPU-baseline processes before the first GPU call
+        cpu_pool = CpuPool(cpu_sample_params(workload, ncores, a.seed), cpu_sample_coll(workload, a))
+    edmd = _load_edmd()
+    L = edmd.load()
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        L.edmd_set_device(dev)
+    r = measure(edmd, a, workload, engine, coll, a.steps, a.warmup, rank, world, dist, dev,
+                max(1, min(a.steps, 3)))
+    other = {}
+    if workload == "batched" and not a.no_secondary:
+        s = measure(edmd, a, "single_large", "round", DEFAULT_COLL["single_large"], 3, 3, rank, world,
+                    dist, dev, 1)
+        other["single_large"] = {"metric": METRICS["single_large"], "value": s["value"], "unit": UNIT,
+                                 "engine": "round (exact mode, radius %d)" % a.radius,
+                                 "ms_per_step": s["ms_per_step"], "e2e": s["e2e"],
+                                 "roofline": s["roofline"], "clocks": s["clocks"],
+                                 "gpu_launches": s["launches"]}
     if rank != 0:
         if cpu_pool:
             cpu_pool.close()
@@ -313,39 +399,36 @@ def run_ours(a, rank, world, dist):
     if cpu_pool:
         n, w, rate = cpu_pool.step()
         cpu_pool.close()
-        cpu = {"value": n / w, "unit": UNIT, "cores": ncores, "kind": "port",
-               "sample": f"{ncores} systems of the same workload, one per process, {a.cpu_coll} collisions "
-                         f"each, oracle restatement (-O2 IEEE), growth untimed"}
-    # roofline: algorithmic bytes per collision B = P_pair*S + P_pred*(S+24) + 4*S,
-    # S = 48 B (x, y, vx, vy, t, r in FP64) -- see the design doc
-    S = 48
-    p_pair = npair / max(ncoll, 1)
-    p_pred = npred / max(ncoll, 1)
-    Bcoll = p_pair * S + p_pred * (S + 24) + 4 * S
-    achieved = Bcoll * ncoll / t_dev / 1e9
-    peak = json.load(open(PEAKS))["hbm_gbs"] if os.path.exists(PEAKS) else 6800.0
+        nproc = len(cpu_pool.p)
+        cpu = {"value": n / w, "unit": UNIT, "cores": nproc, "kind": "port",
+               "sample": f"{nproc} system(s) of the same workload, one per process, "
+                         f"{cpu_sample_coll(workload, a)} collisions each, oracle restatement (-O2 IEEE), "
+                         f"set-up untimed"}
+    workload_desc = {
+        "batched": "batched: %d systems/GPU, N~U[256,4096], phi~U[0.30,0.75], bidisperse 1.0/1.4, growth start"
+                   % r["systems"],
+        "single_large": "single Hex system, N=%d, phi=%.2f, %d equilibration collisions" %
+                        (r["TN"], LARGE_PHI, LARGE_EQUIL),
+        "plain_small": "single Hex system, N=1980, phi=0.70",
+    }[workload]
     line = {
-        "metric": METRIC if a.workload == "batched" else "collisions/s on 1 GB300 (plain single system)",
-        "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
-        "ms_per_step": 1000 * t_max / a.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": a.workload if a.workload != "batched" else
-                   "batched: 4096 systems/GPU, N~U[256,4096], phi~U[0.30,0.75], bidisperse 1.0/1.4, growth start",
-                   "systems_per_gpu": len(systems), "disks_per_gpu": TN,
-                   "collisions_per_system_per_step": a.coll,
-                   "l2": "state (~%.0f MB/GPU) larger than L2, no flush" % (TN * 160 / 1e6),
+        "metric": METRICS[workload], "value": r["value"], "unit": UNIT, "n_gpus": world,
+        "steps": a.steps, "warmup": a.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": workload_desc, "engine": engine, "systems_per_gpu": r["systems"],
+                   "disks_per_gpu": r["TN"], "collisions_per_system_per_step": coll,
+                   "l2": "state (~%.0f MB/GPU) larger than L2, no flush" % (r["TN"] * 160 / 1e6),
                    "parallelism": f"replicas x{world}"},
-        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "path": "edmd_load_state (pinned host) + edmd_advance + edmd_get_states (pinned host)"},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": None, "kernel": "k_run",
-                     "bytes_per_collision": Bcoll, "p_pair": p_pair, "p_pred": p_pred,
-                     "peak_source": "measured hbm_gbs" if os.path.exists(PEAKS) else "fallback"},
+        "e2e": {"value": r["e2e"], "unit": UNIT, "h2d_bytes_per_step": r["h2d"], "d2h_bytes_per_step": r["d2h"],
+                "path": "edmd_load_state (pinned host) + advance + edmd_sync + edmd_get_states (pinned host)"},
+        "roofline": r["roofline"],
         "cpu_baseline": cpu,
-        "clocks": clocks,
-        "gpu_launches": a.steps,
-        "wall_s": wall,
+        "clocks": r["clocks"],
+        "gpu_launches": r["launches"],
+        "wall_s": r["wall"],
     }
+    if other:
+        line["other_workloads"] = other
     print(json.dumps(line), flush=True)
     return 0
 
@@ -356,16 +439,17 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="batched", choices=["batched", "plain_small"])
+    ap.add_argument("--workload", default="batched", choices=["batched", "single_large", "plain_small"])
+    ap.add_argument("--engine", default="auto", choices=["auto", "warp", "lane", "round"])
+    ap.add_argument("--radius", type=int, default=3)
     ap.add_argument("--nsys", type=int, default=None)
-    ap.add_argument("--coll", type=int, default=100000)
+    ap.add_argument("--coll", type=int, default=None)
     ap.add_argument("--cpu-coll", type=int, default=1000000)
     ap.add_argument("--ref-coll", type=int, default=300000)
     ap.add_argument("--seed", type=int, default=20261203)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-secondary", action="store_true")
     a = ap.parse_args()
-    if a.nsys is None:
-        a.nsys = 4096 if a.workload == "batched" else 1
     if a.warmup < 3 and a.impl == "ours":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
     rank, world, dist = dist_init(a.gpus)

@@ -44,6 +44,7 @@ namespace {
 
 constexpr uint64_t KINF = ~0ull;
 constexpr int32_t IINF = 0x7fffffff;
+constexpr int32_t GMASK = 0xffffff;   // disk index inside an event id (rank in the top byte)
 constexpr unsigned FULLM = 0xffffffffu;
 constexpr int TX = 32, TY = 8;        // selection tile (cells)
 constexpr int RTILE = 12;             // largest window radius of the tile kernel
@@ -64,8 +65,10 @@ struct RoundArgs {
   const int64_t* doff;           // disk offset of each system
   const int64_t* coff;           // cell offset of each system
   uint64_t* dkey;                // time key of each disk's next event (KINF: none)
+  int32_t* dpk;                  // its id: serial tie rank << 24 | disk
+  uint8_t* drank;                // tie rank of each disk's collision event
   int32_t* fc;                   // its two footprint cells (local), 2 per disk
-  uint64_t* cmt; int32_t* cmi;   // attributed minimum per cell
+  uint64_t* cmt; int32_t* cmi;   // attributed minimum (key, id) per cell
   uint64_t* lw; uint64_t* lr;    // causality stamps per cell
   int32_t* safe; int32_t* nsafe; // selected events of the round
   int32_t* dcell;                // cells to recompute, MAXDIRTY per selected event
@@ -129,7 +132,7 @@ __device__ __forceinline__ bool adjacent(const Box& B, int a, int b) {
 
 // next event key and footprint of disk i; the collision slot's `b` field holds
 // the partner's cell at prediction time
-__device__ __forceinline__ void attribution(const SysDev& S, int i, uint64_t* key, int* c1, int* c2) {
+__device__ __forceinline__ int attribution(const SysDev& S, int i, uint64_t* key, int* c1, int* c2) {
   const int slot = next_slot(S, i, key);
   const Box& B = S.B;
   const int cx = S.cx[i], cy = S.cy[i];
@@ -137,9 +140,40 @@ __device__ __forceinline__ void attribution(const SysDev& S, int i, uint64_t* ke
   if (slot < 0) *c2 = *c1;
   else if (slot >= B.N) *c2 = (int)S.ev[slot].b;
   else *c2 = target_cell(B, cx, cy, S.ev[slot].j);
+  return slot;
+}
+
+// id of disk g's next event: a collision carries its serial tie rank
+__device__ __forceinline__ int32_t event_id(const RoundArgs& A, int64_t g, int slot, int N) {
+  return (slot >= N ? ((int32_t)A.drank[g] << 24) : 0) | (int32_t)g;
 }
 
 // ---------------------------------------------------------------- per call
+
+// Exactly equal times of conflicting events are ordered like the serial queue
+// orders them.  The only such ties the serial state carries in quantity are
+// mutual predictions a->b, b->a made by one handler from the same positions
+// (the initial predictions, and stopGrow, src/EDMD.c:4740-4800, whose coll++
+// inside the loop leaves one of the two stale); their serial order is the
+// order of their queue keys (b, tie).  Rank 0 or 1 orders such a pair; events
+// the round engine creates later get rank 2 (a new prediction is never stale,
+// so a tie of two valid mutual events gives the same state either way).
+__global__ void k_rank(const SysDev* __restrict__ sys, RoundArgs A) {
+  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= A.TN) return;
+  const int s = A.dsys[g];
+  const SysDev& S = sys[s];
+  const int N = S.B.N;
+  const int i = (int)(g - A.doff[s]);
+  const Ev e = S.ev[N + i];
+  uint8_t rank = 0;
+  if (e.st & 3u) {
+    const Ev f = S.ev[N + e.j];
+    if ((f.st & 3u) && f.j == i && __double_as_longlong(f.t) == __double_as_longlong(e.t))
+      rank = (f.b < e.b || (f.b == e.b && f.tie < e.tie)) ? 1 : 0;
+  }
+  A.drank[g] = rank;
+}
 
 // serial pop clock and stored partner cell of every pending event, then the
 // attribution of every disk
@@ -165,8 +199,9 @@ __global__ void k_prep(const SysDev* __restrict__ sys, RoundArgs A) {
   }
   uint64_t key;
   int c1, c2;
-  attribution(S, i, &key, &c1, &c2);
+  const int slot = attribution(S, i, &key, &c1, &c2);
   A.dkey[g] = key;
+  A.dpk[g] = event_id(A, g, slot, N);
   A.fc[2 * g] = c1;
   A.fc[2 * g + 1] = c2;
   if (key != KINF) {
@@ -182,8 +217,9 @@ __global__ void k_prep_owner(RoundArgs A) {
   if (key == KINF) return;
   const int64_t base = A.coff[A.dsys[g]];
   const int64_t a = base + A.fc[2 * g], b = base + A.fc[2 * g + 1];
-  if (A.cmt[a] == key) atomicMin(&A.cmi[a], (int32_t)g);
-  if (b != a && A.cmt[b] == key) atomicMin(&A.cmi[b], (int32_t)g);
+  const int32_t id = A.dpk[g];
+  if (A.cmt[a] == key) atomicMin(&A.cmi[a], id);
+  if (b != a && A.cmt[b] == key) atomicMin(&A.cmi[b], id);
 }
 
 // eligibility bound of every system for the next round
@@ -273,9 +309,10 @@ __global__ void __launch_bounds__(256) k_select(const SysDev* __restrict__ sys, 
   if (cx < Nxc && cy < Nyc) {
     const int o = (iy + H) * CW + ix + H;
     const uint64_t k = ck[o];
-    g = ci[o];
+    const int32_t id = ci[o];
+    g = id & GMASK;
     const int w = (iy + 1) * HW + ix + 1;
-    if (k < lim && wk[w] == k && wi[w] == g) {
+    if (k < lim && wk[w] == k && wi[w] == id) {
       const int c = cy * Nxc + cx;
       if (A.fc[2 * (int64_t)g] == c) {
         const int c2 = A.fc[2 * (int64_t)g + 1];
@@ -289,7 +326,7 @@ __global__ void __launch_bounds__(256) k_select(const SysDev* __restrict__ sys, 
           if (dy < -1) dy += Nyc;
           if (dx >= -1 && dx <= 1 && dy >= -1 && dy <= 1) {
             const int w2 = (iy + 1 + dy) * HW + ix + 1 + dx;
-            sel = wk[w2] == k && wi[w2] == g;
+            sel = wk[w2] == k && wi[w2] == id;
           }
         }
       }
@@ -467,8 +504,9 @@ __device__ __forceinline__ void reattribute(const SysDev& S, const RoundArgs& A,
                                             int64_t base, int32_t* dc, int* nd) {
   uint64_t key;
   int c1, c2;
-  attribution(S, i, &key, &c1, &c2);
+  const int slot = attribution(S, i, &key, &c1, &c2);
   A.dkey[g] = key;
+  A.dpk[g] = event_id(A, g, slot, S.B.N);
   A.fc[2 * g] = c1;
   A.fc[2 * g + 1] = c2;
   dc[(*nd)++] = (int32_t)(base + c1);
@@ -548,6 +586,7 @@ __global__ void __launch_bounds__(32 * WPB) k_process(const SysDev* __restrict__
         nstale = 1;
         if (lane == 0) {
           set_event(S, N + a, t + p0.dt, p0.partner, p0.ca, p0.pcell, clk);
+          A.drank[g] = 2;
           reattribute(S, A, a, g, base, dc, &nd);
         }
       } else {
@@ -604,6 +643,8 @@ __global__ void __launch_bounds__(32 * WPB) k_process(const SysDev* __restrict__
           set_event(S, b, tc, dir, 0, 0, clk);
           set_event(S, N + a, t + p0.dt, p0.partner, p0.ca, p0.pcell, clk);
           set_event(S, N + b, t + p1.dt, p1.partner, p1.ca, p1.pcell, clk);
+          A.drank[g] = 2;
+          A.drank[gb] = 2;
           reattribute(S, A, a, g, base, dc, &nd);
           reattribute(S, A, b, gb, base, dc, &nd);
         }
@@ -648,6 +689,7 @@ __global__ void __launch_bounds__(32 * WPB) k_process(const SysDev* __restrict__
         const double tc = crossing_time_i(B, Da, cx, cy, t, &dir);
         set_event(S, a, tc, dir, 0, 0, clk);
         set_event(S, N + a, t + p0.dt, p0.partner, p0.ca, p0.pcell, clk);
+        A.drank[g] = 2;
         reattribute(S, A, a, g, base, dc, &nd);
       }
     }
@@ -702,9 +744,9 @@ __global__ void __launch_bounds__(256) k_recompute(const SysDev* __restrict__ sy
       while (p != NIL && guard++ < B.N) {
         const int64_t g = dbase + p;
         const uint64_t k = A.dkey[g];
-        if (k != KINF && (A.fc[2 * g] == c || A.fc[2 * g + 1] == c) && pair_less(k, (int32_t)g, bk, bi)) {
+        if (k != KINF && (A.fc[2 * g] == c || A.fc[2 * g + 1] == c) && pair_less(k, A.dpk[g], bk, bi)) {
           bk = k;
-          bi = (int32_t)g;
+          bi = A.dpk[g];
         }
         p = S.d[p].nxt;
       }
@@ -815,7 +857,8 @@ __global__ void k_round_setup(const int64_t* __restrict__ doff, const SysDev* __
 
 struct RoundBufs {
   int32_t *dsys = nullptr, *fc = nullptr, *cmi = nullptr, *safe = nullptr, *nsafe = nullptr;
-  int32_t *dcell = nullptr, *selflag = nullptr, *active = nullptr;
+  int32_t *dcell = nullptr, *selflag = nullptr, *active = nullptr, *dpk = nullptr;
+  uint8_t *drank = nullptr, *drank_bak = nullptr;
   int32_t *tsys = nullptr, *tx0 = nullptr, *ty0 = nullptr;
   int64_t *doff = nullptr, *coff = nullptr;
   uint64_t *dkey = nullptr, *cmt = nullptr, *lw = nullptr, *lr = nullptr;
@@ -842,7 +885,9 @@ int round_init(edmd_ctx* ctx) {
       }
   }
   R->ntiles = (int64_t)tsys.size();
-  CK(dalloc(&R->dsys, TN)); CK(dalloc(&R->fc, 2 * TN)); CK(dalloc(&R->dkey, TN));
+  if (TN > GMASK) return set_err(ctx, EDMD_ERR_CAPACITY, "the round engine supports up to 2^24 disks per context");
+  CK(dalloc(&R->dsys, TN)); CK(dalloc(&R->fc, 2 * TN)); CK(dalloc(&R->dkey, TN)); CK(dalloc(&R->dpk, TN));
+  CK(dalloc(&R->drank, TN)); CK(dalloc(&R->drank_bak, TN));
   CK(dalloc(&R->cmi, TC)); CK(dalloc(&R->cmt, TC)); CK(dalloc(&R->lw, TC)); CK(dalloc(&R->lr, TC));
   CK(dalloc(&R->safe, TN)); CK(dalloc(&R->nsafe, 1)); CK(dalloc(&R->dcell, TN * MAXDIRTY));
   CK(dalloc(&R->selflag, ctx->nsys)); CK(dalloc(&R->active, 1));
@@ -886,7 +931,8 @@ void round_free(edmd_ctx* ctx) {
   if (!R) return;
   void* p[] = {R->dsys, R->fc, R->cmi, R->safe, R->nsafe, R->dcell, R->selflag, R->active,
                R->tsys, R->tx0, R->ty0, R->doff, R->coff, R->dkey, R->cmt, R->lw, R->lr,
-               R->lim, R->target, R->freeze, R->tlast, R->cnt, R->viol};
+               R->lim, R->target, R->freeze, R->tlast, R->cnt, R->viol, R->dpk, R->drank,
+               R->drank_bak};
   for (void* q : p)
     if (q) cudaFree(q);
   delete R;
@@ -895,8 +941,8 @@ void round_free(edmd_ctx* ctx) {
 
 // rounds until every system has stopped
 static int run_rounds(edmd_ctx* ctx, const std::vector<uint64_t>& tgt, double t_stop, uint32_t flags,
-                      int32_t radius, int64_t max_rounds, int64_t* rounds_out, int32_t* active_out,
-                      unsigned long long* viol_out) {
+                      int32_t radius, bool fresh, int64_t max_rounds, int64_t* rounds_out,
+                      int32_t* active_out, unsigned long long* viol_out) {
   const RoundBufs* R = (const RoundBufs*)ctx->round;
   cudaStream_t st = ctx->stream;
   const int64_t TN = ctx->total_N, TC = ctx->total_C;
@@ -919,11 +965,14 @@ static int run_rounds(edmd_ctx* ctx, const std::vector<uint64_t>& tgt, double t_
     A.tstop_key = (u >> 63) ? ~u : (u | 0x8000000000000000ull);
   }
   A.dsys = R->dsys; A.doff = R->doff; A.coff = R->coff;
-  A.dkey = R->dkey; A.fc = R->fc; A.cmt = R->cmt; A.cmi = R->cmi; A.lw = R->lw; A.lr = R->lr;
+  A.dkey = R->dkey; A.dpk = R->dpk; A.drank = R->drank; A.fc = R->fc; A.cmt = R->cmt; A.cmi = R->cmi; A.lw = R->lw; A.lr = R->lr;
   A.safe = R->safe; A.nsafe = R->nsafe; A.dcell = R->dcell; A.selflag = R->selflag;
   A.active = R->active; A.lim = R->lim; A.target = R->target; A.freeze = R->freeze;
   A.tlast = R->tlast; A.cnt = R->cnt; A.tsys = R->tsys; A.tx0 = R->tx0; A.ty0 = R->ty0; A.violations = R->viol;
   const unsigned gd = (unsigned)((TN + 255) / 256);
+  // the serial queue keys are still in the event records only when the
+  // state comes from a serial engine
+  if (fresh) k_rank<<<gd, 256, 0, st>>>(ctx->ds, A);
   k_prep<<<gd, 256, 0, st>>>(ctx->ds, A);
   k_prep_owner<<<gd, 256, 0, st>>>(A);
   k_limits<<<(ctx->nsys + 127) / 128, 128, 0, st>>>(ctx->ds, A);
@@ -993,9 +1042,12 @@ extern "C" int edmd_advance_rounds(edmd_ctx* ctx, int64_t max_coll, double t_sto
     tgt[s] = st[s].ncol + (uint64_t)max_coll;
   }
   const bool exact = (flags & EDMD_F_EXACT) != 0;
+  const bool fresh = !ctx->round_dirty;
+  const RoundBufs* R = (const RoundBufs*)ctx->round;
   if (exact) {
     rc = ckpt_save(ctx, CKPT_ROUND);
     if (rc) return rc;
+    if (!fresh) CK(cudaMemcpyAsync(R->drank_bak, R->drank, ctx->total_N, cudaMemcpyDeviceToDevice, ctx->stream));
   }
   ctx->round_dirty = true;
   CK(cudaEventRecord(ctx->e0, ctx->stream));
@@ -1004,7 +1056,7 @@ extern "C" int edmd_advance_rounds(edmd_ctx* ctx, int64_t max_coll, double t_sto
   int32_t r = radius;
   for (;;) {
     unsigned long long v = 0;
-    rc = run_rounds(ctx, tgt, t_stop, flags, r, max_rounds, &rounds, &active, &v);
+    rc = run_rounds(ctx, tgt, t_stop, flags, r, fresh, max_rounds, &rounds, &active, &v);
     if (rc) return rc;
     viol_total += (int64_t)v;
     if (!exact || v == 0 || active) break;
@@ -1012,6 +1064,7 @@ extern "C" int edmd_advance_rounds(edmd_ctx* ctx, int64_t max_coll, double t_sto
     if (r >= RTILE) return set_err(ctx, EDMD_ERR_BUDGET, "round engine: violation at the widest window");
     rc = ckpt_restore(ctx, CKPT_ROUND);
     if (rc) return rc;
+    if (!fresh) CK(cudaMemcpyAsync(R->drank, R->drank_bak, ctx->total_N, cudaMemcpyDeviceToDevice, ctx->stream));
     ctx->round_dirty = true;
     r = r * 2 < RTILE ? r * 2 : RTILE;
   }
