@@ -441,7 +441,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="batched", choices=["batched", "single_large", "plain_small"])
     ap.add_argument("--engine", default="auto", choices=["auto", "warp", "lane", "round"])
-    ap.add_argument("--radius", type=int, default=3)
+    ap.add_argument("--radius", type=int, default=4)
     ap.add_argument("--nsys", type=int, default=None)
     ap.add_argument("--coll", type=int, default=None)
     ap.add_argument("--cpu-coll", type=int, default=1000000)

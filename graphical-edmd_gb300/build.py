@@ -20,7 +20,7 @@ HOST = os.path.join(HERE, "host")
 INCLUDE = os.path.join(ROOT, "include")
 BUILD = os.path.join(HERE, "_build")
 
-CUDA_SOURCES = ["edmd_engine.cu", "edmd_lane.cu", "edmd_tangent.cu", "edmd_round.cu"]
+CUDA_SOURCES = ["edmd_engine.cu", "edmd_lane.cu", "edmd_tangent.cu", "edmd_round.cu", "edmd_observe.cu"]
 HOST_SOURCES = ["edmd_init.c"]
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "--fmad=false",
               "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I" + INCLUDE]

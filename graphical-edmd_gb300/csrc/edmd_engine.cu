@@ -89,9 +89,7 @@ __device__ void leaf_update(const SysDev& S, int leaf, int lane) {
   if (lane == 0) S.tree[leaf] = n;
   __syncwarp();
   int idx = leaf;
-#pragma unroll
-  for (int h = 1; h < MAXLEV; h++) {
-    if (h >= S.nlev) break;
+  for (int h = 1; h < S.nlev; h++) {
     int par = idx >> 5;
     int ch = (par << 5) + lane;
     Node c = ch < S.lev_cnt[h - 1] ? S.tree[S.lev_off[h - 1] + ch] : empty_node(0x7fffffff);
@@ -212,8 +210,7 @@ __device__ __forceinline__ double pair_time(const SysDev& S, const Disk& A, int 
 
 __device__ __forceinline__ void best_merge(double& bd, int& bo, int& bp, uint32_t& bc,
                                            double d, int o, int p, uint32_t c) {
-  uint64_t kd = time_key(d), kb = time_key(bd);
-  if (kd < kb || (kd == kb && o < bo)) { bd = d; bo = o; bp = p; bc = c; }
+  if (d < bd || (d == bd && o < bo)) { bd = d; bo = o; bp = p; bc = c; }
 }
 
 // collisionEventNormal / Grow (src/EDMD.c:2829 / 3104) for disks a0 and a1

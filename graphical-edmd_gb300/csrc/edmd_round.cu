@@ -59,6 +59,7 @@ struct RoundArgs {
   int32_t nsys;
   int32_t radius;
   int64_t TN;
+  int32_t ntiles;
   uint32_t flags;
   uint64_t tstop_key;
   const int32_t* dsys;           // system of each disk
@@ -251,10 +252,10 @@ __device__ __forceinline__ int wrapi(int v, int n) {
 // window minima of one tile in shared memory and selection of its events
 __global__ void __launch_bounds__(256) k_select(const SysDev* __restrict__ sys, RoundArgs A) {
   extern __shared__ unsigned char smem[];
-  const int t = blockIdx.x;
+  for (int t = blockIdx.x; t < A.ntiles; t += gridDim.x) {
   const int s = A.tsys[t];
   const uint64_t lim = A.lim[s];
-  if (lim == 0) return;
+  if (lim == 0) continue;             // the system has stopped: nothing to select
   const Box& B = sys[s].B;
   const int Nxc = B.Nxc, Nyc = B.Nyc;
   const int x0 = A.tx0[t], y0 = A.ty0[t];
@@ -341,6 +342,8 @@ __global__ void __launch_bounds__(256) k_select(const SysDev* __restrict__ sys, 
     pos = __shfl_sync(FULLM, pos, lead);
     if (sel) A.safe[pos + __popc(m & ((1u << lane) - 1))] = g;
     if (lane == lead) A.selflag[s] = 1;
+  }
+  __syncthreads();
   }
 }
 
@@ -534,6 +537,20 @@ __device__ __forceinline__ void cnt_addf(const RoundArgs& A, int s, int stripe, 
   atomicAdd((double*)&A.cnt[((int64_t)s * NSTRIPE + stripe) * NCNT + k], v);
 }
 
+__device__ __forceinline__ Disk shfl_disk(const Disk& v, int src) {
+  Disk r;
+  r.x = __shfl_sync(FULLM, v.x, src);
+  r.y = __shfl_sync(FULLM, v.y, src);
+  r.vx = __shfl_sync(FULLM, v.vx, src);
+  r.vy = __shfl_sync(FULLM, v.vy, src);
+  r.tl = __shfl_sync(FULLM, v.tl, src);
+  r.rad = __shfl_sync(FULLM, v.rad, src);
+  r.m = __shfl_sync(FULLM, v.m, src);
+  r.nxt = __shfl_sync(FULLM, v.nxt, src);
+  r.coll = __shfl_sync(FULLM, v.coll, src);
+  return r;
+}
+
 // process the selected events, one warp each: doTheCollisionNormal
 // (src/EDMD.c:3542, elastic rule 3802-3827), its stale branch (3553-3556) or
 // doTheCrossing (2501).  The scalar work is repeated by every lane (same
@@ -564,17 +581,17 @@ __global__ void __launch_bounds__(32 * WPB) k_process(const SysDev* __restrict__
     dc[nd++] = (int32_t)(base + A.fc[2 * g]);
     if (A.fc[2 * g + 1] != A.fc[2 * g]) dc[nd++] = (int32_t)(base + A.fc[2 * g + 1]);
     Disk Da = S.d[a];
-    free_fly_i(B, Da, t);
     const int ax = S.cx[a], ay = S.cy[a];
     const int ca = cell_of(B, ax, ay);
     unsigned long long npair = 0, npred = 0, ncol = 0, ncross = 0, nstale = 0;
-    double ct[4] = {0, 0, 0, 0};
+    double ct[1] = {0};
     bool ovl = false, bad = false;
     int ob = -1;
     if (slot >= N) {
       const int b = E.j;
       Disk Db = S.d[b];
       if (E.ca != Db.coll) {
+        free_fly_i(B, Da, t);
         __syncwarp();
         if (lane == 0) S.d[a] = Da;
         bad |= lane == 0 && stamp_write(A, base, ca, clk);
@@ -595,9 +612,14 @@ __global__ void __launch_bounds__(32 * WPB) k_process(const SysDev* __restrict__
         if (A.fc[2 * gb + 1] != A.fc[2 * gb]) dc[nd++] = (int32_t)(base + A.fc[2 * gb + 1]);
         const int bx = S.cx[b], by = S.cy[b];
         const int cb = cell_of(B, bx, by);
-        free_fly_i(B, Db, t);
-        Da.coll++;
-        Db.coll++;
+        // even lanes advance a, odd lanes b: the per-disk FP64 work of the
+        // two disks shares its instructions
+        const bool odd = lane & 1;
+        Disk M = odd ? Db : Da;
+        free_fly_i(B, M, t);
+        M.coll++;
+        Da = shfl_disk(M, 0);
+        Db = shfl_disk(M, 1);
         double dx = Db.x - Da.x, dy = Db.y - Da.y;
         const double dvx = Db.vx - Da.vx, dvy = Db.vy - Da.vy;
         const double msum = Da.m + Db.m;
@@ -607,14 +629,28 @@ __global__ void __launch_bounds__(32 * WPB) k_process(const SysDev* __restrict__
         const double distSquared = 4 * Da.rad * Db.rad;
         const double f = distSquared == 4.0 ? collKernel * 0.25 : collKernel / distSquared;
         const double cf = Da.m * Db.m * f;
-        ct[0] = cf * dx * dx;
-        ct[1] = cf * dy * dy;
-        ct[2] = cf * dx * dy;
-        ct[3] = cf * dy * dx;
-        Da.vx += f * Db.m * dx;
-        Da.vy += f * Db.m * dy;
-        Db.vx -= f * Da.m * dx;
-        Db.vy -= f * Da.m * dy;
+        // virial term q on lane q: collTermX, Y, XY, YX
+        {
+          const double u = (lane == 1 || lane == 3) ? dy : dx;
+          const double w = (lane == 0 || lane == 3) ? dx : dy;
+          ct[0] = cf * u * w;
+        }
+        if (odd) {
+          M.vx -= f * Da.m * dx;
+          M.vy -= f * Da.m * dy;
+        } else {
+          M.vx += f * Db.m * dx;
+          M.vy += f * Db.m * dy;
+        }
+        Da.vx = __shfl_sync(FULLM, M.vx, 0);
+        Da.vy = __shfl_sync(FULLM, M.vy, 0);
+        Db.vx = __shfl_sync(FULLM, M.vx, 1);
+        Db.vy = __shfl_sync(FULLM, M.vy, 1);
+        // next crossing of each disk on its own lanes
+        int mdir;
+        const double mtc = crossing_time_i(B, M, odd ? bx : ax, odd ? by : ay, t, &mdir);
+        const double tca = __shfl_sync(FULLM, mtc, 0), tcb = __shfl_sync(FULLM, mtc, 1);
+        const int dira = __shfl_sync(FULLM, mdir, 0), dirb = __shfl_sync(FULLM, mdir, 1);
         __syncwarp();
         if (lane == 0) {
           S.d[a] = Da;
@@ -636,11 +672,8 @@ __global__ void __launch_bounds__(32 * WPB) k_process(const SysDev* __restrict__
         npred = 2;
         ncol = 1;
         if (lane == 0) {
-          int dir;
-          double tc = crossing_time_i(B, Da, ax, ay, t, &dir);
-          set_event(S, a, tc, dir, 0, 0, clk);
-          tc = crossing_time_i(B, Db, bx, by, t, &dir);
-          set_event(S, b, tc, dir, 0, 0, clk);
+          set_event(S, a, tca, dira, 0, 0, clk);
+          set_event(S, b, tcb, dirb, 0, 0, clk);
           set_event(S, N + a, t + p0.dt, p0.partner, p0.ca, p0.pcell, clk);
           set_event(S, N + b, t + p1.dt, p1.partner, p1.ca, p1.pcell, clk);
           A.drank[g] = 2;
@@ -650,6 +683,7 @@ __global__ void __launch_bounds__(32 * WPB) k_process(const SysDev* __restrict__
         }
       }
     } else {
+      free_fly_i(B, Da, t);
       int cx = ax, cy = ay;
       int wrapx = 0, wrapy = 0;
       switch (E.j) {
@@ -693,14 +727,9 @@ __global__ void __launch_bounds__(32 * WPB) k_process(const SysDev* __restrict__
         reattribute(S, A, a, g, base, dc, &nd);
       }
     }
+    if (ncol && lane < 4) cnt_addf(A, s, stripe, C_CT0 + lane, ct[0]);
     if (lane == 0) {
       for (int k = 0; k < MAXDIRTY; k++) A.dcell[(int64_t)n * MAXDIRTY + k] = k < nd ? dc[k] : -1;
-      if (ncol) {
-        cnt_addf(A, s, stripe, C_CT0, ct[0]);
-        cnt_addf(A, s, stripe, C_CT1, ct[1]);
-        cnt_addf(A, s, stripe, C_CT2, ct[2]);
-        cnt_addf(A, s, stripe, C_CT3, ct[3]);
-      }
       cnt_add(A, s, stripe, C_NCOL, ncol);
       cnt_add(A, s, stripe, C_NCROSS, ncross);
       cnt_add(A, s, stripe, C_NSTALE, nstale);
@@ -770,50 +799,57 @@ __global__ void __launch_bounds__(256) k_recompute(const SysDev* __restrict__ sy
 // free-flies every disk to it (takeAScreenshot, src/EDMD.c:4657-4661) and
 // reschedules it; then the eligibility bound of the next round
 __global__ void k_barrier(const SysDev* __restrict__ sys, RoundArgs A) {
-  const int s = blockIdx.x;
-  const SysDev& S = sys[s];
-  const int N = S.B.N;
   __shared__ int go;
-  if (threadIdx.x < 32) {
-    const int l = threadIdx.x;
-    const uint64_t* c = A.cnt + ((int64_t)s * NSTRIPE + l) * NCNT;
-    unsigned long long nc = c[C_NCOL];
-    uint64_t tl = c[C_TLAST];
-    for (int o = 16; o > 0; o >>= 1) {
-      nc += __shfl_xor_sync(FULLM, nc, o);
-      const uint64_t t2 = __shfl_xor_sync(FULLM, tl, o);
-      tl = t2 > tl ? t2 : tl;
-    }
-    if (l == 0) {
-      const SysState* R = S.st;
-      const bool ok = R->status == EDMD_OK;
-      uint64_t fz = A.freeze[s];
-      if (ok && fz == KINF && R->ncol + nc >= A.target[s]) {
-        fz = kmax(tl, A.tlast[s]) + 1;
-        A.freeze[s] = fz;
+  for (int s = blockIdx.x; s < A.nsys; s += gridDim.x) {
+    if (A.lim[s] == 0) continue;      // stopped for the rest of the call
+    const SysDev& S = sys[s];
+    const int N = S.B.N;
+    bool run = false;
+    if (threadIdx.x < 32) {
+      const int l = threadIdx.x;
+      const uint64_t* c = A.cnt + ((int64_t)s * NSTRIPE + l) * NCNT;
+      unsigned long long nc = c[C_NCOL];
+      uint64_t tl = c[C_TLAST];
+      for (int o = 16; o > 0; o >>= 1) {
+        nc += __shfl_xor_sync(FULLM, nc, o);
+        const uint64_t t2 = __shfl_xor_sync(FULLM, tl, o);
+        tl = t2 > tl ? t2 : tl;
       }
-      const uint64_t lim = A.tstop_key < fz ? A.tstop_key : fz;
-      const int selected = A.selflag[s];
-      go = (ok && !selected && time_key(S.ev[2 * N + SP_SCREEN].t) < lim) ? 1 : 0;
-      if (ok && (selected || go)) atomicAdd(A.active, 1);
-      A.selflag[s] = 0;
-    }
-  }
-  __syncthreads();
-  if (go) {
-    const double tbar = S.ev[2 * N + SP_SCREEN].t;
-    for (int i = threadIdx.x; i < N; i += blockDim.x) {
-      Disk p = S.d[i];
-      free_fly_i(S.B, p, tbar);
-      S.d[i] = p;
+      if (l == 0) {
+        const SysState* R = S.st;
+        const bool ok = R->status == EDMD_OK;
+        uint64_t fz = A.freeze[s];
+        if (ok && fz == KINF && R->ncol + nc >= A.target[s]) {
+          fz = kmax(tl, A.tlast[s]) + 1;
+          A.freeze[s] = fz;
+        }
+        const uint64_t lim = A.tstop_key < fz ? A.tstop_key : fz;
+        const int selected = A.selflag[s];
+        go = (ok && !selected && time_key(S.ev[2 * N + SP_SCREEN].t) < lim) ? 1 : 0;
+        run = ok && (selected || go);
+        if (run) atomicAdd(A.active, 1);
+        A.selflag[s] = 0;
+        // a system with nothing selected and no screenshot to pass has stopped
+        if (!run) A.lim[s] = 0;
+      }
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-      S.ev[2 * N + SP_SCREEN].t = tbar + S.dtime;
-      A.tlast[s] = kmax(A.tlast[s], time_key(tbar));
+    if (go) {
+      const double tbar = S.ev[2 * N + SP_SCREEN].t;
+      for (int i = threadIdx.x; i < N; i += blockDim.x) {
+        Disk p = S.d[i];
+        free_fly_i(S.B, p, tbar);
+        S.d[i] = p;
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        S.ev[2 * N + SP_SCREEN].t = tbar + S.dtime;
+        A.tlast[s] = kmax(A.tlast[s], time_key(tbar));
+      }
     }
+    if (threadIdx.x == 0 && A.lim[s] != 0) A.lim[s] = system_limit(S, A, s);
+    __syncthreads();
   }
-  if (threadIdx.x == 0) A.lim[s] = system_limit(S, A, s);
 }
 
 // fold the call's counters into each system's state; its time is the last
@@ -917,10 +953,11 @@ size_t select_smem(int r) {
 cudaError_t enqueue_round(edmd_ctx* ctx, const RoundBufs* R, const RoundArgs& A, int nsm) {
   cudaStream_t st = ctx->stream;
   k_round_begin<<<1, 1, 0, st>>>(A);
-  k_select<<<(unsigned)R->ntiles, TX * TY, select_smem(A.radius), st>>>(ctx->ds, A);
+  const unsigned tgrid = (unsigned)(R->ntiles < nsm * 8 ? R->ntiles : nsm * 8);
+  k_select<<<tgrid, TX * TY, select_smem(A.radius), st>>>(ctx->ds, A);
   k_process<<<nsm * 16, 32 * WPB, 0, st>>>(ctx->ds, A);
   k_recompute<<<nsm * 8, 256, 0, st>>>(ctx->ds, A);
-  k_barrier<<<ctx->nsys, 256, 0, st>>>(ctx->ds, A);
+  k_barrier<<<ctx->nsys < nsm * 8 ? ctx->nsys : nsm * 8, 256, 0, st>>>(ctx->ds, A);
   return cudaGetLastError();
 }
 
@@ -956,7 +993,7 @@ static int run_rounds(edmd_ctx* ctx, const std::vector<uint64_t>& tgt, double t_
   CK(cudaMemsetAsync(R->cmt, 0xff, TC * 8, st));
   CK(cudaMemsetAsync(R->cmi, 0x7f, TC * 4, st));
   RoundArgs A;
-  A.nsys = ctx->nsys; A.radius = radius; A.TN = TN; A.flags = flags;
+  A.nsys = ctx->nsys; A.radius = radius; A.TN = TN; A.flags = flags; A.ntiles = (int32_t)R->ntiles;
   {
     // the order-preserving integer image of t_stop (time_key on the host)
     uint64_t u;
@@ -1066,7 +1103,7 @@ extern "C" int edmd_advance_rounds(edmd_ctx* ctx, int64_t max_coll, double t_sto
     if (rc) return rc;
     if (!fresh) CK(cudaMemcpyAsync(R->drank, R->drank_bak, ctx->total_N, cudaMemcpyDeviceToDevice, ctx->stream));
     ctx->round_dirty = true;
-    r = r * 2 < RTILE ? r * 2 : RTILE;
+    r = r < 4 ? 4 : (r * 2 < RTILE ? r * 2 : RTILE);
   }
   CK(cudaEventRecord(ctx->e1, ctx->stream));
   CK(cudaEventSynchronize(ctx->e1));

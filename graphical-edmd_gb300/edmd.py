@@ -54,7 +54,7 @@ class Counters(C.Structure):
 # every symbol the public headers declare, in declaration order
 EXPORTS = [
     "edmd_create", "edmd_load_state", "edmd_advance", "edmd_advance_rounds", "edmd_sync",
-    "edmd_get_state",
+    "edmd_get_pcf", "edmd_get_state",
     "edmd_get_states", "edmd_get_counters", "edmd_get_all_counters", "edmd_get_virial",
     "edmd_get_thermo", "edmd_get_trace", "edmd_set_engine", "edmd_set_lane_threads",
     "edmd_get_engine", "edmd_set_device", "edmd_host_alloc", "edmd_host_free", "edmd_run_noalloc",
@@ -88,6 +88,8 @@ def load(path=LIB_PATH):
                                       C.c_int64, C.POINTER(C.c_float), C.POINTER(C.c_int64),
                                       C.POINTER(C.c_int64)]
     L.edmd_get_states.argtypes = [C.c_void_p] + [C.c_void_p] * 6
+    L.edmd_get_pcf.argtypes = [C.c_void_p, C.c_int32, C.c_double, C.c_double, C.c_void_p, C.c_int32,
+                               C.POINTER(C.c_int32)]
     L.edmd_get_all_counters.argtypes = [C.c_void_p, C.c_void_p]
     L.edmd_host_alloc.argtypes = [C.POINTER(C.c_void_p), C.c_int64]
     L.edmd_host_free.argtypes = [C.c_void_p]
@@ -208,6 +210,7 @@ class Engine:
         self.h = h
         self.n = n
         self.N = [s["desc"].N for s in systems]
+        self._desc = [s["desc"] for s in systems]
         self.trace_cap = trace_cap
         if rc != OK:
             msg = self.last_error()
@@ -247,6 +250,17 @@ class Engine:
 
     def sync(self):
         self._ck(self._L.edmd_sync(self.h))
+
+    def pcf(self, s=0, dr=0.1, max_r=None):
+        """(r, g) of calculate_pcf on the stored positions of system s."""
+        if max_r is None:
+            d = self._desc[s]
+            max_r = min(d.Lx, d.Ly) / 2
+        cap = int(max_r / dr) + 1
+        g = np.zeros(cap)
+        nb = C.c_int32()
+        self._ck(self._L.edmd_get_pcf(self.h, s, float(dr), float(max_r), _ptr(g), cap, C.byref(nb)))
+        return (np.arange(nb.value) + 0.5) * dr, g[: nb.value]
 
     def state(self, s=0):
         N = self.N[s]

@@ -150,8 +150,8 @@ int edmd_advance(edmd_ctx* ctx, int64_t max_coll, double t_stop, uint32_t flags,
  * unless *violations_out > 0: events processed before an earlier event of the
  * same region, detected exactly with per-cell time stamps (a larger radius
  * makes them rarer).  With EDMD_F_EXACT the call keeps a device copy of the
- * engine state and, after a violation, replays from it with a 2x wider window
- * (up to radius 12; a violation there returns EDMD_ERR_BUDGET), so a successful
+ * engine state and, after a violation, replays from it with a wider window
+ * (3 -> 4 -> 8 -> 12; a violation at 12 returns EDMD_ERR_BUDGET), so a successful
  * call is always the serial result and *violations_out counts the discarded
  * ones.
  * EDMD_F_TRACE records collisions in processing order.  After this call
@@ -163,6 +163,15 @@ int edmd_advance_rounds(edmd_ctx* ctx, int64_t max_coll, double t_stop, uint32_t
 /* Free-fly every disk of every system to its current time, the first step of
  * takeAScreenshot (src/EDMD.c:4657-4661). */
 int edmd_sync(edmd_ctx* ctx);
+
+/* Pair correlation g(r) of one system, calculate_pcf (src/pcf.c:16-75) as
+ * save_pcf calls it (src/EDMD.c:5637): bins of width dr up to max_r
+ * (<= half the shorter box side), counted exactly on the device over the cell
+ * lists and normalised by 2 pi r dr rho N at the bin centres, so the values
+ * are the reference's bit for bit.  Uses the stored positions (call edmd_sync
+ * first for positions at the current time).  *nbins_out = (int)(max_r/dr). */
+int edmd_get_pcf(edmd_ctx* ctx, int32_t sys, double dr, double max_r, double* g_out, int32_t cap,
+                 int32_t* nbins_out);
 
 /* Copy the state of one system to host arrays (any pointer may be NULL). */
 int edmd_get_state(edmd_ctx* ctx, int32_t sys, double* x, double* y, double* vx,
