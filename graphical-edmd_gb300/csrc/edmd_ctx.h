@@ -64,5 +64,22 @@ static inline int set_err(edmd_ctx* c, int code, const std::string& m) {
 
 static inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
+// Copies and sets ordered after everything queued on the context's stream.
+// The stream is non-blocking, so a plain cudaMemcpy on the legacy default
+// stream would not wait for the context's kernels.
+static inline cudaError_t sync_copy(edmd_ctx* c, void* dst, const void* src, size_t n, cudaMemcpyKind k) {
+  cudaError_t e = cudaMemcpyAsync(dst, src, n, k, c->stream);
+  return e != cudaSuccess ? e : cudaStreamSynchronize(c->stream);
+}
+static inline cudaError_t sync_copy2d(edmd_ctx* c, void* dst, size_t dp, const void* src, size_t sp, size_t w,
+                                      size_t h, cudaMemcpyKind k) {
+  cudaError_t e = cudaMemcpy2DAsync(dst, dp, src, sp, w, h, k, c->stream);
+  return e != cudaSuccess ? e : cudaStreamSynchronize(c->stream);
+}
+static inline cudaError_t sync_set(edmd_ctx* c, void* dst, int v, size_t n) {
+  cudaError_t e = cudaMemsetAsync(dst, v, n, c->stream);
+  return e != cudaSuccess ? e : cudaStreamSynchronize(c->stream);
+}
+
 template <class T>
 static inline cudaError_t dalloc(T** p, size_t n) { return cudaMalloc((void**)p, (n ? n : 1) * sizeof(T)); }

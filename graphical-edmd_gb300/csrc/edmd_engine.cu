@@ -101,7 +101,7 @@ __device__ void leaf_update(const SysDev& S, int leaf, int lane) {
 }
 
 // rebuild every level of the tree (after init or the growth stop)
-__device__ void tree_rebuild(const SysDev& S, int lane) {
+__device__ __noinline__ void tree_rebuild(const SysDev& S, int lane) {
   const int N = S.B.N;
   for (int l = lane; l < S.L; l += 32) {
     Node n = empty_node(l);
@@ -174,7 +174,7 @@ __device__ void unqueue(const SysDev& S, SysState& R, int e, int lane) {
 
 // the overflow bucket is redistributed when the calendar wraps
 // (addNextPaulEvent src/EDMD.c:2287-2300)
-__device__ void do_wrap(const SysDev& S, SysState& R, int lane) {
+__device__ __noinline__ void do_wrap(const SysDev& S, SysState& R, int lane) {
   const int N = S.B.N;
   int e = R.ovf;
   R.ovf = NIL;
@@ -342,7 +342,7 @@ __device__ __forceinline__ void seq_sums(const SysDev& S, int lane, int nval, do
 }
 
 // physicalQ (src/EDMD.c:5968-6013): px, py, E
-__device__ void physical_q(const SysDev& S, int lane, double* E, double* px, double* py) {
+__device__ __noinline__ void physical_q(const SysDev& S, int lane, double* E, double* px, double* py) {
   double o[3];
   seq_sums(S, lane, 3, o, [&](int i, double* v) {
     Disk p = S.d[i];
@@ -355,7 +355,7 @@ __device__ void physical_q(const SysDev& S, int lane, double* E, double* px, dou
 }
 
 // takeAThermo + saveThermo (src/EDMD.c:4679, 5232-5697) with Nthermo = 1
-__device__ void do_thermo(const SysDev& S, SysState& R, int lane) {
+__device__ __noinline__ void do_thermo(const SysDev& S, SysState& R, int lane) {
   const int N = S.B.N;
   double E, px, py;
   physical_q(S, lane, &E, &px, &py);
@@ -393,7 +393,7 @@ __device__ void do_thermo(const SysDev& S, SysState& R, int lane) {
 }
 
 // stopGrow (src/EDMD.c:4740-4800)
-__device__ void do_growstop(const SysDev& S, SysState& R, int lane, WarpSmem* sm,
+__device__ __noinline__ void do_growstop(const SysDev& S, SysState& R, int lane, WarpSmem* sm,
                             bool* ovl, int* oa, int* ob) {
   const int N = S.B.N;
   for (int i = lane; i < N; i += 32) {
@@ -539,10 +539,16 @@ __device__ void run_system(const SysDev& S, const RunArgs& A, int lane, WarpSmem
             lg->dvx = dvx; lg->dvy = dvy; lg->f = f;
           }
           if (A.flags & EDMD_F_LOG) R.nlog++;
-          di.vx += f * dj.m * dx;
-          di.vy += f * dj.m * dy;
-          dj.vx -= f * di.m * dx;
-          dj.vy -= f * di.m * dy;
+          // even lanes update i, odd lanes j: the two disks share instructions
+          {
+            const bool odd = lane & 1;
+            double vx = odd ? dj.vx : di.vx, vy = odd ? dj.vy : di.vy;
+            const double mo = odd ? di.m : dj.m;
+            if (odd) { vx -= f * mo * dx; vy -= f * mo * dy; }
+            else { vx += f * mo * dx; vy += f * mo * dy; }
+            di.vx = __shfl_sync(FULL, vx, 0); di.vy = __shfl_sync(FULL, vy, 0);
+            dj.vx = __shfl_sync(FULL, vx, 1); dj.vy = __shfl_sync(FULL, vy, 1);
+          }
         } else {       // growth rule src/EDMD.c:3479-3520
           double delta = 0.1 * 0;
           double res = 0.75 * 0 + 1;
@@ -562,8 +568,16 @@ __device__ void run_system(const SysDev& S, const RunArgs& A, int lane, WarpSmem
         unqueue(S, R, i, lane);
         unqueue(S, R, j, lane);
         int diri, dirj;
-        double tci = crossing_time_i(B, di, S.cx[i], S.cy[i], R.t, &diri);
-        double tcj = crossing_time_i(B, dj, S.cx[j], S.cy[j], R.t, &dirj);
+        double tci, tcj;
+        {
+          // next crossings of i (even lanes) and j (odd lanes) in shared instructions
+          const bool odd = lane & 1;
+          const int k = odd ? j : i;
+          int dir;
+          const double tc = crossing_time_i(B, odd ? dj : di, S.cx[k], S.cy[k], R.t, &dir);
+          tci = __shfl_sync(FULL, tc, 0); tcj = __shfl_sync(FULL, tc, 1);
+          diri = __shfl_sync(FULL, dir, 0); dirj = __shfl_sync(FULL, dir, 1);
+        }
         schedule(S, R, i, tci, diri, 0, 2ull, lane);
         schedule(S, R, j, tcj, dirj, 0, 2ull, lane);
         unqueue(S, R, N + j, lane);
@@ -650,7 +664,7 @@ __device__ void run_system(const SysDev& S, const RunArgs& A, int lane, WarpSmem
   __syncwarp();
 }
 
-__global__ void __launch_bounds__(32 * WARPS_PER_BLOCK)
+__global__ void __launch_bounds__(32 * WARPS_PER_BLOCK, 4)
 k_run(const SysDev* __restrict__ sys, RunArgs A) {
   __shared__ WarpSmem smem[WARPS_PER_BLOCK];
   const int lane = threadIdx.x & 31;
@@ -728,37 +742,106 @@ __global__ void k_init_events(const SysDev* __restrict__ sys) {
 }
 
 // link the initial overflow bucket in LIFO order and finish the scalar state;
-// one thread per system
-__global__ void k_init_finish(const SysDev* __restrict__ sys, int nsys) {
-  int s = blockIdx.x * blockDim.x + threadIdx.x;
+// one block per system.  The reference pushes the initial events in the order
+// thermo, [growth stop], screenshot, then crossing i and collision i for
+// i = 0..N-1 (eventListInit, src/EDMD.c:1935-2019); an overflow event's `on`
+// link is the previous overflow event in that order and `op` the next one, so
+// both follow from a running maximum over the push positions.
+__device__ __forceinline__ int init_slot(int p, int N, bool grow) {
+  const int nspec = grow ? 3 : 2;
+  if (p < nspec) {
+    if (p == 0) return 2 * N + SP_THERMO;
+    if (grow && p == 1) return 2 * N + SP_GROW;
+    return 2 * N + SP_SCREEN;
+  }
+  const int k = p - nspec;
+  return (k & 1) ? N + (k >> 1) : (k >> 1);
+}
+
+__global__ void __launch_bounds__(256) k_init_finish(const SysDev* __restrict__ sys, int nsys) {
+  const int s = blockIdx.x;
   if (s >= nsys) return;
   const SysDev& S = sys[s];
   const int N = S.B.N;
   const bool grow = S.st->grow != 0;
-  int head = NIL;
-  auto push = [&](int e) {
-    if (S.ev[e].st != ST_OVF) return;
-    S.on[e] = head; S.op[e] = NIL;
-    if (head != NIL) S.op[head] = e;
-    head = e;
-  };
-  push(2 * N + SP_THERMO);
-  if (grow) push(2 * N + SP_GROW);
-  push(2 * N + SP_SCREEN);
-  for (int i = 0; i < N; i++) { push(i); push(N + i); }
-  SysState& R = *S.st;
-  R.ovf = head;
-  R.C = (uint64_t)(grow ? 3 : 2) + 2ull * N;
-  R.npred = (uint64_t)N;
-  R.lastThermo = 0;
-  R.collT[0] = R.collT[1] = 0;
+  const int P = (grow ? 3 : 2) + 2 * N;
+  __shared__ int wmax[8];
+  __shared__ int carry;
+  if (threadIdx.x == 0) carry = -1;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int base = 0; base < P; base += blockDim.x) {
+    const int p = base + threadIdx.x;
+    const int e = p < P ? init_slot(p, N, grow) : -1;
+    const bool ovf = e >= 0 && S.ev[e].st == ST_OVF;
+    // exclusive running maximum of the overflow positions: the previous one
+    int v = ovf ? p : -1;
+    int incl = v;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int u = __shfl_up_sync(FULL, incl, o);
+      if (lane >= o && u > incl) incl = u;
+    }
+    if (lane == 31) wmax[w] = incl;
+    __syncthreads();
+    int before = carry;
+    for (int k = 0; k < w; k++) before = wmax[k] > before ? wmax[k] : before;
+    int excl = __shfl_up_sync(FULL, incl, 1);
+    if (lane == 0) excl = -1;
+    const int prev = excl > before ? excl : before;
+    if (ovf) {
+      // every overflow event but the last gets its `op` from its successor
+      const int pe = prev >= 0 ? init_slot(prev, N, grow) : NIL;
+      S.on[e] = pe;
+      if (pe != NIL) S.op[pe] = e;
+    }
+    __syncthreads();
+    if (threadIdx.x == blockDim.x - 1) {
+      const int last = incl > before ? incl : before;
+      carry = last;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    SysState& R = *S.st;
+    R.ovf = carry >= 0 ? init_slot(carry, N, grow) : NIL;
+    if (R.ovf != NIL) S.op[R.ovf] = NIL;
+    R.C = (uint64_t)(grow ? 3 : 2) + 2ull * N;
+    R.npred = (uint64_t)N;
+    R.lastThermo = 0;
+    R.collT[0] = R.collT[1] = 0;
+  }
 }
 
-// one warp per system
-__global__ void k_tree_build(const SysDev* __restrict__ sys, int nsys) {
-  int s = blockIdx.x;
+// one block per system: the leaves in parallel, then one level at a time
+// with a warp per parent node
+__global__ void __launch_bounds__(256) k_tree_build(const SysDev* __restrict__ sys, int nsys) {
+  const int s = blockIdx.x;
   if (s >= nsys) return;
-  tree_rebuild(sys[s], threadIdx.x & 31);
+  const SysDev& S = sys[s];
+  const int N = S.B.N;
+  for (int l = threadIdx.x; l < S.L; l += blockDim.x) {
+    Node n = empty_node(l);
+    if (l < N) {
+      Ev e0 = S.ev[l], e1 = S.ev[N + l];
+      if (e0.st == ST_QUEUED) n = ev_node(e0, l);
+      if (e1.st == ST_QUEUED) { Node m = ev_node(e1, l); if (node_less(m, n)) n = m; }
+    } else {
+      Ev e = S.ev[2 * N + (l - N)];
+      if (e.st == ST_QUEUED) n = ev_node(e, l);
+    }
+    S.tree[l] = n;
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int h = 1; h < S.nlev; h++) {
+    for (int par = w; par < S.lev_cnt[h]; par += nw) {
+      const int ch = (par << 5) + lane;
+      Node c = ch < S.lev_cnt[h - 1] ? S.tree[S.lev_off[h - 1] + ch] : empty_node(0x7fffffff);
+      warp_min(c);
+      if (lane == 0) S.tree[S.lev_off[h] + par] = c;
+    }
+    __syncthreads();
+  }
 }
 
 __global__ void k_sync(const SysDev* __restrict__ sys, int nsys) {
@@ -880,14 +963,14 @@ static int stage_all(edmd_ctx* ctx, const double* x, const double* y, const doub
   CK(cudaMemcpyAsync(ctx->head, hhead.data(), ctx->total_C * 4, cudaMemcpyHostToDevice, sm));
   dim3 g((ctx->maxN + 1 + 127) / 128, ctx->nsys);
   k_init_events<<<g, 128, 0, sm>>>(ctx->ds);
-  k_init_finish<<<(ctx->nsys + 127) / 128, 128, 0, sm>>>(ctx->ds, ctx->nsys);
+  k_init_finish<<<ctx->nsys, 256, 0, sm>>>(ctx->ds, ctx->nsys);
   if (ctx->engine == EDMD_ENGINE_LANE) CK(lane_build(ctx->ds, ctx->nsys, sm));
-  else k_tree_build<<<ctx->nsys, 32, 0, sm>>>(ctx->ds, ctx->nsys);
+  else k_tree_build<<<ctx->nsys, 256, 0, sm>>>(ctx->ds, ctx->nsys);
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(sm));   // host staging vectors go out of scope
   std::vector<int32_t> status(ctx->nsys);
   for (int s = 0; s < ctx->nsys; s++) status[s] = 0;
-  CK(cudaMemcpy2D(status.data(), 4, &ctx->st[0].status, sizeof(SysState), 4, ctx->nsys,
+  CK(sync_copy2d(ctx, status.data(), 4, &ctx->st[0].status, sizeof(SysState), 4, ctx->nsys,
                   cudaMemcpyDeviceToHost));
   for (int s = 0; s < ctx->nsys; s++)
     if (status[s] != EDMD_OK)
@@ -1030,7 +1113,7 @@ extern "C" int edmd_advance(edmd_ctx* ctx, int64_t max_coll, double t_stop, uint
   CK(cudaEventSynchronize(ctx->e1));
   if (elapsed_ms) CK(cudaEventElapsedTime(elapsed_ms, ctx->e0, ctx->e1));
   std::vector<int32_t> status(ctx->nsys);
-  CK(cudaMemcpy2D(status.data(), 4, &ctx->st[0].status, sizeof(SysState), 4, ctx->nsys,
+  CK(sync_copy2d(ctx, status.data(), 4, &ctx->st[0].status, sizeof(SysState), 4, ctx->nsys,
                   cudaMemcpyDeviceToHost));
   for (int s = 0; s < ctx->nsys; s++)
     if (status[s] != EDMD_OK) {
@@ -1056,9 +1139,9 @@ extern "C" int edmd_get_state(edmd_ctx* ctx, int32_t s, double* x, double* y, do
   int N = S.B.N;
   std::vector<Disk> hd(N);
   std::vector<int32_t> hcx(N), hcy(N);
-  CK(cudaMemcpy(hd.data(), S.d, N * sizeof(Disk), cudaMemcpyDeviceToHost));
-  CK(cudaMemcpy(hcx.data(), S.cx, N * 4, cudaMemcpyDeviceToHost));
-  CK(cudaMemcpy(hcy.data(), S.cy, N * 4, cudaMemcpyDeviceToHost));
+  CK(sync_copy(ctx, hd.data(), S.d, N * sizeof(Disk), cudaMemcpyDeviceToHost));
+  CK(sync_copy(ctx, hcx.data(), S.cx, N * 4, cudaMemcpyDeviceToHost));
+  CK(sync_copy(ctx, hcy.data(), S.cy, N * 4, cudaMemcpyDeviceToHost));
   for (int i = 0; i < N; i++) {
     if (x) x[i] = hd[i].x;
     if (y) y[i] = hd[i].y;
@@ -1089,7 +1172,7 @@ extern "C" int edmd_get_states(edmd_ctx* ctx, double* x, double* y, double* vx, 
 extern "C" int edmd_get_counters(edmd_ctx* ctx, int32_t s, edmd_counters* out) {
   if (!ctx || s < 0 || s >= ctx->nsys || !out) return EDMD_ERR_ARG;
   SysState R;
-  CK(cudaMemcpy(&R, ctx->hs[s].st, sizeof(R), cudaMemcpyDeviceToHost));
+  CK(sync_copy(ctx, &R, ctx->hs[s].st, sizeof(R), cudaMemcpyDeviceToHost));
   out->ncol = R.ncol; out->ncol_total = R.ncol_total; out->ncross = R.ncross;
   out->nstale = R.nstale; out->npair = R.npair; out->npred = R.npred; out->nevents = R.nevents;
   out->t = R.t; out->growing = R.grow; out->stop_reason = R.stop_reason;
@@ -1099,7 +1182,7 @@ extern "C" int edmd_get_counters(edmd_ctx* ctx, int32_t s, edmd_counters* out) {
 extern "C" int edmd_get_all_counters(edmd_ctx* ctx, edmd_counters* out) {
   if (!ctx || !out) return EDMD_ERR_ARG;
   std::vector<SysState> R(ctx->nsys);
-  CK(cudaMemcpy(R.data(), ctx->st, ctx->nsys * sizeof(SysState), cudaMemcpyDeviceToHost));
+  CK(sync_copy(ctx, R.data(), ctx->st, ctx->nsys * sizeof(SysState), cudaMemcpyDeviceToHost));
   for (int s = 0; s < ctx->nsys; s++) {
     edmd_counters& o = out[s];
     o.ncol = R[s].ncol; o.ncol_total = R[s].ncol_total; o.ncross = R[s].ncross;
@@ -1112,8 +1195,8 @@ extern "C" int edmd_get_all_counters(edmd_ctx* ctx, edmd_counters* out) {
 extern "C" int edmd_get_virial(edmd_ctx* ctx, int32_t s, double out[4], int32_t reset) {
   if (!ctx || s < 0 || s >= ctx->nsys || !out) return EDMD_ERR_ARG;
   SysState* p = ctx->hs[s].st;
-  CK(cudaMemcpy(out, p->collT, 4 * sizeof(double), cudaMemcpyDeviceToHost));
-  if (reset) CK(cudaMemset(p->collT, 0, 4 * sizeof(double)));
+  CK(sync_copy(ctx, out, p->collT, 4 * sizeof(double), cudaMemcpyDeviceToHost));
+  if (reset) CK(sync_set(ctx, p->collT, 0, 4 * sizeof(double)));
   return EDMD_OK;
 }
 
@@ -1121,11 +1204,11 @@ extern "C" int edmd_get_thermo(edmd_ctx* ctx, int32_t s, double* rows, int32_t c
   if (!ctx || s < 0 || s >= ctx->nsys || !n) return EDMD_ERR_ARG;
   const SysDev& S = ctx->hs[s];
   int32_t nr = 0;
-  CK(cudaMemcpy(&nr, &S.st->nrows, 4, cudaMemcpyDeviceToHost));
+  CK(sync_copy(ctx, &nr, &S.st->nrows, 4, cudaMemcpyDeviceToHost));
   *n = nr;
   int k = nr < cap ? nr : cap;
   if (k > S.rows_cap) k = S.rows_cap;
-  if (rows && k > 0) CK(cudaMemcpy(rows, S.rows, (size_t)k * 9 * 8, cudaMemcpyDeviceToHost));
+  if (rows && k > 0) CK(sync_copy(ctx, rows, S.rows, (size_t)k * 9 * 8, cudaMemcpyDeviceToHost));
   return nr > S.rows_cap ? EDMD_ERR_CAPACITY : EDMD_OK;
 }
 
@@ -1133,11 +1216,11 @@ extern "C" int edmd_get_trace(edmd_ctx* ctx, int32_t s, edmd_collision* out, int
   if (!ctx || s < 0 || s >= ctx->nsys || !n) return EDMD_ERR_ARG;
   const SysDev& S = ctx->hs[s];
   uint64_t nt = 0;
-  CK(cudaMemcpy(&nt, &S.st->ntrace, 8, cudaMemcpyDeviceToHost));
+  CK(sync_copy(ctx, &nt, &S.st->ntrace, 8, cudaMemcpyDeviceToHost));
   *n = (int64_t)nt;
   int64_t k = (int64_t)nt < cap ? (int64_t)nt : cap;
   if (k > S.trace_cap) k = S.trace_cap;
-  if (out && k > 0) CK(cudaMemcpy(out, S.trace, k * sizeof(edmd_collision), cudaMemcpyDeviceToHost));
+  if (out && k > 0) CK(sync_copy(ctx, out, S.trace, k * sizeof(edmd_collision), cudaMemcpyDeviceToHost));
   return (int64_t)nt > S.trace_cap ? EDMD_ERR_CAPACITY : EDMD_OK;
 }
 
@@ -1327,8 +1410,8 @@ extern "C" int edmd_run_noalloc(const edmd_system_desc* desc, double* x, double*
   k_noalloc_put<<<1, 1, 0, st>>>(S, dsys);
   k_noalloc_stage<<<1, 32, 0, st>>>(dsys, x, y, vx, vy, rad, m, D.first_screen, D.first_thermo);
   k_init_events<<<dim3((unsigned)((N + 1 + 127) / 128), 1), 128, 0, st>>>(dsys);
-  k_init_finish<<<1, 32, 0, st>>>(dsys, 1);
-  k_tree_build<<<1, 32, 0, st>>>(dsys, 1);
+  k_init_finish<<<1, 256, 0, st>>>(dsys, 1);
+  k_tree_build<<<1, 256, 0, st>>>(dsys, 1);
   if (cudaMemsetAsync(work, 0, sizeof(int32_t), st) != cudaSuccess)
     return noalloc_fail(EDMD_ERR_CUDA, "edmd_run_noalloc: memset failed");
   k_run<<<1, 32 * WARPS_PER_BLOCK, 0, st>>>(dsys, A);

@@ -556,7 +556,7 @@ __device__ __forceinline__ Disk shfl_disk(const Disk& v, int src) {
 // doTheCrossing (2501).  The scalar work is repeated by every lane (same
 // values), stores are made by lane 0, predictions are shared by the warp.
 // Per-system counters go to one of NSTRIPE stripes to spread the atomics.
-__global__ void __launch_bounds__(32 * WPB) k_process(const SysDev* __restrict__ sys, RoundArgs A) {
+__global__ void __launch_bounds__(32 * WPB, 2) k_process(const SysDev* __restrict__ sys, RoundArgs A) {
   __shared__ WarpScratch scr[WPB];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   WarpScratch* W = &scr[wid];
@@ -932,12 +932,12 @@ int round_init(edmd_ctx* ctx) {
   CK(dalloc(&R->tlast, ctx->nsys)); CK(dalloc(&R->viol, 1));
   CK(dalloc(&R->cnt, (int64_t)ctx->nsys * NSTRIPE * NCNT));
   CK(dalloc(&R->tsys, R->ntiles)); CK(dalloc(&R->tx0, R->ntiles)); CK(dalloc(&R->ty0, R->ntiles));
-  CK(cudaMemcpy(R->doff, ctx->disk_off.data(), ctx->nsys * 8, cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(R->coff, ctx->cell_off.data(), ctx->nsys * 8, cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(R->tsys, tsys.data(), R->ntiles * 4, cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(R->tx0, tx0.data(), R->ntiles * 4, cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(R->ty0, ty0.data(), R->ntiles * 4, cudaMemcpyHostToDevice));
-  CK(cudaMemset(R->selflag, 0, ctx->nsys * 4));
+  CK(sync_copy(ctx, R->doff, ctx->disk_off.data(), ctx->nsys * 8, cudaMemcpyHostToDevice));
+  CK(sync_copy(ctx, R->coff, ctx->cell_off.data(), ctx->nsys * 8, cudaMemcpyHostToDevice));
+  CK(sync_copy(ctx, R->tsys, tsys.data(), R->ntiles * 4, cudaMemcpyHostToDevice));
+  CK(sync_copy(ctx, R->tx0, tx0.data(), R->ntiles * 4, cudaMemcpyHostToDevice));
+  CK(sync_copy(ctx, R->ty0, ty0.data(), R->ntiles * 4, cudaMemcpyHostToDevice));
+  CK(sync_set(ctx, R->selflag, 0, ctx->nsys * 4));
   k_round_setup<<<dim3(64, ctx->nsys), 256, 0, ctx->stream>>>(R->doff, ctx->ds, R->dsys);
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(ctx->stream));
@@ -1071,7 +1071,7 @@ extern "C" int edmd_advance_rounds(edmd_ctx* ctx, int64_t max_coll, double t_sto
   int rc = round_init(ctx);
   if (rc) return rc;
   std::vector<SysState> st(ctx->nsys);
-  CK(cudaMemcpy(st.data(), ctx->st, ctx->nsys * sizeof(SysState), cudaMemcpyDeviceToHost));
+  CK(sync_copy(ctx, st.data(), ctx->st, ctx->nsys * sizeof(SysState), cudaMemcpyDeviceToHost));
   std::vector<uint64_t> tgt(ctx->nsys);
   for (int s = 0; s < ctx->nsys; s++) {
     if (st[s].grow) return set_err(ctx, EDMD_ERR_ARG, "the round engine runs the constant-radius phase only");
@@ -1111,7 +1111,7 @@ extern "C" int edmd_advance_rounds(edmd_ctx* ctx, int64_t max_coll, double t_sto
   if (rounds_out) *rounds_out = rounds;
   if (violations_out) *violations_out = viol_total;
   std::vector<int32_t> status(ctx->nsys);
-  CK(cudaMemcpy2D(status.data(), 4, &ctx->st[0].status, sizeof(SysState), 4, ctx->nsys,
+  CK(sync_copy2d(ctx, status.data(), 4, &ctx->st[0].status, sizeof(SysState), 4, ctx->nsys,
                   cudaMemcpyDeviceToHost));
   for (int s = 0; s < ctx->nsys; s++)
     if (status[s] != EDMD_OK) {

@@ -72,9 +72,11 @@ __device__ __forceinline__ double row_at(const double* T, const double* tl, int 
   return v;
 }
 
-// Gram matrix G = T'^T T' of the tangent vectors flown to tq (G zeroed before)
+// per-block partial Gram matrices of the tangent vectors flown to tq; summed
+// over the blocks in a fixed order by k_gram_sum, so the result is
+// reproducible run to run
 __global__ void k_gram(const double* __restrict__ T, const double* __restrict__ tl, int N, int K,
-                       double tq, double* __restrict__ G) {
+                       double tq, double* __restrict__ Gp) {
   __shared__ double rows[32][33];
   const int k = threadIdx.x & 31, l = threadIdx.x >> 5;   // 32 x 32 threads
   double acc = 0;
@@ -86,7 +88,15 @@ __global__ void k_gram(const double* __restrict__ T, const double* __restrict__ 
       for (int r = 0; r < 32; r++) acc += rows[r][k] * rows[r][l];
     __syncthreads();
   }
-  if (k < K && l < K) atomicAdd(&G[k * K + l], acc);
+  if (k < K && l < K) Gp[(size_t)blockIdx.x * K * K + k * K + l] = acc;
+}
+
+__global__ void k_gram_sum(const double* __restrict__ Gp, int nblocks, int K, double* __restrict__ G) {
+  const int e = threadIdx.x;
+  if (e >= K * K) return;
+  double s = 0;
+  for (int b = 0; b < nblocks; b++) s += Gp[(size_t)b * K * K + e];
+  G[e] = s;
 }
 
 // Cholesky G = R^T R (R upper), logs of diag(R) accumulated, Rinv = R^-1
@@ -238,12 +248,12 @@ extern "C" int edmd_clear_log(edmd_ctx* ctx) {
 extern "C" int edmd_get_log(edmd_ctx* ctx, int32_t s, edmd_log_entry* out, int64_t cap, int64_t* n) {
   if (!ctx || s < 0 || s >= ctx->nsys || !n) return EDMD_ERR_ARG;
   uint64_t nl = 0;
-  CK(cudaMemcpy(&nl, &ctx->st[s].nlog, 8, cudaMemcpyDeviceToHost));
+  CK(sync_copy(ctx, &nl, &ctx->st[s].nlog, 8, cudaMemcpyDeviceToHost));
   *n = (int64_t)nl;
   int64_t k = (int64_t)nl < cap ? (int64_t)nl : cap;
   if (k > ctx->log_cap) k = ctx->log_cap;
   if (out && k > 0)
-    CK(cudaMemcpy(out, ctx->hs[s].log, k * sizeof(edmd_log_entry), cudaMemcpyDeviceToHost));
+    CK(sync_copy(ctx, out, ctx->hs[s].log, k * sizeof(edmd_log_entry), cudaMemcpyDeviceToHost));
   return (int64_t)nl > ctx->log_cap ? EDMD_ERR_CAPACITY : EDMD_OK;
 }
 
@@ -308,7 +318,7 @@ extern "C" int edmd_checkpoint_restore(edmd_ctx* ctx, int32_t slot) {
 // ==================================================================== tangent driver
 
 static int current_time(edmd_ctx* ctx, int s, double* t) {
-  CK(cudaMemcpy(t, &ctx->st[s].t, 8, cudaMemcpyDeviceToHost));
+  CK(sync_copy(ctx, t, &ctx->st[s].t, 8, cudaMemcpyDeviceToHost));
   return EDMD_OK;
 }
 
@@ -319,25 +329,27 @@ static int advance_logged(edmd_ctx* ctx, int s, int64_t ncoll, int64_t* nlog) {
   rc = edmd_advance(ctx, ncoll, INFINITY, EDMD_F_LOG | EDMD_F_COUNT_NORMAL, (int64_t)1 << 60, nullptr);
   if (rc) return rc;
   uint64_t nl = 0;
-  CK(cudaMemcpy(&nl, &ctx->st[s].nlog, 8, cudaMemcpyDeviceToHost));
+  CK(sync_copy(ctx, &nl, &ctx->st[s].nlog, 8, cudaMemcpyDeviceToHost));
   if ((int64_t)nl > ctx->log_cap) return set_err(ctx, EDMD_ERR_CAPACITY, "collision log overflow");
   *nlog = (int64_t)nl;
   return EDMD_OK;
 }
 
-static int cholqr(edmd_ctx* ctx, double* T, double* tl, int N, int K, double tq, double* G,
+constexpr int GRAM_BLOCKS = 1024;
+
+static int cholqr(edmd_ctx* ctx, double* T, double* tl, int N, int K, double tq, double* G, double* Gp,
                   double* Rinv, double* logdiag, int* fail, bool accumulate) {
   for (int pass = 0; pass < 2; pass++) {    // CholQR2: the second pass restores orthogonality
-    CK(cudaMemsetAsync(G, 0, K * K * sizeof(double), ctx->stream));
     int blocks = (4 * N + 31) / 32;
-    if (blocks > 1024) blocks = 1024;
-    k_gram<<<blocks, 1024, 0, ctx->stream>>>(T, tl, N, K, tq, G);
+    if (blocks > GRAM_BLOCKS) blocks = GRAM_BLOCKS;
+    k_gram<<<blocks, 1024, 0, ctx->stream>>>(T, tl, N, K, tq, Gp);
+    k_gram_sum<<<1, 1024, 0, ctx->stream>>>(Gp, blocks, K, G);
     k_chol<<<1, 1, 0, ctx->stream>>>(G, K, Rinv, logdiag, accumulate ? 1 : 0, fail);
     k_apply_rinv<<<(N + 127) / 128, 128, 0, ctx->stream>>>(T, tl, N, K, tq, Rinv);
     CK(cudaGetLastError());
   }
   int h = 0;
-  CK(cudaMemcpy(&h, fail, 4, cudaMemcpyDeviceToHost));
+  CK(sync_copy(ctx, &h, fail, 4, cudaMemcpyDeviceToHost));
   if (h) return set_err(ctx, EDMD_ERR_ARG, "tangent vectors became linearly dependent");
   return EDMD_OK;
 }
@@ -351,15 +363,16 @@ extern "C" int edmd_tangent_run(edmd_ctx* ctx, int32_t s, int32_t K, int64_t n_c
   int64_t chunk = qr_every > 0 ? qr_every : (n_coll > 0 ? n_coll : 1);
   int rc = edmd_set_log_capacity(ctx, chunk + 16);
   if (rc) return rc;
-  double *T = nullptr, *tl = nullptr, *G = nullptr, *Rinv = nullptr, *logdiag = nullptr;
+  double *T = nullptr, *tl = nullptr, *G = nullptr, *Gp = nullptr, *Rinv = nullptr, *logdiag = nullptr;
   int* fail = nullptr;
   CK(dalloc(&T, (size_t)4 * N * K));
   CK(dalloc(&tl, N));
   CK(dalloc(&G, K * K));
+  CK(dalloc(&Gp, (size_t)GRAM_BLOCKS * K * K));
   CK(dalloc(&Rinv, K * K));
   CK(dalloc(&logdiag, K));
   CK(dalloc(&fail, 1));
-  struct Free { void* p[6]; ~Free() { for (void* q : p) if (q) cudaFree(q); } } guard{{T, tl, G, Rinv, logdiag, fail}};
+  struct Free { void* p[7]; ~Free() { for (void* q : p) if (q) cudaFree(q); } } guard{{T, tl, G, Gp, Rinv, logdiag, fail}};
   double t0;
   if ((rc = current_time(ctx, s, &t0))) return rc;
   // initial vectors: the caller's ([K][N][4]) or seeded random orthonormal ones
@@ -376,7 +389,7 @@ extern "C" int edmd_tangent_run(edmd_ctx* ctx, int32_t s, int32_t K, int64_t n_c
   k_fill<<<(N + 255) / 256, 256, 0, ctx->stream>>>(tl, N, t0);
   CK(cudaMemsetAsync(logdiag, 0, K * sizeof(double), ctx->stream));
   CK(cudaMemsetAsync(fail, 0, 4, ctx->stream));
-  if (!tangent_io && (rc = cholqr(ctx, T, tl, N, K, t0, G, Rinv, logdiag, fail, false))) return rc;
+  if (!tangent_io && (rc = cholqr(ctx, T, tl, N, K, t0, G, Gp, Rinv, logdiag, fail, false))) return rc;
   int64_t done = 0;
   double t = t0;
   while (done < n_coll) {
@@ -386,20 +399,20 @@ extern "C" int edmd_tangent_run(edmd_ctx* ctx, int32_t s, int32_t K, int64_t n_c
     k_tangent_apply<<<1, 32, 0, ctx->stream>>>((const edmd_log_entry*)ctx->hs[s].log, nl, ctx->hs[s].d, T, tl, K);
     CK(cudaGetLastError());
     if ((rc = current_time(ctx, s, &t))) return rc;
-    if (qr_every > 0 && (rc = cholqr(ctx, T, tl, N, K, t, G, Rinv, logdiag, fail, true))) return rc;
+    if (qr_every > 0 && (rc = cholqr(ctx, T, tl, N, K, t, G, Gp, Rinv, logdiag, fail, true))) return rc;
     done += want;
     if (nl < want) break;     // the run ended early (tmax or t_stop)
   }
   if (lyap_out) {
     std::vector<double> ld(K);
-    CK(cudaMemcpy(ld.data(), logdiag, K * 8, cudaMemcpyDeviceToHost));
+    CK(sync_copy(ctx, ld.data(), logdiag, K * 8, cudaMemcpyDeviceToHost));
     for (int k = 0; k < K; k++) lyap_out[k] = (t > t0) ? ld[k] / (t - t0) : 0.0;
   }
   if (tangent_io) {
     // tangents at the final time (virtual flight of every row)
-    CK(cudaMemcpy(h.data(), T, h.size() * 8, cudaMemcpyDeviceToHost));
+    CK(sync_copy(ctx, h.data(), T, h.size() * 8, cudaMemcpyDeviceToHost));
     std::vector<double> htl(N);
-    CK(cudaMemcpy(htl.data(), tl, N * 8, cudaMemcpyDeviceToHost));
+    CK(sync_copy(ctx, htl.data(), tl, N * 8, cudaMemcpyDeviceToHost));
     for (int k = 0; k < K; k++)
       for (int i = 0; i < N; i++)
         for (int c = 0; c < 4; c++) {
@@ -488,9 +501,10 @@ extern "C" int edmd_msd_gradient(edmd_ctx* ctx, int32_t s, int64_t n_coll, int64
   CK(cudaStreamSynchronize(ctx->stream));
   // leave the engine at the end of the run
   if ((rc = edmd_checkpoint_restore(ctx, (int32_t)nseg))) return rc;
+  // u = r(t) - r(0) also depends on the initial positions directly
   for (int i = 0; i < N; i++) {
-    if (g_x) g_x[i] = hA[4 * i + 0];
-    if (g_y) g_y[i] = hA[4 * i + 1];
+    if (g_x) g_x[i] = hA[4 * i + 0] - 2.0 * (ux[i] - mx) / N;
+    if (g_y) g_y[i] = hA[4 * i + 1] - 2.0 * (uy[i] - my) / N;
     if (g_vx) g_vx[i] = hA[4 * i + 2];
     if (g_vy) g_vy[i] = hA[4 * i + 3];
   }

@@ -2,9 +2,12 @@
 
 Finite differences come from the CPU oracle (the reference's serial algorithm),
 run from initial states displaced by +-eps (eps = 1e-7) along a direction, to
-a fixed observation time t_obs placed between the 1000th and 1001st collision
-of the unperturbed run; each perturbed run must process the same collisions,
-otherwise the comparison is meaningless.  Tolerances: 1e-5 relative (tangent,
+a fixed observation time t_obs placed between the n-th and (n+1)-th collision
+of the unperturbed run (n = 1000 for the adjoint, 300 for the full 4N tangent
+direction); each perturbed run must process the same collisions, otherwise the
+comparison is meaningless.  The MSD displacement is measured from the
+(perturbed) initial positions, so its gradient with respect to r(0) includes
+the direct term.  Tolerances: 1e-5 relative (tangent,
 full 4N vector) and 1e-6 relative (adjoint gradient components, the north-star
 figure), both far above the O(eps^2) truncation and the 1e-9 roundoff of the
 differences.
@@ -18,8 +21,7 @@ EPS = 1e-7
 NCOLL = 1000
 
 
-@pytest.fixture(scope="module")
-def setup(edmd, oracle):
+def make_setup(edmd, oracle, ncoll):
     """A generic N = 1024, phi = 0.60 state (the Hex start run 3000 collisions)."""
     s = edmd.hex_start(1024, 0.60, 11)
     o = oracle.Oracle(arrays={k: s[k] for k in ("x", "y", "vx", "vy", "rad", "m", "type")},
@@ -29,14 +31,26 @@ def setup(edmd, oracle):
     st = o.state()
     init = {k: st[k].copy() for k in ("x", "y", "vx", "vy", "rad", "m")}
     init["type"] = st["type"].copy()
-    # unperturbed reference run: observation time between collisions 1000 and 1001
+    # unperturbed reference run: observation time between collisions ncoll and ncoll+1
     ob = oracle.Oracle(arrays=init, Lx=s["Lx"], Ly=s["Ly"])
-    tr, n = ob.run(NCOLL + 1)
-    T, t_next = tr["t"][NCOLL - 1], tr["t"][NCOLL]
+    tr, n = ob.run(ncoll + 1)
+    T, t_next = tr["t"][ncoll - 1], tr["t"][ncoll]
     assert t_next > T
     t_obs = T + 0.25 * (t_next - T)
-    return dict(init=init, Lx=s["Lx"], Ly=s["Ly"], N=s["N"], T=T, t_obs=t_obs,
-                pairs=np.sort(np.stack([tr["i"][:NCOLL], tr["j"][:NCOLL]], 1), axis=1))
+    return dict(init=init, Lx=s["Lx"], Ly=s["Ly"], N=s["N"], T=T, t_obs=t_obs, ncoll=ncoll,
+                pairs=np.sort(np.stack([tr["i"][:ncoll], tr["j"][:ncoll]], 1), axis=1))
+
+
+@pytest.fixture(scope="module")
+def setup(edmd, oracle):
+    return make_setup(edmd, oracle, NCOLL)
+
+
+@pytest.fixture(scope="module")
+def setup_short(edmd, oracle):
+    """300 collisions: short enough that +-eps along a random 4N direction keeps
+    the collision sequence of this chaotic system."""
+    return make_setup(edmd, oracle, 300)
 
 
 def engine(edmd, setup):
@@ -50,7 +64,7 @@ def oracle_state_at(oracle, setup, arrays):
     o = oracle.Oracle(arrays=arrays, Lx=setup["Lx"], Ly=setup["Ly"])
     tr, n = o.run(10 ** 9, t_stop=setup["t_obs"])
     pairs = np.sort(np.stack([tr["i"], tr["j"]], 1), axis=1)
-    same = n == NCOLL and np.array_equal(pairs, setup["pairs"])
+    same = n == setup["ncoll"] and np.array_equal(pairs, setup["pairs"])
     st = o.state()
     t = setup["t_obs"]
     out = np.stack([st["x"] + st["vx"] * (t - st["tl"]), st["y"] + st["vy"] * (t - st["tl"]),
@@ -72,26 +86,33 @@ def min_image(setup, dpos):
     return out
 
 
-def msd_of(setup, pos):
-    u = min_image(setup, pos - np.stack([setup["init"]["x"], setup["init"]["y"]], 1))
+def msd_of(setup, pos, init=None):
+    init = setup["init"] if init is None else init
+    u = min_image(setup, pos - np.stack([init["x"], init["y"]], 1))
     u -= u.mean(0)
     return (u * u).sum() / setup["N"]
 
 
-def test_tangent_matches_central_differences(edmd, oracle, setup):
+def test_tangent_matches_central_differences(edmd, oracle, setup_short):
+    """A random direction in all four components of 64 disks."""
+    setup = setup_short
     N = setup["N"]
-    d = np.random.default_rng(3).normal(size=(N, 4))
+    for seed in (3, 4, 5):
+        rng = np.random.default_rng(seed)
+        d = np.zeros((N, 4))
+        d[rng.choice(N, 64, replace=False)] = rng.normal(size=(64, 4))
+        sp, okp = oracle_state_at(oracle, setup, perturbed(setup, d, +1))
+        sm, okm = oracle_state_at(oracle, setup, perturbed(setup, d, -1))
+        if okp and okm:
+            break
+    assert okp and okm, "the perturbation changed the collision sequence"
     eng = engine(edmd, setup)
-    vec, _ = eng.tangent(1, NCOLL, vectors=d[None])
+    vec, _ = eng.tangent(1, setup["ncoll"], vectors=d[None])
     T = eng.counters(0)["t"]
     assert T == setup["T"]                        # the GPU run is the oracle's run
     tan = vec[0].copy()
     tan[:, 0] += tan[:, 2] * (setup["t_obs"] - T)
     tan[:, 1] += tan[:, 3] * (setup["t_obs"] - T)
-    sp, okp = oracle_state_at(oracle, setup, perturbed(setup, d, +1))
-    sm, okm = oracle_state_at(oracle, setup, perturbed(setup, d, -1))
-    if not (okp and okm):
-        pytest.skip("the perturbation changed the collision sequence")
     diff = sp - sm
     diff[:, :2] = min_image(setup, diff[:, :2])
     fd = diff / (2 * EPS)
@@ -109,17 +130,19 @@ def test_adjoint_gradient_matches_central_differences(edmd, oracle, setup):
     rng = np.random.default_rng(7)
     checked = 0
     for k in rng.choice(N, 6, replace=False):
-        for c, key in ((2, "vx"), (3, "vy")):
+        for c, key in ((0, "x"), (1, "y"), (2, "vx"), (3, "vy")):
             d = np.zeros((N, 4))
             d[k, c] = 1.0
-            sp, okp = oracle_state_at(oracle, setup, perturbed(setup, d, +1))
-            sm, okm = oracle_state_at(oracle, setup, perturbed(setup, d, -1))
+            ap, am = perturbed(setup, d, +1), perturbed(setup, d, -1)
+            sp, okp = oracle_state_at(oracle, setup, ap)
+            sm, okm = oracle_state_at(oracle, setup, am)
             if not (okp and okm):
                 continue
-            fd = (msd_of(setup, sp[:, :2]) - msd_of(setup, sm[:, :2])) / (2 * EPS)
+            # the displacement is measured from the perturbed initial positions
+            fd = (msd_of(setup, sp[:, :2], ap) - msd_of(setup, sm[:, :2], am)) / (2 * EPS)
             assert abs(g[key][k] - fd) <= 1e-6 * abs(fd) + 1e-9, (k, key, g[key][k], fd)
             checked += 1
-    assert checked >= 6
+    assert checked >= 12
 
 
 def test_duality_with_oracle_displacement(edmd, oracle, setup):
@@ -134,7 +157,8 @@ def test_duality_with_oracle_displacement(edmd, oracle, setup):
     base, _ = oracle_state_at(oracle, setup, setup["init"])
     u = min_image(setup, base[:, :2] - np.stack([setup["init"]["x"], setup["init"]["y"]], 1))
     u -= u.mean(0)
-    dmsd_tangent = (2.0 / N) * (u * tan[:, :2]).sum()
+    # d u = d r(t_obs) - d r(0)
+    dmsd_tangent = (2.0 / N) * (u * (tan[:, :2] - d[:, :2])).sum()
     eng2 = engine(edmd, setup)
     _, g = eng2.msd_gradient(NCOLL, ckpt_every=200, t_obs=setup["t_obs"])
     adj = np.stack([g["x"], g["y"], g["vx"], g["vy"]], 1)
