@@ -14,6 +14,9 @@ Workloads (``--workload``):
   single_large  one Hex system of 10^6 monodisperse disks at phi = 0.72,
                 10^5 equilibration collisions (untimed), one step = 2*10^7
                 collisions in the round-parallel engine (exact mode).
+  single_4m     the same at 4*10^6 disks and phi = 0.78 (one step = 10^8
+                collisions), the scale of the precision configuration, run in
+                full FP64.
   plain_small   one 1980-disk Hex system at phi = 0.70, one step = 10^5
                 collisions, serial-exact warp engine (the plain GPU path).
 Data are synthetic (the reference has no dataset).  The batched state
@@ -50,11 +53,13 @@ XS, Q = 0.5, 0.7142857
 METRICS = {
     "batched": "collisions/s on 1 GB300 (batched systems)",
     "single_large": "collisions/s on 1 GB300 (single 10^6-disk system, round-parallel)",
+    "single_4m": "collisions/s on 1 GB300 (single 4*10^6-disk system, phi 0.78, round-parallel)",
     "plain_small": "collisions/s on 1 GB300 (plain single system)",
 }
-DEFAULT_COLL = {"batched": 100000, "single_large": 20000000, "plain_small": 100000}
-DEFAULT_ENGINE = {"batched": "warp", "single_large": "round", "plain_small": "warp"}
+DEFAULT_COLL = {"batched": 100000, "single_large": 20000000, "single_4m": 100000000, "plain_small": 100000}
+DEFAULT_ENGINE = {"batched": "warp", "single_large": "round", "single_4m": "round", "plain_small": "warp"}
 LARGE_N, LARGE_PHI, LARGE_EQUIL = 1000000, 0.72, 100000
+SINGLE = {"single_large": (LARGE_N, LARGE_PHI), "single_4m": (4000000, 0.78)}
 
 
 def _load_edmd():
@@ -130,13 +135,13 @@ class CpuPool:
 def cpu_sample_params(workload, ncores, seed):
     if workload == "plain_small":
         return [(2000, 0.70, seed + k, "hex") for k in range(ncores)]
-    if workload == "single_large":
-        return [(LARGE_N, LARGE_PHI, seed, "hex")]          # one system: one thread
+    if workload in SINGLE:
+        return [(SINGLE[workload][0], SINGLE[workload][1], seed, "hex")]   # one system: one thread
     return [(n, p, s, "grow") for n, p, s in batched_params(ncores, seed, 0)]
 
 
 def cpu_sample_coll(workload, a):
-    return a.cpu_coll if workload != "single_large" else 2000000
+    return a.cpu_coll if workload not in SINGLE else 2000000
 
 
 # ------------------------------------------------------------------ clocks
@@ -222,7 +227,7 @@ def run_reference(a, rank, world, dist):
     if rank != 0:
         return 0
     ncores = os.cpu_count() or 1
-    coll = a.ref_coll if a.workload != "single_large" else 2000000
+    coll = a.ref_coll if a.workload not in SINGLE else 2000000
     params = cpu_sample_params(a.workload, ncores, a.seed)
     pool = CpuPool(params, coll)
     for _ in range(a.warmup):
@@ -256,8 +261,8 @@ def build_systems(edmd, workload, nsys, seed, rank):
             s["desc"] = edmd.default_desc(s["N"], s["Lx"], s["Ly"], 0.0, 1e30)
             systems.append(s)
         return systems
-    if workload == "single_large":
-        s = edmd.hex_start(LARGE_N, LARGE_PHI, seed + rank)
+    if workload in SINGLE:
+        s = edmd.hex_start(SINGLE[workload][0], SINGLE[workload][1], seed + rank)
         s["desc"] = edmd.default_desc(s["N"], s["Lx"], s["Ly"], 0.0, 1e30)
         return [s]
     for N, phi, sd in batched_params(nsys, seed, rank):
@@ -278,7 +283,7 @@ class Stepper:
         if self.engine == "round":
             _, ms, rounds, _ = self.eng.advance_rounds(max_coll=self.coll, radius=self.radius,
                                                        flags=self.edmd.F_EXACT)
-            self.launches += 5 * rounds + 4
+            self.launches += 6 * rounds + 4
             return ms
         _, ms = self.eng.advance(max_coll=self.coll, flags=self.edmd.F_COUNT_NORMAL)
         self.launches += 1
@@ -296,7 +301,7 @@ def measure(edmd, a, workload, engine, coll, steps, warmup, rank, world, dist, d
         eng.advance(flags=edmd.F_STOP_AT_GROW)
         c = eng.all_counters()
         assert not c["growing"].any(), "growth did not finish"
-    elif workload == "single_large":
+    elif workload in SINGLE:
         eng.advance_rounds(max_coll=LARGE_EQUIL, radius=a.radius, flags=edmd.F_EXACT)
     st = Stepper(edmd, eng, engine, coll, a.radius)
     for _ in range(warmup):
@@ -416,6 +421,8 @@ def run_ours(a, rank, world, dist):
                    % r["systems"],
         "single_large": "single Hex system, N=%d, phi=%.2f, %d equilibration collisions" %
                         (r["TN"], LARGE_PHI, LARGE_EQUIL),
+        "single_4m": "single Hex system, N=%d, phi=%.2f, %d equilibration collisions, full FP64" %
+                     (r["TN"], SINGLE["single_4m"][1], LARGE_EQUIL),
         "plain_small": "single Hex system, N=1980, phi=0.70",
     }[workload]
     line = {
@@ -446,7 +453,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="batched", choices=["batched", "single_large", "plain_small"])
+    ap.add_argument("--workload", default="batched", choices=["batched", "single_large", "single_4m", "plain_small"])
     ap.add_argument("--engine", default="auto", choices=["auto", "warp", "lane", "round"])
     ap.add_argument("--radius", type=int, default=4)
     ap.add_argument("--nsys", type=int, default=None)

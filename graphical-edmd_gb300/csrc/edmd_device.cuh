@@ -76,6 +76,7 @@ struct SysState {
   int32_t ovf, grow, nrows, stop_reason;
   int32_t status, err_a, err_b, pad;
   uint64_t nlog;               // collision-geometry records written (EDMD_F_LOG)
+  uint64_t nscreen;            // candidate pairs rejected by the FP32 screen (round engine)
 };
 
 struct SysDev {

@@ -1175,6 +1175,7 @@ extern "C" int edmd_get_counters(edmd_ctx* ctx, int32_t s, edmd_counters* out) {
   CK(sync_copy(ctx, &R, ctx->hs[s].st, sizeof(R), cudaMemcpyDeviceToHost));
   out->ncol = R.ncol; out->ncol_total = R.ncol_total; out->ncross = R.ncross;
   out->nstale = R.nstale; out->npair = R.npair; out->npred = R.npred; out->nevents = R.nevents;
+  out->nscreen = R.nscreen;
   out->t = R.t; out->growing = R.grow; out->stop_reason = R.stop_reason;
   return EDMD_OK;
 }
@@ -1187,6 +1188,7 @@ extern "C" int edmd_get_all_counters(edmd_ctx* ctx, edmd_counters* out) {
     edmd_counters& o = out[s];
     o.ncol = R[s].ncol; o.ncol_total = R[s].ncol_total; o.ncross = R[s].ncross;
     o.nstale = R[s].nstale; o.npair = R[s].npair; o.npred = R[s].npred; o.nevents = R[s].nevents;
+    o.nscreen = R[s].nscreen;
     o.t = R[s].t; o.growing = R[s].grow; o.stop_reason = R[s].stop_reason;
   }
   return EDMD_OK;

@@ -1,6 +1,6 @@
 // edmd_round.cu -- round-parallel event engine: the causally independent events
-// of one large system, or of a whole batch, processed at once, one thread per
-// event.
+// of one large system, or of a whole batch, processed at once, one warp or one
+// thread per event.
 //
 // Every disk has one pending event: the earlier of its crossing event
 // (crossingEventNormal, src/EDMD.c:2405) and its collision event
@@ -20,8 +20,8 @@
 //      next screenshot, t_stop and its collision budget) that is the window
 //      minimum at both of its footprint cells: no earlier pending event lies
 //      within r cells, and selected events are more than r cells apart;
-//   3. the selected events are processed, one thread each, with the
-//      arithmetic of the serial engines;
+//   3. the selected events are processed, one warp each or (rounds of many
+//      events) one thread each, with the arithmetic of the serial engines;
 //   4. the cell minima around them are recomputed, and systems with nothing
 //      left before their screenshot pass it (every disk free-flown to it).
 // Events created inside a round can still precede a processed event (a chain
@@ -32,11 +32,14 @@
 // and an event that writes a cell with a later lw or lr, or reads one with a
 // later lw, is counted as a causality violation.  With none, every disk sees
 // the serial sequence of events, so the state is the reference's; only the
-// summation order of the virial and the order of the trace differ.  Mutual
-// equal-time predictions (a->b and b->a) resolve to the smaller owner; both
-// orders give bit-identical velocities since the collision rule is odd in
-// (dx, dy) and in (dvx, dvy).
+// summation order of the virial and the order of the trace differ.  Equal
+// keys are ordered like the serial queue orders them: mutual equal-time
+// predictions inherited from a serial engine carry the rank of their queue
+// keys (k_rank) in the event id, and new ones rank after them; two valid
+// mutual events give bit-identical velocities in either order since the
+// collision rule is odd in (dx, dy) and in (dvx, dvy).
 #include <cstdio>
+#include <cstdint>
 #include <cstring>
 #include "edmd_ctx.h"
 
@@ -53,7 +56,7 @@ constexpr int MAXC = 8;               // candidates buffered per cell list per l
 constexpr int WPB = 8;                // warps per block of the processing kernel
 constexpr int NSTRIPE = 32;           // copies of each system's counters
 // counters of the round engine, per system and stripe (u64 slots)
-enum { C_CT0, C_CT1, C_CT2, C_CT3, C_NCOL, C_NCROSS, C_NSTALE, C_NPAIR, C_NPRED, C_NEV, C_TLAST, NCNT };
+enum { C_CT0, C_CT1, C_CT2, C_CT3, C_NCOL, C_NCROSS, C_NSTALE, C_NPAIR, C_NPRED, C_NEV, C_NSCREEN, C_TLAST, NCNT };
 
 struct RoundArgs {
   int32_t nsys;
@@ -80,6 +83,10 @@ struct RoundArgs {
   uint64_t* freeze;              // per-system key bound once the budget is met
   uint64_t* tlast;               // per-system largest screenshot key passed
   uint64_t* cnt;                 // [nsys][NSTRIPE][NCNT] counters of this call
+  int32_t thr_min;               // rounds of at least this many events run one thread per event
+  float4* shp;                   // FP32 shadow of each disk: cell-relative x, y and vx, vy
+  float* sht;                    // ... and its time relative to the system's epoch
+  double* epoch;                 // per-system time origin of the shadows (the call's start)
   const int32_t* tsys;           // tiles: system, first cell x, first cell y
   const int32_t* tx0;
   const int32_t* ty0;
@@ -144,6 +151,30 @@ __device__ __forceinline__ int attribution(const SysDev& S, int i, uint64_t* key
   return slot;
 }
 
+// FP32 shadow of a disk record for the candidate screen: position relative to
+// its cell's corner, velocity, time relative to the epoch.  Values outside the
+// range the screen's error bound covers are stored as NaN, which no screen test
+// passes, so those pairs always take the FP64 path.
+// coordinate relative to the corner of cell c; a disk on the box edge of its
+// cell can sit at the other side of the periodic box by rounding
+__device__ __forceinline__ float cell_rel(double x, int c, double cs, double L) {
+  double r = x - c * cs;
+  if (r > cs + 1.0) r -= L;
+  else if (r < -1.0) r += L;
+  return (float)r;
+}
+
+__device__ __forceinline__ void shadow_write(const RoundArgs& A, int64_t g, const Box& B, const Disk& D, int cx,
+                                             int cy, double epoch) {
+  const float nan = __int_as_float(0x7fffffff);
+  float xr = cell_rel(D.x, cx, B.cxs, B.Lx), yr = cell_rel(D.y, cy, B.cys, B.Ly);
+  float vx = (float)D.vx, vy = (float)D.vy, tl = (float)(D.tl - epoch);
+  const bool ok = xr > -1.0f && xr < (float)B.cxs + 1.0f && yr > -1.0f && yr < (float)B.cys + 1.0f &&
+                  fabsf(vx) < 8.0f && fabsf(vy) < 8.0f && fabsf(tl) < 16.0f;
+  A.shp[g] = ok ? make_float4(xr, yr, vx, vy) : make_float4(nan, nan, nan, nan);
+  A.sht[g] = ok ? tl : nan;
+}
+
 // id of disk g's next event: a collision carries its serial tie rank
 __device__ __forceinline__ int32_t event_id(const RoundArgs& A, int64_t g, int slot, int N) {
   return (slot >= N ? ((int32_t)A.drank[g] << 24) : 0) | (int32_t)g;
@@ -198,6 +229,9 @@ __global__ void k_prep(const SysDev* __restrict__ sys, RoundArgs A) {
       e.b = (uint32_t)(adjacent(B, own, pc) ? pc : own);
     }
   }
+  const double ep = S.st->t;
+  if (i == 0) A.epoch[s] = ep;
+  shadow_write(A, g, B, S.d[i], S.cx[i], S.cy[i], ep);
   uint64_t key;
   int c1, c2;
   const int slot = attribution(S, i, &key, &c1, &c2);
@@ -551,22 +585,24 @@ __device__ __forceinline__ Disk shfl_disk(const Disk& v, int src) {
   return r;
 }
 
-// process the selected events, one warp each: doTheCollisionNormal
+// outcome of one processed event (lane 0 holds everything but `ct`, which
+// lane q < 4 holds for virial term q)
+struct EvResult {
+  int32_t dc[MAXDIRTY];              // cells whose minimum can have changed
+  int nd;
+  unsigned long long npair, npred, ncol, ncross, nstale, nscreen;
+  double ct;
+  uint64_t key;
+  bool bad, ovl;
+  int a, ob;
+};
+
+// one selected event g of system s processed by one warp: doTheCollisionNormal
 // (src/EDMD.c:3542, elastic rule 3802-3827), its stale branch (3553-3556) or
 // doTheCrossing (2501).  The scalar work is repeated by every lane (same
 // values), stores are made by lane 0, predictions are shared by the warp.
-// Per-system counters go to one of NSTRIPE stripes to spread the atomics.
-__global__ void __launch_bounds__(32 * WPB, 2) k_process(const SysDev* __restrict__ sys, RoundArgs A) {
-  __shared__ WarpScratch scr[WPB];
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  WarpScratch* W = &scr[wid];
-  const int nsafe = *A.nsafe;
-  const int gw = blockIdx.x * WPB + wid, nw = gridDim.x * WPB;
-  const int stripe = gw & (NSTRIPE - 1);
-  for (int n = gw; n < nsafe; n += nw) {
-    const int64_t g = A.safe[n];
-    const int s = A.dsys[g];
-    const SysDev& S = sys[s];
+__device__ void process_event_warp(const SysDev& S, const RoundArgs& A, int s, int64_t g, WarpScratch* W,
+                                   int lane, EvResult& res) {
     const Box& B = S.B;
     const int N = B.N;
     const int64_t base = A.coff[s], dbase = A.doff[s];
@@ -593,7 +629,10 @@ __global__ void __launch_bounds__(32 * WPB, 2) k_process(const SysDev* __restric
       if (E.ca != Db.coll) {
         free_fly_i(B, Da, t);
         __syncwarp();
-        if (lane == 0) S.d[a] = Da;
+        if (lane == 0) {
+          S.d[a] = Da;
+          shadow_write(A, g, B, Da, ax, ay, A.epoch[s]);
+        }
         bad |= lane == 0 && stamp_write(A, base, ca, clk);
         bad |= stamp_read_warp(B, A, base, ca, clk, lane, 0);
         __syncwarp();
@@ -655,6 +694,8 @@ __global__ void __launch_bounds__(32 * WPB, 2) k_process(const SysDev* __restric
         if (lane == 0) {
           S.d[a] = Da;
           S.d[b] = Db;
+          shadow_write(A, g, B, Da, ax, ay, A.epoch[s]);
+          shadow_write(A, gb, B, Db, bx, by, A.epoch[s]);
           if ((A.flags & EDMD_F_TRACE) && S.trace) {
             const unsigned long long k = atomicAdd((unsigned long long*)&S.st->ntrace, 1ull);
             if ((int64_t)k < S.trace_cap) {
@@ -708,6 +749,7 @@ __global__ void __launch_bounds__(32 * WPB, 2) k_process(const SysDev* __restric
         S.prv[a] = NIL;
         Da.nxt = h;
         S.d[a] = Da;
+        shadow_write(A, g, B, Da, cx, cy, A.epoch[s]);
         S.head[c] = a;
         if (h != NIL) S.prv[h] = a;
       }
@@ -727,22 +769,360 @@ __global__ void __launch_bounds__(32 * WPB, 2) k_process(const SysDev* __restric
         reattribute(S, A, a, g, base, dc, &nd);
       }
     }
-    if (ncol && lane < 4) cnt_addf(A, s, stripe, C_CT0 + lane, ct[0]);
-    if (lane == 0) {
-      for (int k = 0; k < MAXDIRTY; k++) A.dcell[(int64_t)n * MAXDIRTY + k] = k < nd ? dc[k] : -1;
+    for (int k = 0; k < MAXDIRTY; k++) res.dc[k] = dc[k];
+    res.nd = nd;
+    res.npair = npair; res.npred = npred; res.ncol = ncol; res.ncross = ncross; res.nstale = nstale;
+    res.nscreen = 0;
+    res.ct = ct[0];
+    res.key = key;
+    res.bad = bad; res.ovl = ovl;
+    res.a = a; res.ob = ob;
+}
+
+// ---- one thread per event (rounds with many selected events): the lanes of
+// a warp run 32 different events, so their scalar FP64 work shares issue slots
+
+// collisionEventNormal (src/EDMD.c:2829-2905) by one thread: the 3x3 cells dy
+// outer, dx inner, each list in order, first strict minimum below NEVER
+__device__ Pred predict_thread(const SysDev& S, const RoundArgs& A, int s, int a, const Disk& Da, int X, int Y,
+                               double t, unsigned long long* npair, unsigned long long* nscreen, bool* ovl,
+                               int* ob) {
+  const Box& B = S.B;
+  Pred r;
+  r.dt = NEVER;
+  r.partner = 0;
+  r.ca = 0;
+  r.pcell = cell_of(B, X, Y);
+  uint64_t kb = time_key(NEVER);
+  bool found = false;
+  // FP32 screen: the owner in its cell's frame at time t.  The bound on the
+  // FP32 error of b = dr.dv (|positions| < cell + 1, |v| < 8, |times - epoch|
+  // < 16: at most ~7e-4) is below SCREEN_B, so b32 > SCREEN_B proves the FP64
+  // b > 0: collisionTimeNormal returns "never" there before any other test.
+  constexpr float SCREEN_B = 2e-3f;
+  const double dt0 = t - A.epoch[s];
+  // with at least 5 cells a side the neighbour cell offset gives the minimum image
+  const bool screen = (A.flags & EDMD_F_SCREEN) && dt0 > -16.0 && dt0 < 16.0 && B.Nxc >= 5 && B.Nyc >= 5;
+  const float t32 = (float)dt0;
+  const float axr = cell_rel(Da.x, X, B.cxs, B.Lx), ayr = cell_rel(Da.y, Y, B.cys, B.Ly);
+  const bool own_ok = axr > -1.0f && axr < (float)B.cxs + 1.0f && ayr > -1.0f && ayr < (float)B.cys + 1.0f &&
+                      fabs(Da.vx) < 8.0 && fabs(Da.vy) < 8.0;
+  const float avx = (float)Da.vx, avy = (float)Da.vy;
+  const float cxs = (float)B.cxs, cys = (float)B.cys;
+  const int64_t dbase = A.doff[s];
+  int guard = 0;                     // a list is never longer than N
+  for (int q = 0; q < 9; q++) {
+    const int ox = q % 3 - 1, oy = q / 3 - 1;
+    const int cell = pbc_cy(B, Y + oy) * B.Nxc + pbc_cx(B, X + ox);
+    int p = S.head[cell];
+    while (p != NIL && guard++ < 9 * B.N) {
+      if (p == a) {
+        p = S.d[p].nxt;
+        continue;
+      }
+      (*npair)++;
+      if (screen && own_ok) {
+        const float4 P = A.shp[dbase + p];
+        const float lat = t32 - A.sht[dbase + p];
+        const float dx = (P.x + lat * P.z) + ox * cxs - axr;
+        const float dy = (P.y + lat * P.w) + oy * cys - ayr;
+        const float b = dx * (P.z - avx) + dy * (P.w - avy);
+        if (b > SCREEN_B) {          // separating: FP64 would return NEVER
+          (*nscreen)++;
+          p = S.d[p].nxt;
+          continue;
+        }
+      }
+      const Disk P = S.d[p];
+      bool ov = false;
+      const double d = coll_time_normal_i(B, Da, P, t, &ov);
+      if (ov) { *ovl = true; *ob = p; }
+      const uint64_t kd = time_key(d);
+      if (kd < kb) { r.dt = d; kb = kd; r.partner = p; r.ca = P.coll; r.pcell = cell; found = true; }
+      p = P.nxt;
+    }
+  }
+  if (!found) r.ca = S.d[0].coll;
+  return r;
+}
+
+// read stamps of the 3x3 cells around local cell c by one thread
+__device__ bool stamp_read_thread(const Box& B, const RoundArgs& A, int64_t base, int c, uint64_t clk) {
+  const int x = c % B.Nxc, y = c / B.Nxc;
+  bool bad = false;
+  for (int q = 0; q < 9; q++) {
+    const int64_t gc = base + pbc_cy(B, y + q / 3 - 1) * B.Nxc + pbc_cx(B, x + q % 3 - 1);
+    if (A.lw[gc] > clk) bad = true;
+    if (A.lr[gc] < clk) atomicMax((unsigned long long*)&A.lr[gc], (unsigned long long)clk);
+  }
+  return bad;
+}
+
+// one selected event by one thread: the handlers of process_event_warp with
+// the same arithmetic; all four virial terms end in r.ct4
+__device__ void process_event_thread(const SysDev& S, const RoundArgs& A, int s, int64_t g, EvResult& res,
+                                     double* ct4) {
+  const Box& B = S.B;
+  const int N = B.N;
+  const int64_t base = A.coff[s], dbase = A.doff[s];
+  const int a = (int)(g - dbase);
+  uint64_t key;
+  const int slot = next_slot(S, a, &key);
+  const Ev E = S.ev[slot];
+  const double t = E.t;
+  const uint64_t clk = E.tie;
+  int nd = 0;
+  res.dc[nd++] = (int32_t)(base + A.fc[2 * g]);
+  if (A.fc[2 * g + 1] != A.fc[2 * g]) res.dc[nd++] = (int32_t)(base + A.fc[2 * g + 1]);
+  Disk Da = S.d[a];
+  const int ax = S.cx[a], ay = S.cy[a];
+  const int ca = cell_of(B, ax, ay);
+  res.npair = res.npred = res.ncol = res.ncross = res.nstale = res.nscreen = 0;
+  ct4[0] = ct4[1] = ct4[2] = ct4[3] = 0;
+  res.ovl = res.bad = false;
+  res.ob = -1;
+  if (slot >= N) {
+    const int b = E.j;
+    Disk Db = S.d[b];
+    free_fly_i(B, Da, t);
+    if (E.ca != Db.coll) {
+      S.d[a] = Da;
+      shadow_write(A, g, B, Da, ax, ay, A.epoch[s]);
+      res.bad |= stamp_write(A, base, ca, clk);
+      res.bad |= stamp_read_thread(B, A, base, ca, clk);
+      const Pred p0 = predict_thread(S, A, s, a, Da, ax, ay, t, &res.npair, &res.nscreen, &res.ovl, &res.ob);
+      res.npred = 1;
+      res.nstale = 1;
+      set_event(S, N + a, t + p0.dt, p0.partner, p0.ca, p0.pcell, clk);
+      A.drank[g] = 2;
+      uint64_t k2; int c1, c2;
+      const int sl = attribution(S, a, &k2, &c1, &c2);
+      A.dkey[g] = k2; A.dpk[g] = event_id(A, g, sl, N); A.fc[2 * g] = c1; A.fc[2 * g + 1] = c2;
+      res.dc[nd++] = (int32_t)(base + c1);
+      if (c2 != c1) res.dc[nd++] = (int32_t)(base + c2);
+    } else {
+      const int64_t gb = dbase + b;
+      res.dc[nd++] = (int32_t)(base + A.fc[2 * gb]);
+      if (A.fc[2 * gb + 1] != A.fc[2 * gb]) res.dc[nd++] = (int32_t)(base + A.fc[2 * gb + 1]);
+      const int bx = S.cx[b], by = S.cy[b];
+      const int cb = cell_of(B, bx, by);
+      free_fly_i(B, Db, t);
+      Da.coll++;
+      Db.coll++;
+      double dx = Db.x - Da.x, dy = Db.y - Da.y;
+      const double dvx = Db.vx - Da.vx, dvy = Db.vy - Da.vy;
+      const double msum = Da.m + Db.m;
+      const double invMass = msum == 2.0 ? 0.5 : 1 / msum;
+      pbc_i(B, dx, dy);
+      const double collKernel = invMass * (1 + S.res) * (dx * dvx + dy * dvy);
+      const double distSquared = 4 * Da.rad * Db.rad;
+      const double f = distSquared == 4.0 ? collKernel * 0.25 : collKernel / distSquared;
+      const double cf = Da.m * Db.m * f;
+      ct4[0] = cf * dx * dx;
+      ct4[1] = cf * dy * dy;
+      ct4[2] = cf * dx * dy;
+      ct4[3] = cf * dy * dx;
+      Da.vx += f * Db.m * dx;
+      Da.vy += f * Db.m * dy;
+      Db.vx -= f * Da.m * dx;
+      Db.vy -= f * Da.m * dy;
+      S.d[a] = Da;
+      S.d[b] = Db;
+      shadow_write(A, g, B, Da, ax, ay, A.epoch[s]);
+      shadow_write(A, gb, B, Db, bx, by, A.epoch[s]);
+      if ((A.flags & EDMD_F_TRACE) && S.trace) {
+        const unsigned long long k = atomicAdd((unsigned long long*)&S.st->ntrace, 1ull);
+        if ((int64_t)k < S.trace_cap) {
+          edmd_collision* tr = (edmd_collision*)S.trace + k;
+          tr->i = a; tr->j = b; tr->cell_i = ca; tr->cell_j = cb; tr->t = t;
+        }
+      }
+      res.bad |= stamp_write(A, base, ca, clk) | stamp_write(A, base, cb, clk);
+      res.bad |= stamp_read_thread(B, A, base, ca, clk);
+      res.bad |= stamp_read_thread(B, A, base, cb, clk);
+      int dir;
+      double tc = crossing_time_i(B, Da, ax, ay, t, &dir);
+      set_event(S, a, tc, dir, 0, 0, clk);
+      tc = crossing_time_i(B, Db, bx, by, t, &dir);
+      set_event(S, b, tc, dir, 0, 0, clk);
+      const Pred p0 = predict_thread(S, A, s, a, Da, ax, ay, t, &res.npair, &res.nscreen, &res.ovl, &res.ob);
+      const Pred p1 = predict_thread(S, A, s, b, Db, bx, by, t, &res.npair, &res.nscreen, &res.ovl, &res.ob);
+      res.npred = 2;
+      res.ncol = 1;
+      set_event(S, N + a, t + p0.dt, p0.partner, p0.ca, p0.pcell, clk);
+      set_event(S, N + b, t + p1.dt, p1.partner, p1.ca, p1.pcell, clk);
+      A.drank[g] = 2;
+      A.drank[gb] = 2;
+      uint64_t k2; int c1, c2;
+      int sl = attribution(S, a, &k2, &c1, &c2);
+      A.dkey[g] = k2; A.dpk[g] = event_id(A, g, sl, N); A.fc[2 * g] = c1; A.fc[2 * g + 1] = c2;
+      res.dc[nd++] = (int32_t)(base + c1);
+      if (c2 != c1) res.dc[nd++] = (int32_t)(base + c2);
+      sl = attribution(S, b, &k2, &c1, &c2);
+      A.dkey[gb] = k2; A.dpk[gb] = event_id(A, gb, sl, N); A.fc[2 * gb] = c1; A.fc[2 * gb + 1] = c2;
+      res.dc[nd++] = (int32_t)(base + c1);
+      if (c2 != c1) res.dc[nd++] = (int32_t)(base + c2);
+    }
+  } else {
+    free_fly_i(B, Da, t);
+    int cx = ax, cy = ay;
+    const int pv = S.prv[a], nx = Da.nxt;
+    if (pv == NIL) S.head[ca] = nx;
+    else S.d[pv].nxt = nx;
+    if (nx != NIL) S.prv[nx] = pv;
+    switch (E.j) {
+      case 1: if (cx - 1 == -1) { cx = B.Nxc - 1; S.crossX[a] -= 1; } else cx -= 1; break;
+      case 2: if (cx + 1 == B.Nxc) { cx = 0; S.crossX[a] += 1; } else cx += 1; break;
+      case 3: if (cy - 1 == -1) { cy = B.Nyc - 1; S.crossY[a] -= 1; } else cy -= 1; break;
+      default: if (cy + 1 == B.Nyc) { cy = 0; S.crossY[a] += 1; } else cy += 1; break;
+    }
+    const int c = cell_of(B, cx, cy);
+    const int h = S.head[c];
+    S.cx[a] = cx;
+    S.cy[a] = cy;
+    S.prv[a] = NIL;
+    Da.nxt = h;
+    S.d[a] = Da;
+    shadow_write(A, g, B, Da, cx, cy, A.epoch[s]);
+    S.head[c] = a;
+    if (h != NIL) S.prv[h] = a;
+    res.bad |= stamp_write(A, base, ca, clk) | stamp_write(A, base, c, clk);
+    res.bad |= stamp_read_thread(B, A, base, c, clk);
+    int dir;
+    const double tc = crossing_time_i(B, Da, cx, cy, t, &dir);
+    set_event(S, a, tc, dir, 0, 0, clk);
+    const Pred p0 = predict_thread(S, A, s, a, Da, cx, cy, t, &res.npair, &res.nscreen, &res.ovl, &res.ob);
+    res.npred = 1;
+    res.ncross = 1;
+    set_event(S, N + a, t + p0.dt, p0.partner, p0.ca, p0.pcell, clk);
+    A.drank[g] = 2;
+    uint64_t k2; int c1, c2;
+    const int sl = attribution(S, a, &k2, &c1, &c2);
+    A.dkey[g] = k2; A.dpk[g] = event_id(A, g, sl, N); A.fc[2 * g] = c1; A.fc[2 * g + 1] = c2;
+    res.dc[nd++] = (int32_t)(base + c1);
+    if (c2 != c1) res.dc[nd++] = (int32_t)(base + c2);
+  }
+  res.nd = nd;
+  res.key = key;
+  res.a = a;
+}
+
+// sums and maximum over the lanes of mask m (all 32 lanes call these)
+__device__ __forceinline__ double group_sum(unsigned m, double v) {
+  double acc = 0;
+  for (int l = 0; l < 32; l++) {
+    const double x = __shfl_sync(FULLM, v, l);
+    if ((m >> l) & 1u) acc += x;
+  }
+  return acc;
+}
+__device__ __forceinline__ unsigned long long group_sum_u(unsigned m, unsigned long long v) {
+  unsigned long long acc = 0;
+  for (int l = 0; l < 32; l++) {
+    const unsigned long long x = __shfl_sync(FULLM, v, l);
+    if ((m >> l) & 1u) acc += x;
+  }
+  return acc;
+}
+__device__ __forceinline__ uint64_t group_max(unsigned m, uint64_t v) {
+  uint64_t acc = 0;
+  for (int l = 0; l < 32; l++) {
+    const uint64_t x = __shfl_sync(FULLM, v, l);
+    if (((m >> l) & 1u) && x > acc) acc = x;
+  }
+  return acc;
+}
+
+// the selected events of a round, one thread each (rounds of at least
+// A.thr_min events; k_process takes the others); per-system counters are
+// summed over the lanes of a warp that share the system before one atomic
+__global__ void __launch_bounds__(128) k_process_thread(const SysDev* __restrict__ sys, RoundArgs A) {
+  const int nsafe = *A.nsafe;
+  if (nsafe < A.thr_min) return;
+  const int lane = threadIdx.x & 31;
+  const int wstart = (blockIdx.x * blockDim.x + threadIdx.x) - lane;
+  const int wstride = gridDim.x * blockDim.x;
+  const int stripe = (wstart >> 5) & (NSTRIPE - 1);
+  for (int w = wstart; w < nsafe; w += wstride) {
+    const int n = w + lane;
+    const bool valid = n < nsafe;
+    int s = -1;
+    EvResult r;
+    double ct4[4] = {0, 0, 0, 0};
+    r.nd = 0; r.npair = r.npred = r.ncol = r.ncross = r.nstale = r.nscreen = 0; r.key = 0;
+    r.bad = r.ovl = false; r.a = r.ob = -1;
+    if (valid) {
+      const int64_t g = A.safe[n];
+      s = A.dsys[g];
+      process_event_thread(sys[s], A, s, g, r, ct4);
+      for (int k = 0; k < MAXDIRTY; k++) A.dcell[(int64_t)n * MAXDIRTY + k] = k < r.nd ? r.dc[k] : -1;
+      if (r.bad) atomicAdd(A.violations, 1ull);
+      if (r.ovl) {
+        SysState* R = sys[s].st;
+        R->err_a = r.a;
+        R->err_b = r.ob;
+        R->status = EDMD_ERR_OVERLAP;
+      }
+    }
+    const unsigned m = __match_any_sync(FULLM, s);
+    const bool leader = lane == __ffs(m) - 1;
+    const double c0 = group_sum(m, ct4[0]), c1 = group_sum(m, ct4[1]);
+    const double c2 = group_sum(m, ct4[2]), c3 = group_sum(m, ct4[3]);
+    const unsigned long long ncol = group_sum_u(m, r.ncol), ncross = group_sum_u(m, r.ncross);
+    const unsigned long long nstale = group_sum_u(m, r.nstale), npair = group_sum_u(m, r.npair);
+    const unsigned long long npred = group_sum_u(m, r.npred), nscr = group_sum_u(m, r.nscreen);
+    const uint64_t kmx = group_max(m, r.key);
+    if (leader && s >= 0) {
+      if (ncol) {
+        cnt_addf(A, s, stripe, C_CT0, c0);
+        cnt_addf(A, s, stripe, C_CT1, c1);
+        cnt_addf(A, s, stripe, C_CT2, c2);
+        cnt_addf(A, s, stripe, C_CT3, c3);
+      }
       cnt_add(A, s, stripe, C_NCOL, ncol);
       cnt_add(A, s, stripe, C_NCROSS, ncross);
       cnt_add(A, s, stripe, C_NSTALE, nstale);
       cnt_add(A, s, stripe, C_NPAIR, npair);
       cnt_add(A, s, stripe, C_NPRED, npred);
+      cnt_add(A, s, stripe, C_NEV, (unsigned long long)__popc(m));
+      cnt_add(A, s, stripe, C_NSCREEN, nscr);
+      atomicMax((unsigned long long*)&A.cnt[((int64_t)s * NSTRIPE + stripe) * NCNT + C_TLAST],
+                (unsigned long long)kmx);
+    }
+  }
+}
+
+// the selected events of a round, one warp each; per-system counters go to
+// one of NSTRIPE stripes to spread the atomics
+__global__ void __launch_bounds__(32 * WPB, 2) k_process(const SysDev* __restrict__ sys, RoundArgs A) {
+  __shared__ WarpScratch scr[WPB];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  WarpScratch* W = &scr[wid];
+  const int nsafe = *A.nsafe;
+  if (nsafe >= A.thr_min) return;                 // k_process_thread takes the round
+  const int gw = blockIdx.x * WPB + wid, nw = gridDim.x * WPB;
+  const int stripe = gw & (NSTRIPE - 1);
+  for (int n = gw; n < nsafe; n += nw) {
+    const int64_t g = A.safe[n];
+    const int s = A.dsys[g];
+    EvResult r;
+    process_event_warp(sys[s], A, s, g, W, lane, r);
+    if (r.ncol && lane < 4) cnt_addf(A, s, stripe, C_CT0 + lane, r.ct);
+    if (lane == 0) {
+      for (int k = 0; k < MAXDIRTY; k++) A.dcell[(int64_t)n * MAXDIRTY + k] = k < r.nd ? r.dc[k] : -1;
+      cnt_add(A, s, stripe, C_NCOL, r.ncol);
+      cnt_add(A, s, stripe, C_NCROSS, r.ncross);
+      cnt_add(A, s, stripe, C_NSTALE, r.nstale);
+      cnt_add(A, s, stripe, C_NPAIR, r.npair);
+      cnt_add(A, s, stripe, C_NPRED, r.npred);
       cnt_add(A, s, stripe, C_NEV, 1ull);
       atomicMax((unsigned long long*)&A.cnt[((int64_t)s * NSTRIPE + stripe) * NCNT + C_TLAST],
-                (unsigned long long)key);
-      if (bad) atomicAdd(A.violations, 1ull);
-      if (ovl) {
-        SysState* R = S.st;
-        R->err_a = a;
-        R->err_b = ob;
+                (unsigned long long)r.key);
+      if (r.bad) atomicAdd(A.violations, 1ull);
+      if (r.ovl) {
+        SysState* R = sys[s].st;
+        R->err_a = r.a;
+        R->err_b = r.ob;
         R->status = EDMD_ERR_OVERLAP;
       }
     }
@@ -750,8 +1130,40 @@ __global__ void __launch_bounds__(32 * WPB, 2) k_process(const SysDev* __restric
   }
 }
 
-// minimum (key, owner) of the events attributed to each dirty cell: one warp
-// per cell, lanes 0..8 walk the lists of the 3x3 block around it
+// minimum (key, id) of the events attributed to cell gc (global index) of
+// system S: one warp, lanes 0..8 walk the lists of the 3x3 block around it
+__device__ void recompute_cell(const SysDev& S, const RoundArgs& A, int64_t base, int64_t dbase, int32_t gc,
+                               int lane) {
+  const Box& B = S.B;
+  const int c = (int)(gc - base);
+  uint64_t bk = KINF;
+  int32_t bi = IINF;
+  if (lane < 9) {
+    const int x = c % B.Nxc, y = c / B.Nxc;
+    int p = S.head[pbc_cy(B, y + lane / 3 - 1) * B.Nxc + pbc_cx(B, x + lane % 3 - 1)];
+    int guard = 0;
+    while (p != NIL && guard++ < B.N) {
+      const int64_t g = dbase + p;
+      const uint64_t k = A.dkey[g];
+      if (k != KINF && (A.fc[2 * g] == c || A.fc[2 * g + 1] == c) && pair_less(k, A.dpk[g], bk, bi)) {
+        bk = k;
+        bi = A.dpk[g];
+      }
+      p = S.d[p].nxt;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    const uint64_t k2 = __shfl_xor_sync(FULLM, bk, o);
+    const int32_t i2 = __shfl_xor_sync(FULLM, bi, o);
+    if (pair_less(k2, i2, bk, bi)) { bk = k2; bi = i2; }
+  }
+  if (lane == 0) {
+    A.cmt[gc] = bk;
+    A.cmi[gc] = bi;
+  }
+}
+
+// the cells whose minimum the selected events can have changed, one warp each
 __global__ void __launch_bounds__(256) k_recompute(const SysDev* __restrict__ sys, RoundArgs A) {
   const int lane = threadIdx.x & 31;
   const int64_t total = (int64_t)(*A.nsafe) * MAXDIRTY;
@@ -760,35 +1172,161 @@ __global__ void __launch_bounds__(256) k_recompute(const SysDev* __restrict__ sy
     const int32_t gc = A.dcell[w];
     if (gc < 0) continue;
     const int s = A.dsys[A.safe[w / MAXDIRTY]];
+    recompute_cell(sys[s], A, A.coff[s], A.doff[s], gc, lane);
+  }
+}
+
+// is (k, id) the minimum of the (2r+1)^2 window around local cell c?
+__device__ bool window_min(const RoundArgs& A, int64_t base, int Nxc, int Nyc, int c, uint64_t k, int32_t id,
+                           int r) {
+  const int x = c % Nxc, y = c / Nxc;
+  for (int dy = -r; dy <= r; dy++) {
+    const int yy = wrapi(y + dy, Nyc);
+    for (int dx = -r; dx <= r; dx++) {
+      const int64_t cc = base + (int64_t)yy * Nxc + wrapi(x + dx, Nxc);
+      if (pair_less(A.cmt[cc], A.cmi[cc], k, id)) return false;
+    }
+  }
+  return true;
+}
+
+// Block mode (EDMD_F_ROUND_BLOCK): one block per system at a time (persistent
+// grid pulling systems from a counter).  The block runs the same rounds as the
+// grid-wide kernels -- selection over its cells, one warp per selected event,
+// minima of the dirty cells, screenshot barriers and the collision budget --
+// separated by block barriers instead of kernel boundaries, and keeps the
+// system's counters in shared memory.
+constexpr int BMAXEV = 128;          // events processed per round and system
+constexpr int BWPB = 4;              // warps per system block
+
+__global__ void __launch_bounds__(32 * BWPB, 4) k_block_rounds(const SysDev* __restrict__ sys, RoundArgs A,
+                                                            int32_t* __restrict__ work, int64_t max_rounds) {
+  __shared__ WarpScratch scr[BWPB];
+  __shared__ int32_t evl[BMAXEV];
+  __shared__ int32_t dl[BMAXEV * MAXDIRTY];
+  __shared__ int nev, ndl, s_sh, go, stop;
+  __shared__ uint64_t tlast, freeze;
+  __shared__ unsigned long long c_ncol, c_ncross, c_nstale, c_npair, c_npred, c_nev;
+  __shared__ double c_ct[4];
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  for (;;) {
+    if (tid == 0) s_sh = atomicAdd(work, 1);
+    __syncthreads();
+    const int s = s_sh;
+    if (s >= A.nsys) break;
     const SysDev& S = sys[s];
     const Box& B = S.B;
+    const int N = B.N, C = B.Nxc * B.Nyc;
     const int64_t base = A.coff[s], dbase = A.doff[s];
-    const int c = (int)(gc - base);
-    uint64_t bk = KINF;
-    int32_t bi = IINF;
-    if (lane < 9) {
-      const int x = c % B.Nxc, y = c / B.Nxc;
-      int p = S.head[pbc_cy(B, y + lane / 3 - 1) * B.Nxc + pbc_cx(B, x + lane % 3 - 1)];
-      int guard = 0;
-      while (p != NIL && guard++ < B.N) {
-        const int64_t g = dbase + p;
-        const uint64_t k = A.dkey[g];
-        if (k != KINF && (A.fc[2 * g] == c || A.fc[2 * g + 1] == c) && pair_less(k, A.dpk[g], bk, bi)) {
-          bk = k;
-          bi = A.dpk[g];
-        }
-        p = S.d[p].nxt;
+    if (tid == 0) {
+      c_ncol = c_ncross = c_nstale = c_npair = c_npred = c_nev = 0;
+      c_ct[0] = c_ct[1] = c_ct[2] = c_ct[3] = 0;
+      tlast = 0;
+      freeze = KINF;
+      stop = S.st->status != EDMD_OK;
+    }
+    __syncthreads();
+    int64_t rounds = 0;
+    while (!stop) {
+      if (++rounds > max_rounds) {
+        if (tid == 0) atomicAdd(A.active, 1);          // budget exhausted
+        break;
       }
+      if (tid == 0) { nev = 0; ndl = 0; }
+      __syncthreads();
+      uint64_t lim = time_key(S.ev[2 * N + SP_SCREEN].t);
+      if (A.tstop_key < lim) lim = A.tstop_key;
+      if (freeze < lim) lim = freeze;
+      for (int c = tid; c < C; c += blockDim.x) {
+        const uint64_t k = A.cmt[base + c];
+        if (k >= lim) continue;
+        const int32_t id = A.cmi[base + c];
+        const int64_t g = id & GMASK;
+        if (A.fc[2 * g] != c) continue;                 // decided at the owner's cell
+        if (!window_min(A, base, B.Nxc, B.Nyc, c, k, id, A.radius)) continue;
+        const int c2 = A.fc[2 * g + 1];
+        if (c2 != c && !window_min(A, base, B.Nxc, B.Nyc, c2, k, id, A.radius)) continue;
+        const int q = atomicAdd(&nev, 1);
+        if (q < BMAXEV) evl[q] = (int32_t)g;          // the rest waits for the next round
+      }
+      __syncthreads();
+      const int n = nev < BMAXEV ? nev : BMAXEV;
+      if (n == 0) {
+        // nothing eligible before the screenshot: pass it (takeAScreenshot,
+        // src/EDMD.c:4657-4661) or stop
+        const double tbar = S.ev[2 * N + SP_SCREEN].t;
+        const uint64_t fl = A.tstop_key < freeze ? A.tstop_key : freeze;
+        if (tid == 0) {
+          go = time_key(tbar) < fl ? 1 : 0;
+          if (!go) stop = 1;
+        }
+        __syncthreads();
+        if (go) {
+          for (int i = tid; i < N; i += blockDim.x) {
+            Disk p = S.d[i];
+            free_fly_i(B, p, tbar);
+            S.d[i] = p;
+            shadow_write(A, dbase + i, B, p, S.cx[i], S.cy[i], A.epoch[s]);
+          }
+          __syncthreads();
+          if (tid == 0) {
+            S.ev[2 * N + SP_SCREEN].t = tbar + S.dtime;
+            tlast = kmax(tlast, time_key(tbar));
+          }
+        }
+        __syncthreads();
+        continue;
+      }
+      for (int e = wid; e < n; e += BWPB) {
+        EvResult r;
+        process_event_warp(S, A, s, evl[e], &scr[wid], lane, r);
+        if (r.ncol && lane < 4) atomicAdd(&c_ct[lane], r.ct);
+        if (lane == 0) {
+          const int q = atomicAdd(&ndl, r.nd);
+          for (int k = 0; k < r.nd; k++) dl[q + k] = r.dc[k];
+          atomicAdd(&c_ncol, r.ncol);
+          atomicAdd(&c_ncross, r.ncross);
+          atomicAdd(&c_nstale, r.nstale);
+          atomicAdd(&c_npair, r.npair);
+          atomicAdd(&c_npred, r.npred);
+          atomicAdd(&c_nev, 1ull);
+          atomicMax((unsigned long long*)&tlast, (unsigned long long)r.key);
+          if (r.bad) atomicAdd(A.violations, 1ull);
+          if (r.ovl) {
+            S.st->err_a = r.a;
+            S.st->err_b = r.ob;
+            S.st->status = EDMD_ERR_OVERLAP;
+          }
+        }
+        __syncwarp();
+      }
+      __syncthreads();
+      for (int w = wid; w < ndl; w += BWPB) recompute_cell(S, A, base, dbase, dl[w], lane);
+      __syncthreads();
+      if (tid == 0) {
+        if (S.st->status != EDMD_OK) stop = 1;
+        if (freeze == KINF && S.st->ncol + c_ncol >= A.target[s]) freeze = tlast + 1;
+      }
+      __syncthreads();
     }
-    for (int o = 16; o > 0; o >>= 1) {
-      const uint64_t k2 = __shfl_xor_sync(FULLM, bk, o);
-      const int32_t i2 = __shfl_xor_sync(FULLM, bi, o);
-      if (pair_less(k2, i2, bk, bi)) { bk = k2; bi = i2; }
+    if (tid == 0) {
+      SysState* R = S.st;
+      for (int k = 0; k < 4; k++) R->collT[k] += c_ct[k];
+      R->ncol += c_ncol;
+      R->ncol_total += c_ncol;
+      R->ncross += c_ncross;
+      R->nstale += c_nstale;
+      R->npair += c_npair;
+      R->npred += c_npred;
+      R->nevents += c_nev;
+      if (tlast != 0) {
+        const double t = key_time(tlast);
+        if (t > R->t) R->t = t;
+      }
+      R->stop_reason = freeze != KINF ? EDMD_STOP_COLL : EDMD_STOP_TIME;
+      A.tlast[s] = rounds;                            // rounds this system took
     }
-    if (lane == 0) {
-      A.cmt[gc] = bk;
-      A.cmi[gc] = bi;
-    }
+    __syncthreads();
   }
 }
 
@@ -840,6 +1378,7 @@ __global__ void k_barrier(const SysDev* __restrict__ sys, RoundArgs A) {
         Disk p = S.d[i];
         free_fly_i(S.B, p, tbar);
         S.d[i] = p;
+        shadow_write(A, A.doff[s] + i, S.B, p, S.cx[i], S.cy[i], A.epoch[s]);
       }
       __syncthreads();
       if (threadIdx.x == 0) {
@@ -865,7 +1404,7 @@ __global__ void k_round_finish(const SysDev* __restrict__ sys, RoundArgs A) {
   for (int l = 0; l < NSTRIPE; l++) {
     const uint64_t* c = A.cnt + ((int64_t)s * NSTRIPE + l) * NCNT;
     for (int k = 0; k < 4; k++) ct[k] += __longlong_as_double((long long)c[k]);
-    for (int k = C_NCOL; k <= C_NEV; k++) v[k] += c[k];
+    for (int k = C_NCOL; k <= C_NSCREEN; k++) v[k] += c[k];
     tl = kmax(tl, c[C_TLAST]);
   }
   for (int k = 0; k < 4; k++) R->collT[k] += ct[k];
@@ -876,6 +1415,7 @@ __global__ void k_round_finish(const SysDev* __restrict__ sys, RoundArgs A) {
   R->npair += v[C_NPAIR];
   R->npred += v[C_NPRED];
   R->nevents += v[C_NEV];
+  R->nscreen += v[C_NSCREEN];
   if (tl != 0) {
     const double t = key_time(tl);
     if (t > R->t) R->t = t;
@@ -893,12 +1433,15 @@ __global__ void k_round_setup(const int64_t* __restrict__ doff, const SysDev* __
 
 struct RoundBufs {
   int32_t *dsys = nullptr, *fc = nullptr, *cmi = nullptr, *safe = nullptr, *nsafe = nullptr;
-  int32_t *dcell = nullptr, *selflag = nullptr, *active = nullptr, *dpk = nullptr;
+  int32_t *dcell = nullptr, *selflag = nullptr, *active = nullptr, *dpk = nullptr, *work = nullptr;
   uint8_t *drank = nullptr, *drank_bak = nullptr;
   int32_t *tsys = nullptr, *tx0 = nullptr, *ty0 = nullptr;
   int64_t *doff = nullptr, *coff = nullptr;
   uint64_t *dkey = nullptr, *cmt = nullptr, *lw = nullptr, *lr = nullptr;
   uint64_t *lim = nullptr, *target = nullptr, *freeze = nullptr, *tlast = nullptr, *cnt = nullptr;
+  float4* shp = nullptr;
+  float* sht = nullptr;
+  double* epoch = nullptr;
   unsigned long long* viol = nullptr;
   int64_t ntiles = 0;
 };
@@ -926,11 +1469,12 @@ int round_init(edmd_ctx* ctx) {
   CK(dalloc(&R->drank, TN)); CK(dalloc(&R->drank_bak, TN));
   CK(dalloc(&R->cmi, TC)); CK(dalloc(&R->cmt, TC)); CK(dalloc(&R->lw, TC)); CK(dalloc(&R->lr, TC));
   CK(dalloc(&R->safe, TN)); CK(dalloc(&R->nsafe, 1)); CK(dalloc(&R->dcell, TN * MAXDIRTY));
-  CK(dalloc(&R->selflag, ctx->nsys)); CK(dalloc(&R->active, 1));
+  CK(dalloc(&R->selflag, ctx->nsys)); CK(dalloc(&R->active, 1)); CK(dalloc(&R->work, 1));
   CK(dalloc(&R->doff, ctx->nsys)); CK(dalloc(&R->coff, ctx->nsys));
   CK(dalloc(&R->lim, ctx->nsys)); CK(dalloc(&R->target, ctx->nsys)); CK(dalloc(&R->freeze, ctx->nsys));
   CK(dalloc(&R->tlast, ctx->nsys)); CK(dalloc(&R->viol, 1));
   CK(dalloc(&R->cnt, (int64_t)ctx->nsys * NSTRIPE * NCNT));
+  CK(dalloc(&R->shp, TN)); CK(dalloc(&R->sht, TN)); CK(dalloc(&R->epoch, ctx->nsys));
   CK(dalloc(&R->tsys, R->ntiles)); CK(dalloc(&R->tx0, R->ntiles)); CK(dalloc(&R->ty0, R->ntiles));
   CK(sync_copy(ctx, R->doff, ctx->disk_off.data(), ctx->nsys * 8, cudaMemcpyHostToDevice));
   CK(sync_copy(ctx, R->coff, ctx->cell_off.data(), ctx->nsys * 8, cudaMemcpyHostToDevice));
@@ -956,6 +1500,7 @@ cudaError_t enqueue_round(edmd_ctx* ctx, const RoundBufs* R, const RoundArgs& A,
   const unsigned tgrid = (unsigned)(R->ntiles < nsm * 8 ? R->ntiles : nsm * 8);
   k_select<<<tgrid, TX * TY, select_smem(A.radius), st>>>(ctx->ds, A);
   k_process<<<nsm * 16, 32 * WPB, 0, st>>>(ctx->ds, A);
+  k_process_thread<<<nsm * 8, 128, 0, st>>>(ctx->ds, A);
   k_recompute<<<nsm * 8, 256, 0, st>>>(ctx->ds, A);
   k_barrier<<<ctx->nsys < nsm * 8 ? ctx->nsys : nsm * 8, 256, 0, st>>>(ctx->ds, A);
   return cudaGetLastError();
@@ -969,7 +1514,7 @@ void round_free(edmd_ctx* ctx) {
   void* p[] = {R->dsys, R->fc, R->cmi, R->safe, R->nsafe, R->dcell, R->selflag, R->active,
                R->tsys, R->tx0, R->ty0, R->doff, R->coff, R->dkey, R->cmt, R->lw, R->lr,
                R->lim, R->target, R->freeze, R->tlast, R->cnt, R->viol, R->dpk, R->drank,
-               R->drank_bak};
+               R->drank_bak, R->work, R->shp, R->sht, R->epoch};
   for (void* q : p)
     if (q) cudaFree(q);
   delete R;
@@ -1005,7 +1550,17 @@ static int run_rounds(edmd_ctx* ctx, const std::vector<uint64_t>& tgt, double t_
   A.dkey = R->dkey; A.dpk = R->dpk; A.drank = R->drank; A.fc = R->fc; A.cmt = R->cmt; A.cmi = R->cmi; A.lw = R->lw; A.lr = R->lr;
   A.safe = R->safe; A.nsafe = R->nsafe; A.dcell = R->dcell; A.selflag = R->selflag;
   A.active = R->active; A.lim = R->lim; A.target = R->target; A.freeze = R->freeze;
-  A.tlast = R->tlast; A.cnt = R->cnt; A.tsys = R->tsys; A.tx0 = R->tx0; A.ty0 = R->ty0; A.violations = R->viol;
+  // one thread per event needs enough events to keep every SM busy with one
+  // lane each: the cells of small systems stay in L2, so 4096 events do; the
+  // events of a large system are far apart, each cell list walk misses L2,
+  // and below ~16k events a warp's 32 lanes per event hide that latency
+  // better (4096-system batch: mixed 2.6e7 coll/s, warp-only 2.4e7,
+  // thread-only 2.0e7; 10^6 disks, 8k events a round: warp 3.0e7, thread
+  // 2.1e7; 4*10^6 disks, 22k events a round: thread 3.2e7, warp 2.9e7)
+  A.thr_min = (flags & EDMD_F_ROUND_THREAD) ? 0
+            : (flags & EDMD_F_ROUND_WARP) ? INT32_MAX
+            : (TN / ctx->nsys <= 65536 ? 4096 : 16384);
+  A.tlast = R->tlast; A.cnt = R->cnt; A.shp = R->shp; A.sht = R->sht; A.epoch = R->epoch; A.tsys = R->tsys; A.tx0 = R->tx0; A.ty0 = R->ty0; A.violations = R->viol;
   const unsigned gd = (unsigned)((TN + 255) / 256);
   // the serial queue keys are still in the event records only when the
   // state comes from a serial engine
@@ -1017,6 +1572,28 @@ static int run_rounds(edmd_ctx* ctx, const std::vector<uint64_t>& tgt, double t_
   int dev = 0, nsm = 0;
   CK(cudaGetDevice(&dev));
   CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  // grid-wide rounds unless asked otherwise: on the 4096-system batch they
+  // run 2.6e7 coll/s against 1.8e7 for one block per system, whose four
+  // warps leave the SMs' FP64 pipes idle at the block barriers
+  const bool block_mode = (flags & EDMD_F_ROUND_BLOCK) != 0;
+  if (block_mode) {
+    // enough systems to fill the GPU: one block per system, no grid-wide rounds
+    CK(cudaMemsetAsync(R->work, 0, 4, st));
+    CK(cudaMemsetAsync(R->active, 0, 4, st));
+    k_block_rounds<<<nsm * 4, 32 * BWPB, 0, st>>>(ctx->ds, A, R->work, max_rounds);
+    CK(cudaGetLastError());
+    std::vector<uint64_t> rs(ctx->nsys);
+    int32_t capped = 0;
+    CK(cudaMemcpyAsync(rs.data(), R->tlast, ctx->nsys * 8, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(&capped, R->active, 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(viol_out, R->viol, 8, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    uint64_t mx = 0;
+    for (uint64_t v : rs) mx = v > mx ? v : mx;
+    *rounds_out += (int64_t)mx;
+    *active_out = capped;
+    return EDMD_OK;
+  }
   // a block of rounds is captured once into a graph and replayed until every
   // system has stopped; the host polls the active count between blocks
   const int per_graph = 16;

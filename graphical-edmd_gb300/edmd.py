@@ -22,6 +22,7 @@ LIB_PATH = os.path.join(HERE, "libedmd_gpu.so")
 OK, ERR_ARG, ERR_CUDA, ERR_OVERLAP, ERR_BUDGET, ERR_CAPACITY, ERR_NODEV = range(7)
 STOP_COLL, STOP_TIME, STOP_TMAX, STOP_SCREEN, STOP_GROW = 1, 2, 3, 4, 5
 F_STOP_AT_SCREEN, F_STOP_AT_GROW, F_TRACE, F_COUNT_NORMAL, F_LOG, F_EXACT = 1, 2, 4, 8, 16, 32
+F_ROUND_GRID, F_ROUND_BLOCK, F_SCREEN, F_ROUND_THREAD, F_ROUND_WARP = 64, 128, 256, 512, 1024
 ENGINE_AUTO, ENGINE_WARP, ENGINE_LANE = 0, 1, 2
 
 
@@ -48,7 +49,7 @@ class Counters(C.Structure):
     _fields_ = [("ncol", C.c_uint64), ("ncol_total", C.c_uint64), ("ncross", C.c_uint64),
                 ("nstale", C.c_uint64), ("npair", C.c_uint64), ("npred", C.c_uint64),
                 ("nevents", C.c_uint64), ("t", C.c_double), ("growing", C.c_int32),
-                ("stop_reason", C.c_int32)]
+                ("stop_reason", C.c_int32), ("nscreen", C.c_uint64)]
 
 
 # every symbol the public headers declare, in declaration order

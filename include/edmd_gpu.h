@@ -57,6 +57,11 @@ extern "C" {
 #define EDMD_F_COUNT_NORMAL    8u  /* max_coll counts normal-phase only       */
 #define EDMD_F_LOG            16u  /* record collision geometry (edmd_log_entry) */
 #define EDMD_F_EXACT          32u  /* edmd_advance_rounds: replay on a causality violation */
+#define EDMD_F_ROUND_GRID     64u  /* edmd_advance_rounds: grid-wide rounds (the default) */
+#define EDMD_F_ROUND_BLOCK   128u  /* edmd_advance_rounds: one block per system, rounds between block barriers */
+#define EDMD_F_SCREEN        256u  /* edmd_advance_rounds: FP32 screen of separating pairs before FP64 */
+#define EDMD_F_ROUND_THREAD  512u  /* edmd_advance_rounds: one thread per selected event in every round */
+#define EDMD_F_ROUND_WARP   1024u  /* edmd_advance_rounds: one warp per selected event in every round */
 
 /*
  * One periodic 2D system.  Replaces the globals that constantInit
@@ -104,6 +109,7 @@ typedef struct edmd_counters {
 	double   t;            /* current simulation time                          */
 	int32_t  growing;      /* 1 while the growth phase runs                    */
 	int32_t  stop_reason;  /* EDMD_STOP_* of the last advance                  */
+	uint64_t nscreen;      /* of npair: pairs the FP32 screen proved separating */
 } edmd_counters;
 
 typedef struct edmd_ctx edmd_ctx;
@@ -139,7 +145,7 @@ int edmd_advance(edmd_ctx* ctx, int64_t max_coll, double t_stop, uint32_t flags,
  * body as edmd_advance, src/EDMD.c:523-618, for many events at once).  Each
  * round processes, in every system, the pending events that are the earliest
  * within `radius` cells (3..12) of their footprint (owner's cell plus partner's
- * or target cell), one GPU thread per event; screenshot events act as barriers
+ * or target cell), one GPU warp or thread per event; screenshot events act as barriers
  * (every disk is free-flown to them, src/EDMD.c:4657-4661).  A system stops at
  * t_stop, or once it has accepted max_coll collisions in this call: it then
  * finishes the pending events earlier than the latest one it processed, so
@@ -154,6 +160,14 @@ int edmd_advance(edmd_ctx* ctx, int64_t max_coll, double t_stop, uint32_t flags,
  * (3 -> 4 -> 8 -> 12; a violation at 12 returns EDMD_ERR_BUDGET), so a successful
  * call is always the serial result and *violations_out counts the discarded
  * ones.
+ * Rounds are grid-wide (selection over every tile, one kernel per step);
+ * EDMD_F_ROUND_BLOCK runs them inside one block per system instead.  A round
+ * of many events runs one thread per event (from 4096 events when the systems
+ * average at most 65536 disks, else from 16384), a smaller one one warp per
+ * event; EDMD_F_ROUND_THREAD / EDMD_F_ROUND_WARP force either.  EDMD_F_SCREEN
+ * lets the thread path reject separating pairs in FP32 first, with a bound on
+ * the FP32 error that keeps every FP64 decision.  All choices give the same
+ * results.
  * EDMD_F_TRACE records collisions in processing order.  After this call
  * edmd_advance refuses the context until edmd_load_state restages it. */
 int edmd_advance_rounds(edmd_ctx* ctx, int64_t max_coll, double t_stop, uint32_t flags,

@@ -76,19 +76,24 @@ def oracle_run_to(oracle, start, t_stop):
     return o, n
 
 
-@pytest.mark.parametrize("N,phi,seed,t_stop", [(20000, 0.72, 5, 3.0), (4096, 0.45, 6, 12.0),
-                                                (100000, 0.72, 8, 0.6)])
-def test_rounds_match_oracle_state(edmd, oracle, N, phi, seed, t_stop):
-    """Larger systems against the oracle: counters, final state, screenshot at t = 1."""
+@pytest.mark.parametrize("N,phi,seed,t_stop,mode", [(20000, 0.72, 5, 3.0, 0), (4096, 0.45, 6, 12.0, 0),
+                                                     (100000, 0.72, 8, 0.6, 0), (100000, 0.72, 8, 0.6, 1),
+                                                     (640000, 0.72, 9, 0.25, 1), (640000, 0.72, 9, 0.25, 2)])
+def test_rounds_match_oracle_state(edmd, oracle, N, phi, seed, t_stop, mode):
+    """Larger systems against the oracle: counters, final state, screenshot at t = 1.
+    mode 1 runs every round one thread per event, mode 2 adds the FP32 screen
+    of separating pairs."""
     s = edmd.hex_start(N, phi, seed)
     o, n = oracle_run_to(oracle, s, t_stop)
     eng = edmd.Engine([dict(desc=edmd.default_desc(s["N"], s["Lx"], s["Ly"]), **s)])
-    rc, ms, rounds, viol = eng.advance_rounds(t_stop=t_stop, radius=3, flags=EXACT)
+    fl = EXACT | (edmd.F_ROUND_THREAD if mode else 0) | (edmd.F_SCREEN if mode == 2 else 0)
+    rc, ms, rounds, viol = eng.advance_rounds(t_stop=t_stop, radius=3, flags=fl)
     eng.sync()
     c = eng.counters(0)
     oc = o.counters()
     assert (c["ncol"], c["ncross"]) == (oc["ncol"], oc["ncross"]) and c["ncol"] == n
     assert c["t"] == o.t
+    assert (c["nscreen"] > 0) == (mode == 2)
     st, ost = eng.state(0), o.state()
     for k in ("x", "y", "vx", "vy"):
         np.testing.assert_array_equal(st[k], ost[k])
@@ -188,3 +193,46 @@ def test_exact_mode_replays_to_the_same_result(edmd):
     for k in ("x", "y", "vx", "vy", "coll"):
         np.testing.assert_array_equal(out[0][0][k], out[1][0][k])
     assert out[0][1]["ncol"] == out[1][1]["ncol"]
+
+
+def test_block_rounds_match_grid_rounds_and_oracle(edmd, oracle):
+    """One block per system gives the grid-wide engine's result, and the oracle's."""
+    rng = np.random.default_rng(31)
+    cases = [(int(n), float(p), 100 + k) for k, (n, p) in
+             enumerate(zip(rng.integers(256, 1500, 160), rng.uniform(0.3, 0.72, 160)))]
+    starts = [edmd.hex_start(N, phi, seed) for N, phi, seed in cases]
+    systems = [dict(desc=edmd.default_desc(s["N"], s["Lx"], s["Ly"]), **s) for s in starts]
+    t_stop = 1.5
+    out = []
+    for mode in (edmd.F_ROUND_BLOCK, edmd.F_ROUND_GRID):
+        eng = edmd.Engine(systems)
+        rc, ms, rounds, viol = eng.advance_rounds(t_stop=t_stop, radius=3, flags=EXACT | mode)
+        eng.sync()
+        out.append(eng.states())
+        cb = eng.all_counters()
+        eng.close()
+    for k in ("x", "y", "vx", "vy"):
+        np.testing.assert_array_equal(out[0][k], out[1][k])
+    off = np.cumsum([0] + [s["N"] for s in starts])
+    for q in (0, 57, 159):
+        o, n = oracle_run_to(oracle, starts[q], t_stop)
+        ost = o.state()
+        for k in ("x", "y", "vx", "vy"):
+            np.testing.assert_array_equal(out[0][k][off[q]:off[q + 1]], ost[k])
+        assert cb["ncol"][q] == o.counters()["ncol"]
+
+
+def test_block_rounds_collision_budget(edmd, oracle):
+    """Block mode with a collision budget per system ends on serial states."""
+    cases = [(300 + 7 * k, 0.5 + 0.001 * k, 200 + k) for k in range(160)]
+    starts = [edmd.hex_start(N, phi, seed) for N, phi, seed in cases]
+    eng = edmd.Engine([dict(desc=edmd.default_desc(s["N"], s["Lx"], s["Ly"]), **s) for s in starts])
+    eng.advance_rounds(max_coll=2000, radius=3, flags=EXACT | edmd.F_ROUND_BLOCK)
+    c = eng.all_counters()
+    assert (c["ncol"] >= 2000).all() and (c["stop_reason"] == edmd.STOP_COLL).all()
+    eng.sync()
+    for q in (3, 99):
+        o, n = oracle_run_to(oracle, starts[q], np.nextafter(c["t"][q], np.inf))
+        assert n == c["ncol"][q]
+        np.testing.assert_array_equal(eng.state(q)["x"], o.state()["x"])
+    eng.close()
