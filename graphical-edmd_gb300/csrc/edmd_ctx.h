@@ -30,6 +30,9 @@ struct edmd_ctx {
   double* rows = nullptr;
   double* stage = nullptr;          // SoA gather buffer (6 x total_N)
   int32_t* work = nullptr;
+  int32_t* order = nullptr;      // warp engine: order the systems are taken in
+  uint32_t* cost = nullptr;      // warp engine: each system's run time in the last call
+  std::vector<int32_t> order_h;
   edmd_log_entry* logbuf = nullptr; // per-system collision-geometry logs
   int64_t log_cap = 0;
   std::vector<void*> ckpt;          // device snapshots of the whole engine state

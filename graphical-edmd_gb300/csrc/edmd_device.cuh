@@ -56,6 +56,12 @@ __device__ __forceinline__ uint64_t time_key(double t) {
   return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
 }
 
+// inverse of time_key (a zero comes back as +0)
+__device__ __forceinline__ double key_time(uint64_t k) {
+  uint64_t u = (k >> 63) ? (k & 0x7fffffffffffffffull) : ~k;
+  return __longlong_as_double((long long)u);
+}
+
 struct Box {
   double Lx, Ly, hLx, hLy;     // box and halves (boxConstantHelper src/EDMD.c:679)
   double cxs, cys, cxf, cyf;   // cell sizes and reciprocals
@@ -115,6 +121,8 @@ struct RunArgs {
   int64_t max_events;
   int32_t nsys;
   int32_t* work;               // persistent work counter (warp engine)
+  const int32_t* order;        // warp engine: systems in the order they are taken (null: 0, 1, ...)
+  uint32_t* cost;              // warp engine: each system's run time in this call (units of 1.024 us)
 };
 
 // ---------------------------------------------------------------- arithmetic

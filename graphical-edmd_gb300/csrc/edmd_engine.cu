@@ -26,6 +26,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <algorithm>
 #include <vector>
 
 using namespace edmd;
@@ -208,9 +209,17 @@ __device__ __forceinline__ double pair_time(const SysDev& S, const Disk& A, int 
   return coll_time_normal_i(S.B, A, P, t, ovl);
 }
 
-__device__ __forceinline__ void best_merge(double& bd, int& bo, int& bp, uint32_t& bc,
-                                           double d, int o, int p, uint32_t c) {
-  if (d < bd || (d == bd && o < bo)) { bd = d; bo = o; bp = p; bc = c; }
+// candidate times compared as their order-preserving integer images: the
+// same order as FP64 '<' (both zeros share one image; a NaN, which '<' never
+// selects, maps above every number), on the integer pipe
+__device__ __forceinline__ uint64_t cand_key(double d) {
+  const uint64_t u = (uint64_t)__double_as_longlong(d);
+  return (u & 0x7fffffffffffffffull) > 0x7ff0000000000000ull ? ~0ull : time_key(d);
+}
+
+__device__ __forceinline__ void best_merge(uint64_t& bk, int& bo, int& bp, uint32_t& bc,
+                                           uint64_t k, int o, int p, uint32_t c) {
+  if (k < bk || (k == bk && o < bo)) { bk = k; bo = o; bp = p; bc = c; }
 }
 
 // collisionEventNormal / Grow (src/EDMD.c:2829 / 3104) for disks a0 and a1
@@ -238,7 +247,7 @@ __device__ void predict2(const SysDev& S, SysState& R, int a0, int a1, Pred& r0,
   bool spill = __any_sync(FULL, cnt > MAXC);
   Disk A0 = S.d[a0];
   Disk A1 = a1 >= 0 ? S.d[a1] : A0;
-  double bd0 = dinit, bd1 = dinit;
+  uint64_t bd0 = cand_key(dinit), bd1 = bd0;
   int bo0 = -1, bo1 = -1, bp0 = 0, bp1 = 0;
   uint32_t bc0 = 0, bc1 = 0;
   bool lovl = false;
@@ -269,8 +278,8 @@ __device__ void predict2(const SysDev& S, SysState& R, int a0, int a1, Pred& r0,
       bool ov = false;
       double d = pair_time(S, g1 ? A1 : A0, g1 ? a1 : a0, P, p, R.t, grow, &ov);
       if (ov) { lovl = true; la = g1 ? a1 : a0; lb = p; }
-      if (g1) best_merge(bd1, bo1, bp1, bc1, d, o, p, P.coll);
-      else best_merge(bd0, bo0, bp0, bc0, d, o, p, P.coll);
+      if (g1) best_merge(bd1, bo1, bp1, bc1, cand_key(d), o, p, P.coll);
+      else best_merge(bd0, bo0, bp0, bc0, cand_key(d), o, p, P.coll);
     }
     __syncwarp();
   } else {
@@ -288,8 +297,8 @@ __device__ void predict2(const SysDev& S, SysState& R, int a0, int a1, Pred& r0,
           bool ov = false;
           double d = pair_time(S, AA, a, P, p, R.t, grow, &ov);
           if (ov) { lovl = true; la = a; lb = p; }
-          if (g) best_merge(bd1, bo1, bp1, bc1, d, q * 4096 + k, p, P.coll);
-          else best_merge(bd0, bo0, bp0, bc0, d, q * 4096 + k, p, P.coll);
+          if (g) best_merge(bd1, bo1, bp1, bc1, cand_key(d), q * 4096 + k, p, P.coll);
+          else best_merge(bd0, bo0, bp0, bc0, cand_key(d), q * 4096 + k, p, P.coll);
           k++;
         }
         p = P.nxt;
@@ -301,7 +310,7 @@ __device__ void predict2(const SysDev& S, SysState& R, int a0, int a1, Pred& r0,
   // lexicographic (dt, scan order) minimum over the warp
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
-    double d = __shfl_xor_sync(FULL, bd0, o); int oo = __shfl_xor_sync(FULL, bo0, o);
+    uint64_t d = __shfl_xor_sync(FULL, bd0, o); int oo = __shfl_xor_sync(FULL, bo0, o);
     int pp = __shfl_xor_sync(FULL, bp0, o); uint32_t cc = __shfl_xor_sync(FULL, bc0, o);
     best_merge(bd0, bo0, bp0, bc0, d, oo, pp, cc);
     d = __shfl_xor_sync(FULL, bd1, o); oo = __shfl_xor_sync(FULL, bo1, o);
@@ -310,8 +319,8 @@ __device__ void predict2(const SysDev& S, SysState& R, int a0, int a1, Pred& r0,
   }
   if (bo0 < 0) bc0 = S.d[0].coll;   // no partner: partner 0 (src/EDMD.c:2830)
   if (bo1 < 0) bc1 = S.d[0].coll;
-  r0.dt = bd0; r0.partner = bp0; r0.ca = bc0;
-  r1.dt = bd1; r1.partner = bp1; r1.ca = bc1;
+  r0.dt = key_time(bd0); r0.partner = bp0; r0.ca = bc0;
+  r1.dt = key_time(bd1); r1.partner = bp1; r1.ca = bc1;
   R.npair += (uint64_t)tot;
   R.npred += (a1 >= 0) ? 2 : 1;
   unsigned m = __ballot_sync(FULL, lovl);
@@ -444,7 +453,7 @@ __device__ __noinline__ void do_growstop(const SysDev& S, SysState& R, int lane,
 
 // ---------------------------------------------------------------- run loop
 
-__device__ void run_system(const SysDev& S, const RunArgs& A, int lane, WarpSmem* sm) {
+__device__ void run_system(const SysDev& S, const RunArgs& A, int64_t max_coll, int lane, WarpSmem* sm) {
   const Box& B = S.B;
   const int N = B.N;
   SysState R = *S.st;
@@ -456,7 +465,7 @@ __device__ void run_system(const SysDev& S, const RunArgs& A, int lane, WarpSmem
   int oa = -1, ob = -1;
   for (;;) {
     if (!(R.t <= S.tmax)) { stop = EDMD_STOP_TMAX; break; }
-    if (logged >= A.max_coll) { stop = EDMD_STOP_COLL; break; }
+    if (logged >= max_coll) { stop = EDMD_STOP_COLL; break; }
     if (nev >= A.max_events) { status = EDMD_ERR_BUDGET; break; }
     Node r;
     int guard = 0;
@@ -664,18 +673,27 @@ __device__ void run_system(const SysDev& S, const RunArgs& A, int lane, WarpSmem
   __syncwarp();
 }
 
+// Persistent launch: warps pull systems from a counter, in A.order, and
+// record each system's run time (globaltimer) for the next call's order.
 __global__ void __launch_bounds__(32 * WARPS_PER_BLOCK, 4)
 k_run(const SysDev* __restrict__ sys, RunArgs A) {
   __shared__ WarpSmem smem[WARPS_PER_BLOCK];
   const int lane = threadIdx.x & 31;
   const int w = threadIdx.x >> 5;
   for (;;) {
-    int s = 0;
-    if (lane == 0) s = atomicAdd(A.work, 1);
-    s = __shfl_sync(FULL, s, 0);
-    if (s >= A.nsys) break;
-    SysDev S = sys[s];
-    run_system(S, A, lane, &smem[w]);
+    int it = 0;
+    if (lane == 0) it = atomicAdd(A.work, 1);
+    it = __shfl_sync(FULL, it, 0);
+    if (it >= A.nsys) break;
+    const int s = A.order ? A.order[it] : it;
+    unsigned long long t0 = 0, t1 = 0;
+    if (A.cost) asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+    run_system(sys[s], A, A.max_coll, lane, &smem[w]);
+    if (A.cost && lane == 0) {
+      asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t1));
+      const unsigned long long c = (t1 - t0) >> 10;
+      A.cost[s] = c > 0xffffffffull ? 0xffffffffu : (uint32_t)c;
+    }
   }
 }
 
@@ -1047,6 +1065,9 @@ extern "C" int edmd_create(int32_t nsys, const edmd_system_desc* desc, const dou
   CK(dalloc(&ctx->trace, (size_t)nsys * trace_cap));
   CK(dalloc(&ctx->rows, (size_t)nsys * rows_cap * 9));
   CK(dalloc(&ctx->work, 1));
+  CK(dalloc(&ctx->order, nsys));
+  CK(dalloc(&ctx->cost, nsys));
+  CK(cudaMemsetAsync(ctx->cost, 0, nsys * sizeof(uint32_t), ctx->stream));
   CK(dalloc(&ctx->ds, nsys));
   if (ctx->engine == EDMD_ENGINE_LANE) {
     CK(dalloc(&ctx->cal, (size_t)TN * CAL_SUB * CAL_LINE));
@@ -1091,6 +1112,7 @@ extern "C" int edmd_advance(edmd_ctx* ctx, int64_t max_coll, double t_stop, uint
   RunArgs A;
   A.max_coll = max_coll; A.t_stop = t_stop; A.flags = flags; A.max_events = max_events;
   A.nsys = ctx->nsys; A.work = ctx->work;
+  A.order = nullptr; A.cost = ctx->cost;
   if (ctx->engine == EDMD_ENGINE_LANE) {
     CK(cudaEventRecord(ctx->e0, ctx->stream));
     CK(lane_run_launch(ctx->ds, A, g_lane_threads, ctx->stream));
@@ -1105,6 +1127,25 @@ extern "C" int edmd_advance(edmd_ctx* ctx, int64_t max_coll, double t_stop, uint
     int grid = per_sm * nsm;
     if (grid > want) grid = want;
     if (grid < 1) grid = 1;
+    // more systems than resident warps: with one item per system the last
+    // wave runs on part of the GPU; chunks of the collision budget let the
+    // warps share the remaining work evenly (same events, same results)
+    const int64_t resident = (int64_t)grid * WARPS_PER_BLOCK;
+    if (ctx->nsys > resident) {
+      // more systems than resident warps: the systems that took longest in
+      // the previous call start first (longest processing time first), so the
+      // last wave holds the short ones and the launch ends with fewer idle
+      // warps; ties keep index order, and the first call runs in index order
+      std::vector<uint32_t> cost(ctx->nsys);
+      CK(sync_copy(ctx, cost.data(), ctx->cost, ctx->nsys * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+      std::vector<int32_t>& ord = ctx->order_h;
+      ord.resize(ctx->nsys);
+      for (int s = 0; s < ctx->nsys; s++) ord[s] = s;
+      std::stable_sort(ord.begin(), ord.end(), [&](int32_t a, int32_t b) { return cost[a] > cost[b]; });
+      CK(cudaMemcpyAsync(ctx->order, ord.data(), ctx->nsys * sizeof(int32_t), cudaMemcpyHostToDevice,
+                         ctx->stream));
+      A.order = ctx->order;
+    }
     CK(cudaEventRecord(ctx->e0, ctx->stream));
     k_run<<<grid, 32 * WARPS_PER_BLOCK, 0, ctx->stream>>>(ctx->ds, A);
   }
@@ -1245,7 +1286,7 @@ extern "C" int edmd_destroy(edmd_ctx* ctx) {
   round_free(ctx);
   void* ptrs[] = {ctx->d, ctx->vr, ctx->cx, ctx->cy, ctx->prv, ctx->crossX, ctx->crossY, ctx->head,
                   ctx->ev, ctx->on, ctx->op, ctx->tree, ctx->st, ctx->trace, ctx->rows, ctx->stage,
-                  ctx->work, ctx->ds, ctx->cal, ctx->mask};
+                  ctx->work, ctx->order, ctx->cost, ctx->ds, ctx->cal, ctx->mask};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (void* p : ctx->ckpt)
@@ -1408,7 +1449,7 @@ extern "C" int edmd_run_noalloc(const edmd_system_desc* desc, double* x, double*
   cudaStream_t st = (cudaStream_t)stream;
   RunArgs A;
   A.max_coll = max_coll; A.t_stop = t_stop; A.flags = 0; A.max_events = (int64_t)1 << 60;
-  A.nsys = 1; A.work = work;
+  A.nsys = 1; A.work = work; A.order = nullptr; A.cost = nullptr;
   k_noalloc_put<<<1, 1, 0, st>>>(S, dsys);
   k_noalloc_stage<<<1, 32, 0, st>>>(dsys, x, y, vx, vy, rad, m, D.first_screen, D.first_thermo);
   k_init_events<<<dim3((unsigned)((N + 1 + 127) / 128), 1), 128, 0, st>>>(dsys);

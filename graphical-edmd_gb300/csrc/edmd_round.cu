@@ -97,11 +97,6 @@ __device__ __forceinline__ bool pair_less(uint64_t t1, int32_t i1, uint64_t t2, 
   return t1 < t2 || (t1 == t2 && i1 < i2);
 }
 
-__device__ __forceinline__ double key_time(uint64_t k) {
-  uint64_t u = (k >> 63) ? (k & 0x7fffffffffffffffull) : ~k;
-  return __longlong_as_double((long long)u);
-}
-
 __device__ __forceinline__ uint64_t kmax(uint64_t a, uint64_t b) { return a > b ? a : b; }
 
 // disk i's next event slot (the crossing wins an exact tie) and its key

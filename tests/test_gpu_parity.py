@@ -82,3 +82,25 @@ def test_batched_systems_match_reference(edmd, engine):
         for s in range(len(systems)):
             check_against_golden(eng, s, gs[s % len(gs)])
         eng.close()
+
+
+def test_batch_larger_than_resident_warps(edmd, oracle):
+    """More systems than resident warps: from the second call on, the systems
+    are taken longest-first by their previous run time; every system still
+    gives the oracle's result."""
+    starts = [edmd.hex_start(256 + 16 * (k % 7), 0.45 + 0.04 * (k % 7), 500 + k) for k in range(2600)]
+    eng = edmd.Engine([dict(desc=edmd.default_desc(s["N"], s["Lx"], s["Ly"]), **s) for s in starts])
+    for _ in range(3):
+        eng.advance(max_coll=1000)
+    eng.sync()
+    assert (eng.all_counters()["ncol"] == 3000).all()
+    for q in (0, 1300, 2599):
+        s = starts[q]
+        o = oracle.Oracle(arrays={k: s[k] for k in ("x", "y", "vx", "vy", "rad", "m", "type")},
+                          Lx=s["Lx"], Ly=s["Ly"])
+        o.run(3000, cap=1)
+        o.sync()
+        st = eng.state(q)
+        for k in ("x", "y", "vx", "vy"):
+            np.testing.assert_array_equal(st[k], o.state()[k])
+    eng.close()
