@@ -237,6 +237,18 @@ __device__ __forceinline__ bool is_neg(double a) {
 }
 __device__ __forceinline__ bool is_pos(double a) { return __double_as_longlong(a) > 0; }
 
+// general a < b and a <= b on the integer pipe: false when either is a NaN,
+// and -0 equals +0, exactly as the FP64 comparisons
+__device__ __forceinline__ bool nan_bits(double a) {
+  return ((unsigned long long)__double_as_longlong(a) & 0x7fffffffffffffffull) > 0x7ff0000000000000ull;
+}
+__device__ __forceinline__ bool lt_i(double a, double b) {
+  return !nan_bits(a) && !nan_bits(b) && time_key(a) < time_key(b);
+}
+__device__ __forceinline__ bool le_i(double a, double b) {
+  return !nan_bits(a) && !nan_bits(b) && time_key(a) <= time_key(b);
+}
+
 // pbc / pbc_in / free flight with integer-pipe comparisons (same results)
 __device__ __forceinline__ void pbc_i(const Box& B, double& dx, double& dy) {
   if (ge_pos(dx, B.hLx)) dx -= B.Lx;
@@ -296,9 +308,41 @@ __device__ __forceinline__ double crossing_time_i(const Box& B, const Disk& p, i
   else { a = (1 + cy) * B.cys - p.y; yy = 4; }
   if (ge_pos(a, B.hLy)) a = a - B.Ly; else if (lt_neg(a, B.hLy)) a = a + B.Ly;
   ty = a / p.vy;
-  if (tx < ty) { *dir = xx; return t + tx; }
+  if (lt_i(tx, ty)) { *dir = xx; return t + tx; }
   *dir = yy;
   return t + ty;
+}
+
+// One axis of crossingEventNormal (src/EDMD.c:2405-2482): the time to the
+// wall of cell (cx, cy) the disk moves towards along x (ydim false) or y, and
+// the direction code.  Branch-free over the axis, with the same operations
+// as crossing_time_i, so lanes working on different axes share instructions.
+__device__ __forceinline__ double axis_time(const Box& B, const Disk& p, int cx, int cy, bool ydim, int* dir) {
+  const double pos = ydim ? p.y : p.x, v = ydim ? p.vy : p.vx;
+  const double cs = ydim ? B.cys : B.cxs, hL = ydim ? B.hLy : B.hLx, L = ydim ? B.Ly : B.Lx;
+  const int c = ydim ? cy : cx;
+  const bool neg = is_neg(v);
+  double a = (neg ? c : 1 + c) * cs - pos;
+  *dir = (ydim ? 3 : 1) + (neg ? 0 : 1);
+  if (ge_pos(a, hL)) a = a - L;
+  else if (lt_neg(a, hL)) a = a + L;
+  return a / v;
+}
+
+// crossing_time_i with the two divisions on two lanes of a full warp: the
+// lane with (lane & xmask) == 0 takes the x axis of its disk, its partner
+// lane ^ xmask the y axis; both lanes return the disk's crossing
+__device__ __forceinline__ double crossing_time_lanes(const Box& B, const Disk& p, int cx, int cy, double t,
+                                                      int lane, int xmask, int* dir) {
+  const bool ydim = (lane & xmask) != 0;
+  int d;
+  const double ta = axis_time(B, p, cx, cy, ydim, &d);
+  const double tb = __shfl_xor_sync(0xffffffffu, ta, xmask);
+  const int db = __shfl_xor_sync(0xffffffffu, d, xmask);
+  const double tx = ydim ? tb : ta, ty = ydim ? ta : tb;
+  const bool ux = lt_i(tx, ty);
+  *dir = ux ? (ydim ? db : d) : (ydim ? d : db);
+  return t + (ux ? tx : ty);
 }
 
 // (int)(dt / dtP) of addEventToQueue without the FP64 division when provably
@@ -308,7 +352,9 @@ __device__ __forceinline__ int bucket_offset(double dt, double dtP, double rdtP)
   double q = dt * rdtP;
   int d = (int)q;
   double fr = q - (double)d;
-  if (fr > 1e-9 && fr < 1.0 - 1e-9) return d;
+  // fr >= +0, so its bits order like its value
+  const long long fb = __double_as_longlong(fr);
+  if (fb > __double_as_longlong(1e-9) && fb < __double_as_longlong(1.0 - 1e-9)) return d;
   return (int)(dt / dtP);
 }
 

@@ -453,18 +453,26 @@ __device__ __noinline__ void do_growstop(const SysDev& S, SysState& R, int lane,
 
 // ---------------------------------------------------------------- run loop
 
+// the four virial sums live on lanes 0..3 (lane l accumulates term l % 4)
+// during the event loop; every lane gets all four back here
+__device__ __forceinline__ void gather_virial(SysState& R, double ctl) {
+#pragma unroll
+  for (int k = 0; k < 4; k++) R.collT[k] = __shfl_sync(FULL, ctl, k);
+}
+
 __device__ void run_system(const SysDev& S, const RunArgs& A, int64_t max_coll, int lane, WarpSmem* sm) {
   const Box& B = S.B;
   const int N = B.N;
   SysState R = *S.st;
   if (R.status != EDMD_OK) return;
+  double ctl = R.collT[lane & 3];      // this lane's virial term, see gather_virial
   const int root = S.lev_off[S.nlev - 1];
   int64_t logged = 0, nev = 0;
   int stop = 0, status = EDMD_OK;
   bool ovl = false;
   int oa = -1, ob = -1;
   for (;;) {
-    if (!(R.t <= S.tmax)) { stop = EDMD_STOP_TMAX; break; }
+    if (!le_i(R.t, S.tmax)) { stop = EDMD_STOP_TMAX; break; }
     if (logged >= max_coll) { stop = EDMD_STOP_COLL; break; }
     if (nev >= A.max_events) { status = EDMD_ERR_BUDGET; break; }
     Node r;
@@ -491,7 +499,7 @@ __device__ void run_system(const SysDev& S, const RunArgs& A, int64_t max_coll, 
       e = 2 * N + (leaf - N);
     }
     Ev E = S.ev[e];
-    if (E.t >= A.t_stop) { stop = EDMD_STOP_TIME; break; }
+    if (le_i(A.t_stop, E.t)) { stop = EDMD_STOP_TIME; break; }
     R.t = E.t;
     nev++;
     R.nevents++;
@@ -531,17 +539,20 @@ __device__ void run_system(const SysDev& S, const RunArgs& A, int64_t max_coll, 
         double dvx = dj.vx - di.vx, dvy = dj.vy - di.vy;
         if (!grow) {   // elastic branch src/EDMD.c:3802-3827
           // 1/(1+1) and x/4 are exact, so these shortcuts round identically
+          // (== 2.0 and == 4.0 as bit compares, on the integer pipe)
           double msum = di.m + dj.m;
-          double invMass = msum == 2.0 ? 0.5 : 1 / msum;
+          double invMass = __double_as_longlong(msum) == 0x4000000000000000ll ? 0.5 : 1 / msum;
           pbc_i(B, dx, dy);
           double collKernel = invMass * (1 + S.res) * (dx * dvx + dy * dvy);
           double distSquared = 4 * di.rad * dj.rad;
-          double f = distSquared == 4.0 ? collKernel * 0.25 : collKernel / distSquared;
+          double f = __double_as_longlong(distSquared) == 0x4010000000000000ll ? collKernel * 0.25
+                                                                                : collKernel / distSquared;
           double ct = di.m * dj.m * f;
-          R.collT[0] += ct * dx * dx;
-          R.collT[1] += ct * dy * dy;
-          R.collT[2] += ct * dx * dy;
-          R.collT[3] += ct * dy * dx;
+          // collTermX, Y, XY, YX: term lane % 4 on each lane, in shared instructions
+          {
+            const int q = lane & 3;
+            ctl += ct * ((q & 1) ? dy : dx) * ((q == 0 || q == 3) ? dx : dy);
+          }
           if ((A.flags & EDMD_F_LOG) && S.log && (int64_t)R.nlog < S.log_cap && lane == 0) {
             edmd_log_entry* lg = (edmd_log_entry*)S.log + R.nlog;
             lg->i = i; lg->j = j; lg->t = R.t; lg->dx = dx; lg->dy = dy;
@@ -583,7 +594,7 @@ __device__ void run_system(const SysDev& S, const RunArgs& A, int64_t max_coll, 
           const bool odd = lane & 1;
           const int k = odd ? j : i;
           int dir;
-          const double tc = crossing_time_i(B, odd ? dj : di, S.cx[k], S.cy[k], R.t, &dir);
+          const double tc = crossing_time_lanes(B, odd ? dj : di, S.cx[k], S.cy[k], R.t, lane, 2, &dir);
           tci = __shfl_sync(FULL, tc, 0); tcj = __shfl_sync(FULL, tc, 1);
           diri = __shfl_sync(FULL, dir, 0); dirj = __shfl_sync(FULL, dir, 1);
         }
@@ -633,7 +644,7 @@ __device__ void run_system(const SysDev& S, const RunArgs& A, int64_t max_coll, 
       }
       __syncwarp();
       int dir;
-      double tc = crossing_time_i(B, di, cx, cy, R.t, &dir);
+      double tc = crossing_time_lanes(B, di, cx, cy, R.t, lane, 1, &dir);
       schedule(S, R, i, tc, dir, 0, 2ull, lane);
       unqueue(S, R, N + i, lane);
       __syncwarp();
@@ -655,7 +666,9 @@ __device__ void run_system(const SysDev& S, const RunArgs& A, int64_t max_coll, 
       leaf_update(S, N + SP_SCREEN, lane);
       if (A.flags & EDMD_F_STOP_AT_SCREEN) { stop = EDMD_STOP_SCREEN; }
     } else if (e == 2 * N + SP_THERMO) {
+      gather_virial(R, ctl);
       do_thermo(S, R, lane);
+      ctl = R.collT[lane & 3];
       schedule(S, R, e, R.t + S.dtimeTh, 0, 0, 2ull, lane);
       __syncwarp();
       leaf_update(S, N + SP_THERMO, lane);
@@ -666,6 +679,7 @@ __device__ void run_system(const SysDev& S, const RunArgs& A, int64_t max_coll, 
     if (ovl) { status = EDMD_ERR_OVERLAP; break; }
     if (stop) break;
   }
+  gather_virial(R, ctl);
   R.stop_reason = stop;
   R.status = status;
   if (ovl) { R.err_a = oa; R.err_b = ob; }

@@ -302,7 +302,7 @@ __device__ void lane_run(const SysDev& S, const RunArgs& A) {
   int64_t logged = 0, nev = 0;
   int stop = 0;
   for (;;) {
-    if (!(R.t <= S.tmax)) { stop = EDMD_STOP_TMAX; break; }
+    if (!le_i(R.t, S.tmax)) { stop = EDMD_STOP_TMAX; break; }
     if (logged >= A.max_coll) { stop = EDMD_STOP_COLL; break; }
     if (nev >= A.max_events) { W.status = EDMD_ERR_BUDGET; break; }
     // ---- findNextEvent: advance over empty buckets, wrapping as addNextPaulEvent
@@ -337,7 +337,7 @@ __device__ void lane_run(const SysDev& S, const RunArgs& A) {
       if (e < 0 || ft < bt || (ft == bt && fk < bk)) { e = f; bt = ft; bk = fk; }
     }
     Ev E = S.ev[e];
-    if (E.t >= A.t_stop) { stop = EDMD_STOP_TIME; break; }
+    if (le_i(A.t_stop, E.t)) { stop = EDMD_STOP_TIME; break; }
     R.t = E.t;
     nev++;
     R.nevents++;
@@ -394,11 +394,12 @@ __device__ void lane_run(const SysDev& S, const RunArgs& A) {
       if (!grow) {   // elastic branch src/EDMD.c:3802-3827
         // 1/(1+1) and x/4 are exact, so the shortcuts below round identically
         double msum = Da.m + Db.m;
-        double invMass = msum == 2.0 ? 0.5 : 1 / msum;
+        double invMass = __double_as_longlong(msum) == 0x4000000000000000ll ? 0.5 : 1 / msum;
         pbc(B, dx, dy);
         double collKernel = invMass * (1 + S.res) * (dx * dvx + dy * dvy);
         double distSquared = 4 * Da.rad * Db.rad;
-        double f = distSquared == 4.0 ? collKernel * 0.25 : collKernel / distSquared;
+        double f = __double_as_longlong(distSquared) == 0x4010000000000000ll
+            ? collKernel * 0.25 : collKernel / distSquared;
         double ct = Da.m * Db.m * f;
         R.collT[0] += ct * dx * dx;
         R.collT[1] += ct * dy * dy;

@@ -657,11 +657,12 @@ __device__ void process_event_warp(const SysDev& S, const RoundArgs& A, int s, i
         double dx = Db.x - Da.x, dy = Db.y - Da.y;
         const double dvx = Db.vx - Da.vx, dvy = Db.vy - Da.vy;
         const double msum = Da.m + Db.m;
-        const double invMass = msum == 2.0 ? 0.5 : 1 / msum;
+        const double invMass = __double_as_longlong(msum) == 0x4000000000000000ll ? 0.5 : 1 / msum;
         pbc_i(B, dx, dy);
         const double collKernel = invMass * (1 + S.res) * (dx * dvx + dy * dvy);
         const double distSquared = 4 * Da.rad * Db.rad;
-        const double f = distSquared == 4.0 ? collKernel * 0.25 : collKernel / distSquared;
+        const double f = __double_as_longlong(distSquared) == 0x4010000000000000ll
+            ? collKernel * 0.25 : collKernel / distSquared;
         const double cf = Da.m * Db.m * f;
         // virial term q on lane q: collTermX, Y, XY, YX
         {
@@ -682,7 +683,7 @@ __device__ void process_event_warp(const SysDev& S, const RoundArgs& A, int s, i
         Db.vy = __shfl_sync(FULLM, M.vy, 1);
         // next crossing of each disk on its own lanes
         int mdir;
-        const double mtc = crossing_time_i(B, M, odd ? bx : ax, odd ? by : ay, t, &mdir);
+        const double mtc = crossing_time_lanes(B, M, odd ? bx : ax, odd ? by : ay, t, lane, 2, &mdir);
         const double tca = __shfl_sync(FULLM, mtc, 0), tcb = __shfl_sync(FULLM, mtc, 1);
         const int dira = __shfl_sync(FULLM, mdir, 0), dirb = __shfl_sync(FULLM, mdir, 1);
         __syncwarp();
@@ -755,9 +756,9 @@ __device__ void process_event_warp(const SysDev& S, const RoundArgs& A, int s, i
       predict_warp(S, a, Da, cx, cy, -1, Da, cx, cy, t, p0, p1, W, lane, &npair, &ovl, &ob);
       npred = 1;
       ncross = 1;
+      int dir;
+      const double tc = crossing_time_lanes(B, Da, cx, cy, t, lane, 1, &dir);
       if (lane == 0) {
-        int dir;
-        const double tc = crossing_time_i(B, Da, cx, cy, t, &dir);
         set_event(S, a, tc, dir, 0, 0, clk);
         set_event(S, N + a, t + p0.dt, p0.partner, p0.ca, p0.pcell, clk);
         A.drank[g] = 2;
@@ -907,11 +908,12 @@ __device__ void process_event_thread(const SysDev& S, const RoundArgs& A, int s,
       double dx = Db.x - Da.x, dy = Db.y - Da.y;
       const double dvx = Db.vx - Da.vx, dvy = Db.vy - Da.vy;
       const double msum = Da.m + Db.m;
-      const double invMass = msum == 2.0 ? 0.5 : 1 / msum;
+      const double invMass = __double_as_longlong(msum) == 0x4000000000000000ll ? 0.5 : 1 / msum;
       pbc_i(B, dx, dy);
       const double collKernel = invMass * (1 + S.res) * (dx * dvx + dy * dvy);
       const double distSquared = 4 * Da.rad * Db.rad;
-      const double f = distSquared == 4.0 ? collKernel * 0.25 : collKernel / distSquared;
+      const double f = __double_as_longlong(distSquared) == 0x4010000000000000ll
+          ? collKernel * 0.25 : collKernel / distSquared;
       const double cf = Da.m * Db.m * f;
       ct4[0] = cf * dx * dx;
       ct4[1] = cf * dy * dy;
