@@ -347,14 +347,30 @@ __device__ __forceinline__ double crossing_time_lanes(const Box& B, const Disk& 
 
 // (int)(dt / dtP) of addEventToQueue without the FP64 division when provably
 // equal: |dt*rdtP - fl(dt/dtP)| <= 3*q*2^-53 < 1e-9 for q < 2^22, so the floor
-// is unchanged unless q is within 1e-9 of an integer (then divide exactly)
+// is unchanged unless q is within 1e-9 of an integer (then divide exactly).
+// floor(q) and the exact fraction q - floor(q) are read from the bits of q
+// (integer pipe): with q = mant * 2^-shift, floor = mant >> shift and the
+// fraction is frac * 2^-shift, frac = the low shift bits; fraction > 1e-9
+// and fraction < 1 - 1e-9 become integer compares of frac with the
+// constants' mantissas scaled by the same power of two.
 __device__ __forceinline__ int bucket_offset(double dt, double dtP, double rdtP) {
-  double q = dt * rdtP;
-  int d = (int)q;
-  double fr = q - (double)d;
-  // fr >= +0, so its bits order like its value
-  const long long fb = __double_as_longlong(fr);
-  if (fb > __double_as_longlong(1e-9) && fb < __double_as_longlong(1.0 - 1e-9)) return d;
+  const double q = dt * rdtP;
+  const unsigned long long u = (unsigned long long)__double_as_longlong(q);
+  const unsigned long long c1 = (unsigned long long)__double_as_longlong(1e-9);
+  const unsigned long long c2 = (unsigned long long)__double_as_longlong(1.0 - 1e-9);
+  const int e = (int)((u >> 52) & 0x7ff) - 1023;
+  if (e < 0) {                        // q < 1: floor 0, fraction q (q >= 0)
+    if (u > c1 && u < c2) return 0;
+  } else if (e <= 30) {
+    const int shift = 52 - e;
+    const unsigned long long M = 0xfffffffffffffull, H = 1ull << 52;
+    const unsigned long long mant = (u & M) | H;
+    const unsigned long long frac = mant & ((1ull << shift) - 1);
+    // 1e-9 = M1 * 2^-82 and 1 - 1e-9 = M2 * 2^-53 (exponents -30 and -1)
+    const unsigned long long M1 = (c1 & M) | H, M2 = (c2 & M) | H;
+    const int k1 = 30 + e, k2 = 1 + e;
+    if (frac > (M1 >> k1) && frac < ((M2 + (1ull << k2) - 1) >> k2)) return (int)(mant >> shift);
+  }
   return (int)(dt / dtP);
 }
 

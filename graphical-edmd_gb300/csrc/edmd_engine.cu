@@ -47,6 +47,8 @@ struct WarpSmem {
   int32_t reg[32 * MAXC];        // per-lane walk buffers
   int32_t comp[2 * 9 * MAXC];    // packed candidates
   int16_t ord[2 * 9 * MAXC];     // their scan order
+  long long msum[2];             // last two mass sums of the collision rule (bits) ...
+  double inv[2];                 // ... and 1 / msum, the same division's result
 };
 
 __device__ __forceinline__ Node empty_node(int idx) {
@@ -132,17 +134,26 @@ __device__ __noinline__ void tree_rebuild(const SysDev& S, int lane) {
 
 // ---------------------------------------------------------------- queue
 
-// addEventToQueue (src/EDMD.c:2144) in key form.  `cls_direct` is 2 for a
-// schedule from an event handler and 0 for the re-add done by a wrap.
-__device__ void schedule(const SysDev& S, SysState& R, int e, double T, int32_t j, uint32_t ca,
-                         uint64_t cls_direct, int lane) {
+// addEventToQueue (src/EDMD.c:2144) in key form, in two parts: where the
+// event goes (FP64: its offset from paulTime; -1 current bucket, -2
+// overflow, else the bucket offset), and the insertion (integer work).
+__device__ __forceinline__ int sched_place(const SysDev& S, const SysState& R, double T) {
   const Box& B = S.B;
+  const double dt = T - R.P;
+  if (!ge_pos(dt, B.dtP)) return -1;           // dt < dtPaul
+  if (ge_pos(dt, B.dtPN)) return -2;           // dt >= dtPaul * N
+  return bucket_offset(dt, B.dtP, S.rdtP);
+}
+
+// `cls_direct` is 2 for a schedule from an event handler and 0 for the
+// re-add done by a wrap
+__device__ __forceinline__ void sched_insert(const SysDev& S, SysState& R, int e, double T, int32_t j,
+                                             uint32_t ca, uint64_t cls_direct, int place, int lane) {
   Ev ev;
   ev.t = T; ev.j = j; ev.ca = ca;
-  double dt = T - R.P;
-  if (!ge_pos(dt, B.dtP)) {                    // dt < dtPaul
+  if (place == -1) {
     ev.b = (uint32_t)R.k; ev.tie = (cls_direct << 62) | R.C; ev.st = ST_QUEUED;
-  } else if (ge_pos(dt, B.dtPN)) {             // dt >= dtPaul * N
+  } else if (place == -2) {
     ev.b = BINF; ev.tie = R.C; ev.st = ST_OVF;
     if (lane == 0) {
       S.on[e] = R.ovf; S.op[e] = NIL;
@@ -150,12 +161,26 @@ __device__ void schedule(const SysDev& S, SysState& R, int e, double T, int32_t 
     }
     R.ovf = e;
   } else {
-    int d = bucket_offset(dt, B.dtP, S.rdtP);
-    ev.b = (uint32_t)(R.k + (uint64_t)d); ev.tie = (1ull << 62) | (TIE_MAX - R.C); ev.st = ST_QUEUED;
+    ev.b = (uint32_t)(R.k + (uint64_t)place); ev.tie = (1ull << 62) | (TIE_MAX - R.C); ev.st = ST_QUEUED;
   }
   R.C++;
   if (lane == 0) S.ev[e] = ev;
   __syncwarp();
+}
+
+__device__ void schedule(const SysDev& S, SysState& R, int e, double T, int32_t j, uint32_t ca,
+                         uint64_t cls_direct, int lane) {
+  sched_insert(S, R, e, T, j, ca, cls_direct, sched_place(S, R, T), lane);
+}
+
+// two handler schedules in a row (e0 first): the FP64 placement of e0 on even
+// lanes and of e1 on odd lanes in shared instructions, then both insertions
+__device__ void schedule2(const SysDev& S, SysState& R, int e0, double T0, int32_t j0, uint32_t ca0,
+                          int e1, double T1, int32_t j1, uint32_t ca1, int lane) {
+  const int pl = sched_place(S, R, (lane & 1) ? T1 : T0);
+  const int p0 = __shfl_sync(FULL, pl, 0), p1 = __shfl_sync(FULL, pl, 1);
+  sched_insert(S, R, e0, T0, j0, ca0, 2ull, p0, lane);
+  sched_insert(S, R, e1, T1, j1, ca1, 2ull, p1, lane);
 }
 
 // removeEventFromQueue (src/EDMD.c:2209) in key form
@@ -466,6 +491,8 @@ __device__ void run_system(const SysDev& S, const RunArgs& A, int64_t max_coll, 
   SysState R = *S.st;
   if (R.status != EDMD_OK) return;
   double ctl = R.collT[lane & 3];      // this lane's virial term, see gather_virial
+  if (lane == 0) { sm->msum[0] = sm->msum[1] = 0; }   // no mass sum is +0
+  __syncwarp();
   const int root = S.lev_off[S.nlev - 1];
   int64_t logged = 0, nev = 0;
   int stop = 0, status = EDMD_OK;
@@ -540,8 +567,23 @@ __device__ void run_system(const SysDev& S, const RunArgs& A, int64_t max_coll, 
         if (!grow) {   // elastic branch src/EDMD.c:3802-3827
           // 1/(1+1) and x/4 are exact, so these shortcuts round identically
           // (== 2.0 and == 4.0 as bit compares, on the integer pipe)
+          // 1 / msum repeats for the few mass pairs of a system: the last two
+          // results are kept (a bit-identical value, without the division)
           double msum = di.m + dj.m;
-          double invMass = __double_as_longlong(msum) == 0x4000000000000000ll ? 0.5 : 1 / msum;
+          const long long mk = __double_as_longlong(msum);
+          double invMass;
+          if (mk == 0x4000000000000000ll) invMass = 0.5;
+          else if (mk == sm->msum[0]) invMass = sm->inv[0];
+          else if (mk == sm->msum[1]) invMass = sm->inv[1];
+          else {
+            invMass = 1 / msum;
+            __syncwarp();
+            if (lane == 0) {
+              sm->msum[1] = sm->msum[0]; sm->inv[1] = sm->inv[0];
+              sm->msum[0] = mk; sm->inv[0] = invMass;
+            }
+            __syncwarp();
+          }
           pbc_i(B, dx, dy);
           double collKernel = invMass * (1 + S.res) * (dx * dvx + dy * dvy);
           double distSquared = 4 * di.rad * dj.rad;
@@ -598,13 +640,15 @@ __device__ void run_system(const SysDev& S, const RunArgs& A, int64_t max_coll, 
           tci = __shfl_sync(FULL, tc, 0); tcj = __shfl_sync(FULL, tc, 1);
           diri = __shfl_sync(FULL, dir, 0); dirj = __shfl_sync(FULL, dir, 1);
         }
-        schedule(S, R, i, tci, diri, 0, 2ull, lane);
-        schedule(S, R, j, tcj, dirj, 0, 2ull, lane);
+        schedule2(S, R, i, tci, diri, 0, j, tcj, dirj, 0, lane);
         unqueue(S, R, N + j, lane);
         Pred r0, r1;
         predict2(S, R, i, j, r0, r1, lane, sm, &ovl, &oa, &ob);
-        schedule(S, R, N + i, R.t + r0.dt, r0.partner, r0.ca, 2ull, lane);
-        schedule(S, R, N + j, R.t + r1.dt, r1.partner, r1.ca, 2ull, lane);
+        {
+          const double tn = R.t + ((lane & 1) ? r1.dt : r0.dt);
+          schedule2(S, R, N + i, __shfl_sync(FULL, tn, 0), r0.partner, r0.ca,
+                    N + j, __shfl_sync(FULL, tn, 1), r1.partner, r1.ca, lane);
+        }
         __syncwarp();
         leaf_update(S, i, lane);
         leaf_update(S, j, lane);
