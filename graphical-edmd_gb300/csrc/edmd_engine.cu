@@ -533,6 +533,7 @@ __device__ void run_system(const SysDev& S, const RunArgs& A, int64_t max_coll, 
     if (lane == 0) S.ev[e].st = ST_NONE;
     __syncwarp();
     const bool grow = R.grow != 0;
+    int pa = -1, pb = -1;              // disks whose collision events are predicted below
     if (e >= N && e < 2 * N) {
       // ---------------- collision (doTheCollisionNormal 3542 / Grow 3465)
       const int i = e - N, j = E.j;
@@ -543,11 +544,7 @@ __device__ void run_system(const SysDev& S, const RunArgs& A, int64_t max_coll, 
         if (lane == 0) S.d[i] = di;
         __syncwarp();
         R.nstale++;
-        Pred r0, r1;
-        predict2(S, R, i, -1, r0, r1, lane, sm, &ovl, &oa, &ob);
-        schedule(S, R, N + i, R.t + r0.dt, r0.partner, r0.ca, 2ull, lane);
-        __syncwarp();
-        leaf_update(S, i, lane);
+        pa = i;
       } else {
         const int ci = S.cy[i] * B.Nxc + S.cx[i];
         const int cj = S.cy[j] * B.Nxc + S.cx[j];
@@ -642,16 +639,8 @@ __device__ void run_system(const SysDev& S, const RunArgs& A, int64_t max_coll, 
         }
         schedule2(S, R, i, tci, diri, 0, j, tcj, dirj, 0, lane);
         unqueue(S, R, N + j, lane);
-        Pred r0, r1;
-        predict2(S, R, i, j, r0, r1, lane, sm, &ovl, &oa, &ob);
-        {
-          const double tn = R.t + ((lane & 1) ? r1.dt : r0.dt);
-          schedule2(S, R, N + i, __shfl_sync(FULL, tn, 0), r0.partner, r0.ca,
-                    N + j, __shfl_sync(FULL, tn, 1), r1.partner, r1.ca, lane);
-        }
-        __syncwarp();
-        leaf_update(S, i, lane);
-        leaf_update(S, j, lane);
+        pa = i;
+        pb = j;
       }
     } else if (e < N) {
       // ---------------- cell crossing (doTheCrossing 2501)
@@ -692,11 +681,7 @@ __device__ void run_system(const SysDev& S, const RunArgs& A, int64_t max_coll, 
       schedule(S, R, i, tc, dir, 0, 2ull, lane);
       unqueue(S, R, N + i, lane);
       __syncwarp();
-      Pred r0, r1;
-      predict2(S, R, i, -1, r0, r1, lane, sm, &ovl, &oa, &ob);
-      schedule(S, R, N + i, R.t + r0.dt, r0.partner, r0.ca, 2ull, lane);
-      __syncwarp();
-      leaf_update(S, i, lane);
+      pa = i;
     } else if (e == 2 * N + SP_SCREEN) {
       // ---------------- screenshot (takeAScreenshot 4657): free-fly everything
       for (int i = lane; i < N; i += 32) {
@@ -719,6 +704,23 @@ __device__ void run_system(const SysDev& S, const RunArgs& A, int64_t max_coll, 
     } else {
       do_growstop(S, R, lane, sm, &ovl, &oa, &ob);
       if (A.flags & EDMD_F_STOP_AT_GROW) stop = EDMD_STOP_GROW;
+    }
+    if (pa >= 0) {
+      // the tail shared by the collision, stale-collision and crossing
+      // handlers: new collision events of the one or two disks that changed
+      // (collisionEvent for i, then j), their insertion, and the tree paths
+      Pred r0, r1;
+      predict2(S, R, pa, pb, r0, r1, lane, sm, &ovl, &oa, &ob);
+      if (pb >= 0) {
+        const double tn = R.t + ((lane & 1) ? r1.dt : r0.dt);
+        schedule2(S, R, N + pa, __shfl_sync(FULL, tn, 0), r0.partner, r0.ca,
+                  N + pb, __shfl_sync(FULL, tn, 1), r1.partner, r1.ca, lane);
+      } else {
+        schedule(S, R, N + pa, R.t + r0.dt, r0.partner, r0.ca, 2ull, lane);
+      }
+      __syncwarp();
+      leaf_update(S, pa, lane);
+      if (pb >= 0) leaf_update(S, pb, lane);
     }
     if (ovl) { status = EDMD_ERR_OVERLAP; break; }
     if (stop) break;
