@@ -173,14 +173,15 @@ __device__ void schedule(const SysDev& S, SysState& R, int e, double T, int32_t 
   sched_insert(S, R, e, T, j, ca, cls_direct, sched_place(S, R, T), lane);
 }
 
-// two handler schedules in a row (e0 first): the FP64 placement of e0 on even
-// lanes and of e1 on odd lanes in shared instructions, then both insertions
+// one or two handler schedules in a row (e0 first; e1 < 0: none): the FP64
+// placement of e0 on even lanes and of e1 on odd lanes in shared
+// instructions, then the insertions
 __device__ void schedule2(const SysDev& S, SysState& R, int e0, double T0, int32_t j0, uint32_t ca0,
                           int e1, double T1, int32_t j1, uint32_t ca1, int lane) {
-  const int pl = sched_place(S, R, (lane & 1) ? T1 : T0);
+  const int pl = sched_place(S, R, (lane & 1) && e1 >= 0 ? T1 : T0);
   const int p0 = __shfl_sync(FULL, pl, 0), p1 = __shfl_sync(FULL, pl, 1);
   sched_insert(S, R, e0, T0, j0, ca0, 2ull, p0, lane);
-  sched_insert(S, R, e1, T1, j1, ca1, 2ull, p1, lane);
+  if (e1 >= 0) sched_insert(S, R, e1, T1, j1, ca1, 2ull, p1, lane);
 }
 
 // removeEventFromQueue (src/EDMD.c:2209) in key form
@@ -533,7 +534,13 @@ __device__ void run_system(const SysDev& S, const RunArgs& A, int64_t max_coll, 
     if (lane == 0) S.ev[e].st = ST_NONE;
     __syncwarp();
     const bool grow = R.grow != 0;
+    int ka = -1, kb = -1, uq = -1;     // disks whose crossing events are scheduled below, event removed
     int pa = -1, pb = -1;              // disks whose collision events are predicted below
+    int se0 = -1, se1 = -1;            // events inserted below, their times, partners, counters
+    double sT0 = 0, sT1 = 0;
+    int32_t sj0 = 0, sj1 = 0;
+    uint32_t sca0 = 0, sca1 = 0;
+    int la = -1, lb = -1;              // leaves whose tree paths are updated below
     if (e >= N && e < 2 * N) {
       // ---------------- collision (doTheCollisionNormal 3542 / Grow 3465)
       const int i = e - N, j = E.j;
@@ -626,19 +633,7 @@ __device__ void run_system(const SysDev& S, const RunArgs& A, int64_t max_coll, 
         __syncwarp();
         unqueue(S, R, i, lane);
         unqueue(S, R, j, lane);
-        int diri, dirj;
-        double tci, tcj;
-        {
-          // next crossings of i (even lanes) and j (odd lanes) in shared instructions
-          const bool odd = lane & 1;
-          const int k = odd ? j : i;
-          int dir;
-          const double tc = crossing_time_lanes(B, odd ? dj : di, S.cx[k], S.cy[k], R.t, lane, 2, &dir);
-          tci = __shfl_sync(FULL, tc, 0); tcj = __shfl_sync(FULL, tc, 1);
-          diri = __shfl_sync(FULL, dir, 0); dirj = __shfl_sync(FULL, dir, 1);
-        }
-        schedule2(S, R, i, tci, diri, 0, j, tcj, dirj, 0, lane);
-        unqueue(S, R, N + j, lane);
+        ka = i; kb = j; uq = N + j;
         pa = i;
         pb = j;
       }
@@ -676,11 +671,7 @@ __device__ void run_system(const SysDev& S, const RunArgs& A, int64_t max_coll, 
         if (h != NIL) S.prv[h] = i;
       }
       __syncwarp();
-      int dir;
-      double tc = crossing_time_lanes(B, di, cx, cy, R.t, lane, 1, &dir);
-      schedule(S, R, i, tc, dir, 0, 2ull, lane);
-      unqueue(S, R, N + i, lane);
-      __syncwarp();
+      ka = i; uq = N + i;
       pa = i;
     } else if (e == 2 * N + SP_SCREEN) {
       // ---------------- screenshot (takeAScreenshot 4657): free-fly everything
@@ -690,37 +681,48 @@ __device__ void run_system(const SysDev& S, const RunArgs& A, int64_t max_coll, 
         S.d[i] = p;
       }
       __syncwarp();
-      schedule(S, R, e, R.t + S.dtime, 0, 0, 2ull, lane);
-      __syncwarp();
-      leaf_update(S, N + SP_SCREEN, lane);
+      se0 = e; sT0 = R.t + S.dtime;
+      la = N + SP_SCREEN;
       if (A.flags & EDMD_F_STOP_AT_SCREEN) { stop = EDMD_STOP_SCREEN; }
     } else if (e == 2 * N + SP_THERMO) {
       gather_virial(R, ctl);
       do_thermo(S, R, lane);
       ctl = R.collT[lane & 3];
-      schedule(S, R, e, R.t + S.dtimeTh, 0, 0, 2ull, lane);
-      __syncwarp();
-      leaf_update(S, N + SP_THERMO, lane);
+      se0 = e; sT0 = R.t + S.dtimeTh;
+      la = N + SP_THERMO;
     } else {
       do_growstop(S, R, lane, sm, &ovl, &oa, &ob);
       if (A.flags & EDMD_F_STOP_AT_GROW) stop = EDMD_STOP_GROW;
     }
+    // the tail shared by the handlers: new crossing events of the one or two
+    // disks that changed (crossingEvent for i, then j; even lanes take i,
+    // odd lanes j), the removal of the collision event they replace, new
+    // collision events (collisionEvent for i, then j), the insertion of the
+    // handler's new events, and the tree paths of the changed leaves
+    if (ka >= 0) {
+      const int k = (lane & 1) && kb >= 0 ? kb : ka;
+      const Disk dk = S.d[k];
+      int dir;
+      const double tc = crossing_time_lanes(B, dk, S.cx[k], S.cy[k], R.t, lane, 2, &dir);
+      schedule2(S, R, ka, __shfl_sync(FULL, tc, 0), __shfl_sync(FULL, dir, 0), 0,
+                kb, __shfl_sync(FULL, tc, 1), __shfl_sync(FULL, dir, 1), 0, lane);
+      unqueue(S, R, uq, lane);
+    }
     if (pa >= 0) {
-      // the tail shared by the collision, stale-collision and crossing
-      // handlers: new collision events of the one or two disks that changed
-      // (collisionEvent for i, then j), their insertion, and the tree paths
       Pred r0, r1;
       predict2(S, R, pa, pb, r0, r1, lane, sm, &ovl, &oa, &ob);
-      if (pb >= 0) {
-        const double tn = R.t + ((lane & 1) ? r1.dt : r0.dt);
-        schedule2(S, R, N + pa, __shfl_sync(FULL, tn, 0), r0.partner, r0.ca,
-                  N + pb, __shfl_sync(FULL, tn, 1), r1.partner, r1.ca, lane);
-      } else {
-        schedule(S, R, N + pa, R.t + r0.dt, r0.partner, r0.ca, 2ull, lane);
-      }
-      __syncwarp();
-      leaf_update(S, pa, lane);
-      if (pb >= 0) leaf_update(S, pb, lane);
+      const double tn = R.t + ((lane & 1) ? r1.dt : r0.dt);
+      se0 = N + pa; sT0 = __shfl_sync(FULL, tn, 0); sj0 = r0.partner; sca0 = r0.ca;
+      if (pb >= 0) { se1 = N + pb; sT1 = __shfl_sync(FULL, tn, 1); sj1 = r1.partner; sca1 = r1.ca; }
+      la = pa;
+      lb = pb;
+    }
+    if (se0 >= 0) schedule2(S, R, se0, sT0, sj0, sca0, se1, sT1, sj1, sca1, lane);
+    __syncwarp();
+    for (int q = 0; q < 2; q++) {
+      const int lf = q ? lb : la;
+      if (lf < 0) break;
+      leaf_update(S, lf, lane);
     }
     if (ovl) { status = EDMD_ERR_OVERLAP; break; }
     if (stop) break;
