@@ -618,9 +618,17 @@ __device__ void process_event_warp(const SysDev& S, const RoundArgs& A, int s, i
     double ct[1] = {0};
     bool ovl = false, bad = false;
     int ob = -1;
+    // what the shared tail does, set by the handler: the second disk of a
+    // collision, the cells of the disks, the cells stamped as written and
+    // the centres of the 3x3 blocks stamped as read, new crossing events
+    int b = -1;
+    int64_t gb = -1;
+    int pax = ax, pay = ay, pbx = ax, pby = ay;
+    int wc1 = -1, rc0 = ca, rc1 = -1;
+    bool cross = false;
+    Disk Db = Da;
     if (slot >= N) {
-      const int b = E.j;
-      Disk Db = S.d[b];
+      Db = S.d[E.j];
       if (E.ca != Db.coll) {
         free_fly_i(B, Da, t);
         __syncwarp();
@@ -628,20 +636,10 @@ __device__ void process_event_warp(const SysDev& S, const RoundArgs& A, int s, i
           S.d[a] = Da;
           shadow_write(A, g, B, Da, ax, ay, A.epoch[s]);
         }
-        bad |= lane == 0 && stamp_write(A, base, ca, clk);
-        bad |= stamp_read_warp(B, A, base, ca, clk, lane, 0);
-        __syncwarp();
-        Pred p0, p1;
-        predict_warp(S, a, Da, ax, ay, -1, Da, ax, ay, t, p0, p1, W, lane, &npair, &ovl, &ob);
-        npred = 1;
         nstale = 1;
-        if (lane == 0) {
-          set_event(S, N + a, t + p0.dt, p0.partner, p0.ca, p0.pcell, clk);
-          A.drank[g] = 2;
-          reattribute(S, A, a, g, base, dc, &nd);
-        }
       } else {
-        const int64_t gb = dbase + b;
+        b = E.j;
+        gb = dbase + b;
         dc[nd++] = (int32_t)(base + A.fc[2 * gb]);
         if (A.fc[2 * gb + 1] != A.fc[2 * gb]) dc[nd++] = (int32_t)(base + A.fc[2 * gb + 1]);
         const int bx = S.cx[b], by = S.cy[b];
@@ -681,11 +679,6 @@ __device__ void process_event_warp(const SysDev& S, const RoundArgs& A, int s, i
         Da.vy = __shfl_sync(FULLM, M.vy, 0);
         Db.vx = __shfl_sync(FULLM, M.vx, 1);
         Db.vy = __shfl_sync(FULLM, M.vy, 1);
-        // next crossing of each disk on its own lanes
-        int mdir;
-        const double mtc = crossing_time_lanes(B, M, odd ? bx : ax, odd ? by : ay, t, lane, 2, &mdir);
-        const double tca = __shfl_sync(FULLM, mtc, 0), tcb = __shfl_sync(FULLM, mtc, 1);
-        const int dira = __shfl_sync(FULLM, mdir, 0), dirb = __shfl_sync(FULLM, mdir, 1);
         __syncwarp();
         if (lane == 0) {
           S.d[a] = Da;
@@ -700,24 +693,10 @@ __device__ void process_event_warp(const SysDev& S, const RoundArgs& A, int s, i
             }
           }
         }
-        bad |= lane == 0 && (stamp_write(A, base, ca, clk) | stamp_write(A, base, cb, clk));
-        bad |= stamp_read_warp(B, A, base, ca, clk, lane, 0);
-        bad |= stamp_read_warp(B, A, base, cb, clk, lane, 16);
-        __syncwarp();
-        Pred p0, p1;
-        predict_warp(S, a, Da, ax, ay, b, Db, bx, by, t, p0, p1, W, lane, &npair, &ovl, &ob);
-        npred = 2;
+        pbx = bx; pby = by;
+        wc1 = cb; rc1 = cb;
+        cross = true;
         ncol = 1;
-        if (lane == 0) {
-          set_event(S, a, tca, dira, 0, 0, clk);
-          set_event(S, b, tcb, dirb, 0, 0, clk);
-          set_event(S, N + a, t + p0.dt, p0.partner, p0.ca, p0.pcell, clk);
-          set_event(S, N + b, t + p1.dt, p1.partner, p1.ca, p1.pcell, clk);
-          A.drank[g] = 2;
-          A.drank[gb] = 2;
-          reattribute(S, A, a, g, base, dc, &nd);
-          reattribute(S, A, b, gb, base, dc, &nd);
-        }
       }
     } else {
       free_fly_i(B, Da, t);
@@ -749,21 +728,38 @@ __device__ void process_event_warp(const SysDev& S, const RoundArgs& A, int s, i
         S.head[c] = a;
         if (h != NIL) S.prv[h] = a;
       }
-      bad |= lane == 0 && (stamp_write(A, base, ca, clk) | stamp_write(A, base, c, clk));
-      bad |= stamp_read_warp(B, A, base, c, clk, lane, 0);
-      __syncwarp();
-      Pred p0, p1;
-      predict_warp(S, a, Da, cx, cy, -1, Da, cx, cy, t, p0, p1, W, lane, &npair, &ovl, &ob);
-      npred = 1;
+      pax = cx; pay = cy;
+      wc1 = c; rc0 = c;
+      cross = true;
       ncross = 1;
-      int dir;
-      const double tc = crossing_time_lanes(B, Da, cx, cy, t, lane, 1, &dir);
-      if (lane == 0) {
-        set_event(S, a, tc, dir, 0, 0, clk);
-        set_event(S, N + a, t + p0.dt, p0.partner, p0.ca, p0.pcell, clk);
-        A.drank[g] = 2;
-        reattribute(S, A, a, g, base, dc, &nd);
-      }
+    }
+    // ---- the tail shared by the three handlers: causality stamps, new
+    // crossing events (a on even lanes, b on odd ones), new collision events
+    // (collisionEvent for a, then b), the event records and attribution
+    bad |= lane == 0 && (stamp_write(A, base, ca, clk) | (wc1 >= 0 && stamp_write(A, base, wc1, clk)));
+    bad |= stamp_read_warp(B, A, base, rc0, clk, lane, 0);
+    if (rc1 >= 0) bad |= stamp_read_warp(B, A, base, rc1, clk, lane, 16);
+    __syncwarp();
+    double ctc = 0;
+    int cdir = 0;
+    if (cross) {
+      const bool od = (lane & 1) && b >= 0;
+      ctc = crossing_time_lanes(B, od ? Db : Da, od ? pbx : pax, od ? pby : pay, t, lane, 2, &cdir);
+    }
+    Pred p0, p1;
+    predict_warp(S, a, Da, pax, pay, b, Db, pbx, pby, t, p0, p1, W, lane, &npair, &ovl, &ob);
+    npred = b >= 0 ? 2 : 1;
+    const double tca = __shfl_sync(FULLM, ctc, 0), tcb = __shfl_sync(FULLM, ctc, 1);
+    const int dira = __shfl_sync(FULLM, cdir, 0), dirb = __shfl_sync(FULLM, cdir, 1);
+    if (lane == 0) {
+      if (cross) set_event(S, a, tca, dira, 0, 0, clk);
+      if (b >= 0) set_event(S, b, tcb, dirb, 0, 0, clk);
+      set_event(S, N + a, t + p0.dt, p0.partner, p0.ca, p0.pcell, clk);
+      if (b >= 0) set_event(S, N + b, t + p1.dt, p1.partner, p1.ca, p1.pcell, clk);
+      A.drank[g] = 2;
+      if (b >= 0) A.drank[gb] = 2;
+      reattribute(S, A, a, g, base, dc, &nd);
+      if (b >= 0) reattribute(S, A, b, gb, base, dc, &nd);
     }
     for (int k = 0; k < MAXDIRTY; k++) res.dc[k] = dc[k];
     res.nd = nd;
@@ -877,27 +873,23 @@ __device__ void process_event_thread(const SysDev& S, const RoundArgs& A, int s,
   ct4[0] = ct4[1] = ct4[2] = ct4[3] = 0;
   res.ovl = res.bad = false;
   res.ob = -1;
+  // what the shared tail does, set by the handler (see process_event_warp)
+  int b = -1;
+  int64_t gb = -1;
+  int pax = ax, pay = ay, pbx = ax, pby = ay;
+  int wc1 = -1, rc0 = ca, rc1 = -1;
+  bool cross = false;
+  Disk Db = Da;
   if (slot >= N) {
-    const int b = E.j;
-    Disk Db = S.d[b];
+    Db = S.d[E.j];
     free_fly_i(B, Da, t);
     if (E.ca != Db.coll) {
       S.d[a] = Da;
       shadow_write(A, g, B, Da, ax, ay, A.epoch[s]);
-      res.bad |= stamp_write(A, base, ca, clk);
-      res.bad |= stamp_read_thread(B, A, base, ca, clk);
-      const Pred p0 = predict_thread(S, A, s, a, Da, ax, ay, t, &res.npair, &res.nscreen, &res.ovl, &res.ob);
-      res.npred = 1;
       res.nstale = 1;
-      set_event(S, N + a, t + p0.dt, p0.partner, p0.ca, p0.pcell, clk);
-      A.drank[g] = 2;
-      uint64_t k2; int c1, c2;
-      const int sl = attribution(S, a, &k2, &c1, &c2);
-      A.dkey[g] = k2; A.dpk[g] = event_id(A, g, sl, N); A.fc[2 * g] = c1; A.fc[2 * g + 1] = c2;
-      res.dc[nd++] = (int32_t)(base + c1);
-      if (c2 != c1) res.dc[nd++] = (int32_t)(base + c2);
     } else {
-      const int64_t gb = dbase + b;
+      b = E.j;
+      gb = dbase + b;
       res.dc[nd++] = (int32_t)(base + A.fc[2 * gb]);
       if (A.fc[2 * gb + 1] != A.fc[2 * gb]) res.dc[nd++] = (int32_t)(base + A.fc[2 * gb + 1]);
       const int bx = S.cx[b], by = S.cy[b];
@@ -934,31 +926,10 @@ __device__ void process_event_thread(const SysDev& S, const RoundArgs& A, int s,
           tr->i = a; tr->j = b; tr->cell_i = ca; tr->cell_j = cb; tr->t = t;
         }
       }
-      res.bad |= stamp_write(A, base, ca, clk) | stamp_write(A, base, cb, clk);
-      res.bad |= stamp_read_thread(B, A, base, ca, clk);
-      res.bad |= stamp_read_thread(B, A, base, cb, clk);
-      int dir;
-      double tc = crossing_time_i(B, Da, ax, ay, t, &dir);
-      set_event(S, a, tc, dir, 0, 0, clk);
-      tc = crossing_time_i(B, Db, bx, by, t, &dir);
-      set_event(S, b, tc, dir, 0, 0, clk);
-      const Pred p0 = predict_thread(S, A, s, a, Da, ax, ay, t, &res.npair, &res.nscreen, &res.ovl, &res.ob);
-      const Pred p1 = predict_thread(S, A, s, b, Db, bx, by, t, &res.npair, &res.nscreen, &res.ovl, &res.ob);
-      res.npred = 2;
+      pbx = bx; pby = by;
+      wc1 = cb; rc1 = cb;
+      cross = true;
       res.ncol = 1;
-      set_event(S, N + a, t + p0.dt, p0.partner, p0.ca, p0.pcell, clk);
-      set_event(S, N + b, t + p1.dt, p1.partner, p1.ca, p1.pcell, clk);
-      A.drank[g] = 2;
-      A.drank[gb] = 2;
-      uint64_t k2; int c1, c2;
-      int sl = attribution(S, a, &k2, &c1, &c2);
-      A.dkey[g] = k2; A.dpk[g] = event_id(A, g, sl, N); A.fc[2 * g] = c1; A.fc[2 * g + 1] = c2;
-      res.dc[nd++] = (int32_t)(base + c1);
-      if (c2 != c1) res.dc[nd++] = (int32_t)(base + c2);
-      sl = attribution(S, b, &k2, &c1, &c2);
-      A.dkey[gb] = k2; A.dpk[gb] = event_id(A, gb, sl, N); A.fc[2 * gb] = c1; A.fc[2 * gb + 1] = c2;
-      res.dc[nd++] = (int32_t)(base + c1);
-      if (c2 != c1) res.dc[nd++] = (int32_t)(base + c2);
     }
   } else {
     free_fly_i(B, Da, t);
@@ -983,19 +954,36 @@ __device__ void process_event_thread(const SysDev& S, const RoundArgs& A, int s,
     shadow_write(A, g, B, Da, cx, cy, A.epoch[s]);
     S.head[c] = a;
     if (h != NIL) S.prv[h] = a;
-    res.bad |= stamp_write(A, base, ca, clk) | stamp_write(A, base, c, clk);
-    res.bad |= stamp_read_thread(B, A, base, c, clk);
-    int dir;
-    const double tc = crossing_time_i(B, Da, cx, cy, t, &dir);
-    set_event(S, a, tc, dir, 0, 0, clk);
-    const Pred p0 = predict_thread(S, A, s, a, Da, cx, cy, t, &res.npair, &res.nscreen, &res.ovl, &res.ob);
-    res.npred = 1;
+    pax = cx; pay = cy;
+    wc1 = c; rc0 = c;
+    cross = true;
     res.ncross = 1;
-    set_event(S, N + a, t + p0.dt, p0.partner, p0.ca, p0.pcell, clk);
-    A.drank[g] = 2;
+  }
+  // ---- the tail shared by the three handlers, so that lanes running
+  // different event kinds share its instructions: causality stamps, then per
+  // changed disk (a, then b) its crossing event, its collision event
+  // (collisionEvent), the event records and its attribution
+  res.bad |= stamp_write(A, base, ca, clk) | (wc1 >= 0 && stamp_write(A, base, wc1, clk));
+  res.bad |= stamp_read_thread(B, A, base, rc0, clk);
+  if (rc1 >= 0) res.bad |= stamp_read_thread(B, A, base, rc1, clk);
+  res.npred = b >= 0 ? 2 : 1;
+  for (int q = 0; q < 2; q++) {
+    const int d = q ? b : a;
+    if (d < 0) break;
+    const int64_t gd = q ? gb : g;
+    const Disk Dd = q ? Db : Da;
+    const int X = q ? pbx : pax, Y = q ? pby : pay;
+    if (cross) {
+      int dir;
+      const double tc = crossing_time_i(B, Dd, X, Y, t, &dir);
+      set_event(S, d, tc, dir, 0, 0, clk);
+    }
+    const Pred pr = predict_thread(S, A, s, d, Dd, X, Y, t, &res.npair, &res.nscreen, &res.ovl, &res.ob);
+    set_event(S, N + d, t + pr.dt, pr.partner, pr.ca, pr.pcell, clk);
+    A.drank[gd] = 2;
     uint64_t k2; int c1, c2;
-    const int sl = attribution(S, a, &k2, &c1, &c2);
-    A.dkey[g] = k2; A.dpk[g] = event_id(A, g, sl, N); A.fc[2 * g] = c1; A.fc[2 * g + 1] = c2;
+    const int sl = attribution(S, d, &k2, &c1, &c2);
+    A.dkey[gd] = k2; A.dpk[gd] = event_id(A, gd, sl, N); A.fc[2 * gd] = c1; A.fc[2 * gd + 1] = c2;
     res.dc[nd++] = (int32_t)(base + c1);
     if (c2 != c1) res.dc[nd++] = (int32_t)(base + c2);
   }
