@@ -545,9 +545,20 @@ __device__ void run_system(const SysDev& S, const RunArgs& A, int64_t max_coll, 
       // ---------------- collision (doTheCollisionNormal 3542 / Grow 3465)
       const int i = e - N, j = E.j;
       Disk di = S.d[i];
-      grow_fly(S, di, i, R.t, grow);
       Disk dj = S.d[j];
-      if (E.ca != dj.coll) {
+      const bool stale = E.ca != dj.coll;
+      {
+        // free flights of i (even lanes) and j (odd lanes) in shared
+        // instructions; j's is used only when the event is not stale
+        const bool odd = lane & 1;
+        Disk M = odd ? dj : di;
+        grow_fly(S, M, odd ? j : i, R.t, grow);
+        di.x = __shfl_sync(FULL, M.x, 0); di.y = __shfl_sync(FULL, M.y, 0);
+        di.tl = __shfl_sync(FULL, M.tl, 0); di.rad = __shfl_sync(FULL, M.rad, 0);
+        dj.x = __shfl_sync(FULL, M.x, 1); dj.y = __shfl_sync(FULL, M.y, 1);
+        dj.tl = __shfl_sync(FULL, M.tl, 1); dj.rad = __shfl_sync(FULL, M.rad, 1);
+      }
+      if (stale) {
         if (lane == 0) S.d[i] = di;
         __syncwarp();
         R.nstale++;
@@ -563,7 +574,6 @@ __device__ void run_system(const SysDev& S, const RunArgs& A, int64_t max_coll, 
         if (!(A.flags & EDMD_F_COUNT_NORMAL) || !grow) logged++;
         R.ncol++;
         R.ncol_total++;
-        grow_fly(S, dj, j, R.t, grow);
         di.coll++;
         dj.coll++;
         double dx = dj.x - di.x, dy = dj.y - di.y;
