@@ -237,6 +237,12 @@ __device__ __forceinline__ bool is_neg(double a) {
 }
 __device__ __forceinline__ bool is_pos(double a) { return __double_as_longlong(a) > 0; }
 
+// -x when neg, else x: an exact sign flip on the integer pipe, so that
+// a + flip(x, true) rounds exactly as a - x
+__device__ __forceinline__ double flip(double x, bool neg) {
+  return __longlong_as_double(__double_as_longlong(x) ^ (neg ? (long long)0x8000000000000000ull : 0ll));
+}
+
 // general a < b and a <= b on the integer pipe: false when either is a NaN,
 // and -0 equals +0, exactly as the FP64 comparisons
 __device__ __forceinline__ bool nan_bits(double a) {

@@ -576,8 +576,15 @@ __device__ void run_system(const SysDev& S, const RunArgs& A, int64_t max_coll, 
         R.ncol_total++;
         di.coll++;
         dj.coll++;
-        double dx = dj.x - di.x, dy = dj.y - di.y;
-        double dvx = dj.vx - di.vx, dvy = dj.vy - di.vy;
+        // dx, dy, dvx, dvy on lanes 0..3 (mod 4) in one instruction
+        const int q4 = lane & 3;
+        double dx, dy, dvx, dvy;
+        {
+          const double d4 = (q4 == 0 ? dj.x : q4 == 1 ? dj.y : q4 == 2 ? dj.vx : dj.vy) -
+                            (q4 == 0 ? di.x : q4 == 1 ? di.y : q4 == 2 ? di.vx : di.vy);
+          dx = __shfl_sync(FULL, d4, 0); dy = __shfl_sync(FULL, d4, 1);
+          dvx = __shfl_sync(FULL, d4, 2); dvy = __shfl_sync(FULL, d4, 3);
+        }
         if (!grow) {   // elastic branch src/EDMD.c:3802-3827
           // 1/(1+1) and x/4 are exact, so these shortcuts round identically
           // (== 2.0 and == 4.0 as bit compares, on the integer pipe)
@@ -599,7 +606,9 @@ __device__ void run_system(const SysDev& S, const RunArgs& A, int64_t max_coll, 
             __syncwarp();
           }
           pbc_i(B, dx, dy);
-          double collKernel = invMass * (1 + S.res) * (dx * dvx + dy * dvy);
+          // dx*dvx on even lanes, dy*dvy on odd lanes, then their sum
+          const double pm = ((q4 & 1) ? dy : dx) * ((q4 & 1) ? dvy : dvx);
+          double collKernel = invMass * (1 + S.res) * (__shfl_sync(FULL, pm, 0) + __shfl_sync(FULL, pm, 1));
           double distSquared = 4 * di.rad * dj.rad;
           double f = __double_as_longlong(distSquared) == 0x4010000000000000ll ? collKernel * 0.25
                                                                                 : collKernel / distSquared;
@@ -615,15 +624,15 @@ __device__ void run_system(const SysDev& S, const RunArgs& A, int64_t max_coll, 
             lg->dvx = dvx; lg->dvy = dvy; lg->f = f;
           }
           if (A.flags & EDMD_F_LOG) R.nlog++;
-          // even lanes update i, odd lanes j: the two disks share instructions
+          // lanes 0..3 (mod 4) update i.vx, j.vx, i.vy, j.vy in shared
+          // instructions (v - x computed as v + (-x), the same rounding)
           {
-            const bool odd = lane & 1;
-            double vx = odd ? dj.vx : di.vx, vy = odd ? dj.vy : di.vy;
-            const double mo = odd ? di.m : dj.m;
-            if (odd) { vx -= f * mo * dx; vy -= f * mo * dy; }
-            else { vx += f * mo * dx; vy += f * mo * dy; }
-            di.vx = __shfl_sync(FULL, vx, 0); di.vy = __shfl_sync(FULL, vy, 0);
-            dj.vx = __shfl_sync(FULL, vx, 1); dj.vy = __shfl_sync(FULL, vy, 1);
+            const bool oj = q4 & 1, yax = q4 & 2;
+            const double v = yax ? (oj ? dj.vy : di.vy) : (oj ? dj.vx : di.vx);
+            const double inc = f * (oj ? di.m : dj.m) * (yax ? dy : dx);
+            const double nv = v + flip(inc, oj);
+            di.vx = __shfl_sync(FULL, nv, 0); dj.vx = __shfl_sync(FULL, nv, 1);
+            di.vy = __shfl_sync(FULL, nv, 2); dj.vy = __shfl_sync(FULL, nv, 3);
           }
         } else {       // growth rule src/EDMD.c:3479-3520
           double delta = 0.1 * 0;

@@ -668,12 +668,11 @@ __device__ void process_event_warp(const SysDev& S, const RoundArgs& A, int s, i
           const double w = (lane == 0 || lane == 3) ? dx : dy;
           ct[0] = cf * u * w;
         }
-        if (odd) {
-          M.vx -= f * Da.m * dx;
-          M.vy -= f * Da.m * dy;
-        } else {
-          M.vx += f * Db.m * dx;
-          M.vy += f * Db.m * dy;
+        // v - x as v + (-x) (the same rounding): no divergent branch
+        {
+          const double fm = f * (odd ? Da.m : Db.m);
+          M.vx = M.vx + flip(fm * dx, odd);
+          M.vy = M.vy + flip(fm * dy, odd);
         }
         Da.vx = __shfl_sync(FULLM, M.vx, 0);
         Da.vy = __shfl_sync(FULLM, M.vy, 0);
