@@ -362,8 +362,10 @@ def measure(edmd, a, workload, engine, coll, steps, warmup, rank, world, dist, d
     peak = peaks.get("hbm_gbs", 6800.0)
     # DRAM bytes per accepted collision of k_run from one ncu capture of a
     # 2000-collision step of the batched workload (dram__bytes_read.sum +
-    # dram__bytes_write.sum = 43.8 GB for 8.19e6 collisions), scaled to a launch
-    traffic = 5350.0 * ncoll / steps if engine == "warp" else None
+    # dram__bytes_write.sum = 41.51 + 5.54 GB for 8.192e6 collisions), scaled
+    # to a launch; the same capture gives the FP64 pipe's busy fraction, the
+    # resource that bounds this kernel
+    traffic = 5744.0 * ncoll / steps if engine == "warp" else None
     kernel = ("k_run (one persistent launch per step)" if engine == "warp" else
               "k_lane_run" if engine == "lane" else
               "round engine graph: k_select + k_process + k_recompute + k_barrier per round")
@@ -371,9 +373,10 @@ def measure(edmd, a, workload, engine, coll, steps, warmup, rank, world, dist, d
                 systems=len(systems), TN=TN, e2e=e2e, h2d=h2d, d2h=d2h,
                 roofline={"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                           "frac": achieved / peak, "traffic": traffic, "kernel": kernel,
-                          "traffic_source": ("ncu capture of a 2000-collision step, 5.35 KB per collision "
+                          "traffic_source": ("ncu capture of a 2000-collision step, 5.74 KB per collision "
                                              "(profiles/warp_k_run_batched.md), scaled to the launch"
                                              if traffic else None),
+                          "fp64_pipe_active": 0.558 if engine == "warp" else None,
                           "bytes_per_collision": Bcoll, "p_pair": p_pair, "p_pred": p_pred,
                           "peak_source": "measured hbm_gbs" if "hbm_gbs" in peaks else "fallback"})
 
