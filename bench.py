@@ -223,6 +223,19 @@ def sum_over_ranks(dist, v):
 
 # ------------------------------------------------------------------ reference arm
 
+def describe_workload(workload, systems, TN):
+    """The workload named in both arms' config."""
+    if workload == "batched":
+        return ("batched: %d systems/GPU, N~U[256,4096], phi~U[0.30,0.75], bidisperse 1.0/1.4, growth start"
+                % systems)
+    if workload == "single_large":
+        return "single Hex system, N=%d, phi=%.2f, %d equilibration collisions" % (TN, LARGE_PHI, LARGE_EQUIL)
+    if workload == "single_4m":
+        return ("single Hex system, N=%d, phi=%.2f, %d equilibration collisions, full FP64"
+                % (TN, SINGLE["single_4m"][1], LARGE_EQUIL))
+    return "single Hex system, N=1980, phi=0.70"
+
+
 def run_reference(a, rank, world, dist):
     if rank != 0:
         return 0
@@ -244,7 +257,9 @@ def run_reference(a, rank, world, dist):
             "value": v, "unit": UNIT, "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup,
             "ms_per_step": 1000 * wall / a.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": a.workload, "sample": sample},
+            "config": {"workload": describe_workload(a.workload, a.nsys or (4096 if a.workload == "batched" else 1),
+                                                     SINGLE[a.workload][0] if a.workload in SINGLE else None),
+                       "sample": sample},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": len(params), "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -419,15 +434,7 @@ def run_ours(a, rank, world, dist):
                "sample": f"{nproc} system(s) of the same workload, one per process, "
                          f"{cpu_sample_coll(workload, a)} collisions each, oracle restatement (-O2 IEEE), "
                          f"set-up untimed"}
-    workload_desc = {
-        "batched": "batched: %d systems/GPU, N~U[256,4096], phi~U[0.30,0.75], bidisperse 1.0/1.4, growth start"
-                   % r["systems"],
-        "single_large": "single Hex system, N=%d, phi=%.2f, %d equilibration collisions" %
-                        (r["TN"], LARGE_PHI, LARGE_EQUIL),
-        "single_4m": "single Hex system, N=%d, phi=%.2f, %d equilibration collisions, full FP64" %
-                     (r["TN"], SINGLE["single_4m"][1], LARGE_EQUIL),
-        "plain_small": "single Hex system, N=1980, phi=0.70",
-    }[workload]
+    workload_desc = describe_workload(workload, r["systems"], r["TN"])
     line = {
         "metric": METRICS[workload], "value": r["value"], "unit": UNIT, "n_gpus": world,
         "steps": a.steps, "warmup": a.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True,
