@@ -15,8 +15,8 @@ for each case:
 * the collision-virial accumulators, final time and counters,
 * the state after free-flying every disk to the final time.
 
-The fixtures are what the GPU parity tests compare against on the GPU machine,
-where the reference checkout does not exist.
+The fixtures are what the GPU parity tests compare against; the tests read
+only these files, never the reference checkout.
 """
 import argparse
 import os

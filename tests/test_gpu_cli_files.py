@@ -1,7 +1,7 @@
-"""The drop-in driver writes the reference's dump and thermo files byte for byte.
+"""The drop-in program writes the reference's dump and thermo files byte for byte.
 
 tests/golden/files_hex64.{dump,thermo} were written by the reference's own
-saveTXT / saveThermo (tests/golden/make_golden.py).  The driver runs the same
+saveTXT / saveThermo (tests/golden/make_golden.py).  The program runs the same
 command line on the GPU; since the trajectory is bit-identical, the text
 files must be identical too (134,574 collisions, 12 frames, 5 thermo rows).
 """
