@@ -308,6 +308,7 @@ class Stepper:
 def measure(edmd, a, workload, engine, coll, steps, warmup, rank, world, dist, dev, e2e_steps):
     nsys = a.nsys if a.nsys is not None else (4096 if workload == "batched" else 1)
     systems = build_systems(edmd, workload, nsys, a.seed, rank)
+    edmd.set_warp_group(a.warp_group)
     eng = edmd.Engine(systems, engine=edmd.ENGINE_LANE if engine == "lane" else edmd.ENGINE_WARP)
     TN = sum(s["desc"].N for s in systems)
     TC = sum(int(s["desc"].Lx / 2) * int(s["desc"].Ly / 2) for s in systems)
@@ -442,7 +443,8 @@ def run_ours(a, rank, world, dist):
         "config": {"workload": workload_desc, "engine": engine, "systems_per_gpu": r["systems"],
                    "disks_per_gpu": r["TN"], "collisions_per_system_per_step": coll,
                    "l2": "state (~%.0f MB/GPU) larger than L2, no flush" % (r["TN"] * 160 / 1e6),
-                   "parallelism": f"replicas x{world}"},
+                   "parallelism": f"replicas x{world}",
+                   "lanes_per_system": a.warp_group if engine == "warp" else None},
         "e2e": {"value": r["e2e"], "unit": UNIT, "h2d_bytes_per_step": r["h2d"], "d2h_bytes_per_step": r["d2h"],
                 "path": "edmd_load_state (pinned host) + advance + edmd_sync + edmd_get_states (pinned host)"},
         "roofline": r["roofline"],
@@ -473,6 +475,8 @@ def main():
     ap.add_argument("--seed", type=int, default=20261203)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-secondary", action="store_true")
+    ap.add_argument("--warp-group", type=int, default=32, choices=[16, 32],
+                    help="warp engine lanes per system (16: two systems per warp)")
     a = ap.parse_args()
     if a.warmup < 3 and a.impl == "ours":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)

@@ -43,12 +43,39 @@ namespace {
 constexpr int MAXC = 8;          // candidates buffered per cell list per lane
 constexpr int WARPS_PER_BLOCK = 4;
 
+// scratch of one lane group (one system)
 struct WarpSmem {
-  int32_t reg[32 * MAXC];        // per-lane walk buffers
+  int32_t reg[2 * 9 * MAXC];     // walk buffers, one per (disk, cell) task
   int32_t comp[2 * 9 * MAXC];    // packed candidates
   int16_t ord[2 * 9 * MAXC];     // their scan order
   long long msum[2];             // last two mass sums of the collision rule (bits) ...
   double inv[2];                 // ... and 1 / msum, the same division's result
+};
+
+// A group of GW lanes that runs one system: the whole warp (GW = 32) or one
+// half of it (GW = 16, two systems per warp).  Every collective of the event
+// loop goes through the group's mask and width, so the two halves of a warp
+// are independent and may diverge.
+template <int GW>
+struct Grp {
+  int lane;                      // 0 .. GW-1
+  unsigned mask;                 // the group's lanes within the warp
+  __device__ __forceinline__ explicit Grp(int tid)
+      : lane(tid & (GW - 1)), mask(GW == 32 ? 0xffffffffu : (((1u << GW) - 1u) << ((tid & 31) & ~(GW - 1)))) {}
+  template <class T> __device__ __forceinline__ T shfl(T v, int src) const { return __shfl_sync(mask, v, src, GW); }
+  template <class T> __device__ __forceinline__ T shfl_xor(T v, int o) const {
+    return __shfl_xor_sync(mask, v, o, GW);
+  }
+  template <class T> __device__ __forceinline__ T shfl_up(T v, int o) const {
+    return __shfl_up_sync(mask, v, o, GW);
+  }
+  __device__ __forceinline__ void sync() const { __syncwarp(mask); }
+  __device__ __forceinline__ bool any(bool p) const { return __any_sync(mask, p); }
+  // group-relative index of the first lane where p holds, or -1
+  __device__ __forceinline__ int first(bool p) const {
+    const unsigned m = __ballot_sync(mask, p) & mask;
+    return m ? ((__ffs(m) - 1) & (GW - 1)) : -1;
+  }
 };
 
 __device__ __forceinline__ Node empty_node(int idx) {
@@ -60,16 +87,36 @@ __device__ __forceinline__ bool node_less(const Node& a, const Node& b) {
   return key_less(a.b, a.tk, a.tie, a.idx, b.b, b.tk, b.tie, b.idx);
 }
 
-__device__ __forceinline__ void warp_min(Node& n) {
+template <int GW>
+__device__ __forceinline__ void grp_min(Node& n, const Grp<GW>& G) {
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
+  for (int o = GW / 2; o > 0; o >>= 1) {
     Node m;
-    m.tk = __shfl_xor_sync(FULL, n.tk, o);
-    m.tie = __shfl_xor_sync(FULL, n.tie, o);
-    m.b = __shfl_xor_sync(FULL, n.b, o);
-    m.idx = __shfl_xor_sync(FULL, n.idx, o);
+    m.tk = G.shfl_xor(n.tk, o);
+    m.tie = G.shfl_xor(n.tie, o);
+    m.b = G.shfl_xor(n.b, o);
+    m.idx = G.shfl_xor(n.idx, o);
     if (node_less(m, n)) n = m;
   }
+}
+
+// the minimum of the 32 children of node `par` of level h-1, on every lane
+template <int GW>
+__device__ __forceinline__ Node children_min(const SysDev& S, int h, int par, const Grp<GW>& G) {
+  const int ch = (par << 5) + G.lane;
+  Node c = ch < S.lev_cnt[h - 1] ? S.tree[S.lev_off[h - 1] + ch] : empty_node(0x7fffffff);
+  if (GW < 32) {
+#pragma unroll
+    for (int k = GW; k < 32; k += GW) {
+      const int c2 = ch + k;
+      if (c2 < S.lev_cnt[h - 1]) {
+        const Node m = S.tree[S.lev_off[h - 1] + c2];
+        if (node_less(m, c)) c = m;
+      }
+    }
+  }
+  grp_min(c, G);
+  return c;
 }
 
 __device__ __forceinline__ Node ev_node(const Ev& e, int idx) {
@@ -78,7 +125,9 @@ __device__ __forceinline__ Node ev_node(const Ev& e, int idx) {
 }
 
 // recompute the leaf of `leaf` from its events and fix its path to the root
-__device__ void leaf_update(const SysDev& S, int leaf, int lane) {
+template <int GW>
+__device__ void leaf_update(const SysDev& S, int leaf, const Grp<GW>& G) {
+  const int lane = G.lane;
   const int N = S.B.N;
   Node n = empty_node(leaf);
   if (leaf < N) {
@@ -90,23 +139,23 @@ __device__ void leaf_update(const SysDev& S, int leaf, int lane) {
     if (e.st == ST_QUEUED) n = ev_node(e, leaf);
   }
   if (lane == 0) S.tree[leaf] = n;
-  __syncwarp();
+  G.sync();
   int idx = leaf;
   for (int h = 1; h < S.nlev; h++) {
     int par = idx >> 5;
-    int ch = (par << 5) + lane;
-    Node c = ch < S.lev_cnt[h - 1] ? S.tree[S.lev_off[h - 1] + ch] : empty_node(0x7fffffff);
-    warp_min(c);
+    const Node c = children_min(S, h, par, G);
     if (lane == 0) S.tree[S.lev_off[h] + par] = c;
-    __syncwarp();
+    G.sync();
     idx = par;
   }
 }
 
 // rebuild every level of the tree (after init or the growth stop)
-__device__ __noinline__ void tree_rebuild(const SysDev& S, int lane) {
+template <int GW>
+__device__ __noinline__ void tree_rebuild(const SysDev& S, const Grp<GW>& G) {
+  const int lane = G.lane;
   const int N = S.B.N;
-  for (int l = lane; l < S.L; l += 32) {
+  for (int l = lane; l < S.L; l += GW) {
     Node n = empty_node(l);
     if (l < N) {
       Ev e0 = S.ev[l], e1 = S.ev[N + l];
@@ -118,17 +167,15 @@ __device__ __noinline__ void tree_rebuild(const SysDev& S, int lane) {
     }
     S.tree[l] = n;
   }
-  __syncwarp();
+  G.sync();
 #pragma unroll
   for (int h = 1; h < MAXLEV; h++) {
     if (h >= S.nlev) break;
     for (int par = 0; par < S.lev_cnt[h]; par++) {
-      int ch = (par << 5) + lane;
-      Node c = ch < S.lev_cnt[h - 1] ? S.tree[S.lev_off[h - 1] + ch] : empty_node(0x7fffffff);
-      warp_min(c);
+      const Node c = children_min(S, h, par, G);
       if (lane == 0) S.tree[S.lev_off[h] + par] = c;
     }
-    __syncwarp();
+    G.sync();
   }
 }
 
@@ -147,8 +194,10 @@ __device__ __forceinline__ int sched_place(const SysDev& S, const SysState& R, d
 
 // `cls_direct` is 2 for a schedule from an event handler and 0 for the
 // re-add done by a wrap
+template <int GW>
 __device__ __forceinline__ void sched_insert(const SysDev& S, SysState& R, int e, double T, int32_t j,
-                                             uint32_t ca, uint64_t cls_direct, int place, int lane) {
+                                             uint32_t ca, uint64_t cls_direct, int place, const Grp<GW>& G) {
+  const int lane = G.lane;
   Ev ev;
   ev.t = T; ev.j = j; ev.ca = ca;
   if (place == -1) {
@@ -165,27 +214,32 @@ __device__ __forceinline__ void sched_insert(const SysDev& S, SysState& R, int e
   }
   R.C++;
   if (lane == 0) S.ev[e] = ev;
-  __syncwarp();
+  G.sync();
 }
 
+template <int GW>
 __device__ void schedule(const SysDev& S, SysState& R, int e, double T, int32_t j, uint32_t ca,
-                         uint64_t cls_direct, int lane) {
-  sched_insert(S, R, e, T, j, ca, cls_direct, sched_place(S, R, T), lane);
+                         uint64_t cls_direct, const Grp<GW>& G) {
+  sched_insert(S, R, e, T, j, ca, cls_direct, sched_place(S, R, T), G);
 }
 
 // one or two handler schedules in a row (e0 first; e1 < 0: none): the FP64
 // placement of e0 on even lanes and of e1 on odd lanes in shared
 // instructions, then the insertions
+template <int GW>
 __device__ void schedule2(const SysDev& S, SysState& R, int e0, double T0, int32_t j0, uint32_t ca0,
-                          int e1, double T1, int32_t j1, uint32_t ca1, int lane) {
+                          int e1, double T1, int32_t j1, uint32_t ca1, const Grp<GW>& G) {
+  const int lane = G.lane;
   const int pl = sched_place(S, R, (lane & 1) && e1 >= 0 ? T1 : T0);
-  const int p0 = __shfl_sync(FULL, pl, 0), p1 = __shfl_sync(FULL, pl, 1);
-  sched_insert(S, R, e0, T0, j0, ca0, 2ull, p0, lane);
-  if (e1 >= 0) sched_insert(S, R, e1, T1, j1, ca1, 2ull, p1, lane);
+  const int p0 = G.shfl(pl, 0), p1 = G.shfl(pl, 1);
+  sched_insert(S, R, e0, T0, j0, ca0, 2ull, p0, G);
+  if (e1 >= 0) sched_insert(S, R, e1, T1, j1, ca1, 2ull, p1, G);
 }
 
 // removeEventFromQueue (src/EDMD.c:2209) in key form
-__device__ void unqueue(const SysDev& S, SysState& R, int e, int lane) {
+template <int GW>
+__device__ void unqueue(const SysDev& S, SysState& R, int e, const Grp<GW>& G) {
+  const int lane = G.lane;
   uint32_t st = S.ev[e].st;
   if (st == ST_OVF) {
     int p = S.op[e], n = S.on[e];
@@ -196,25 +250,27 @@ __device__ void unqueue(const SysDev& S, SysState& R, int e, int lane) {
     if (p == NIL) R.ovf = n;
   }
   if (lane == 0) S.ev[e].st = ST_NONE;
-  __syncwarp();
+  G.sync();
 }
 
 // the overflow bucket is redistributed when the calendar wraps
 // (addNextPaulEvent src/EDMD.c:2287-2300)
-__device__ __noinline__ void do_wrap(const SysDev& S, SysState& R, int lane) {
+template <int GW>
+__device__ __noinline__ void do_wrap(const SysDev& S, SysState& R, const Grp<GW>& G) {
   const int N = S.B.N;
   int e = R.ovf;
   R.ovf = NIL;
-  __syncwarp();
-  while (e != NIL) {
+  G.sync();
+  int guard = 0;                       // the overflow list holds at most 2N + 3 events
+  while (e != NIL && guard++ <= 2 * N + NSPECIAL) {
     int n = S.on[e];
     double T = S.ev[e].t;
     int32_t j = S.ev[e].j;
     uint32_t ca = S.ev[e].ca;
-    schedule(S, R, e, T, j, ca, 0ull, lane);
-    __syncwarp();
+    schedule(S, R, e, T, j, ca, 0ull, G);
+    G.sync();
     int leaf = e < 2 * N ? (e < N ? e : e - N) : N + (e - 2 * N);
-    leaf_update(S, leaf, lane);
+    leaf_update(S, leaf, G);
     e = n;
   }
 }
@@ -250,27 +306,46 @@ __device__ __forceinline__ void best_merge(uint64_t& bk, int& bo, int& bp, uint3
 
 // collisionEventNormal / Grow (src/EDMD.c:2829 / 3104) for disks a0 and a1
 // (a1 may be -1): scan the 3x3 neighbour cells, dy outer and dx inner, list
-// order, keep the first strict minimum.  Lanes 0..8 own a0's cells and lanes
-// 16..24 own a1's; the candidates are then packed over the whole warp.
+// order, keep the first strict minimum.  The (disk, cell) walks are tasks
+// t = 0..8 (a0's cells in scan order) and 9..17 (a1's): task t runs on lane
+// t % GW, a lane with two tasks walks both lists at once.  The candidates are
+// then packed over the group in task order and solved GW at a time.
+template <int GW>
 __device__ void predict2(const SysDev& S, SysState& R, int a0, int a1, Pred& r0, Pred& r1,
-                         int lane, WarpSmem* sm, bool* ovl, int* ovl_a, int* ovl_b) {
+                         const Grp<GW>& G, WarpSmem* sm, bool* ovl, int* ovl_a, int* ovl_b) {
   const Box& B = S.B;
+  const int lane = G.lane;
   const bool grow = R.grow != 0;
   const double dinit = grow ? 10000000 : NEVER;
-  const int g = lane >> 4, q = lane & 15;
-  const int a = g ? a1 : a0;
-  int cnt = 0;
-  int32_t* reg = sm->reg + lane * MAXC;
-  if (a >= 0 && q < 9) {
-    int X = S.cx[a], Y = S.cy[a];
-    int cell = pbc_cy(B, Y + q / 3 - 1) * B.Nxc + pbc_cx(B, X + q % 3 - 1);
-    int p = S.head[cell];
-    while (p != NIL) {
-      if (p != a) { if (cnt < MAXC) reg[cnt] = p; cnt++; }
-      p = S.d[p].nxt;
+  const int ntask = a1 >= 0 ? 18 : 9;
+  // the (up to) two tasks of this lane: t0 = lane, t1 = lane + GW
+  const int t0 = lane, t1 = lane + GW;
+  const bool v0 = t0 < ntask, v1 = t1 < ntask;
+  const int o0 = t0 >= 9 ? a1 : a0, o1 = t1 >= 9 ? a1 : a0;
+  const int q0 = t0 >= 9 ? t0 - 9 : t0, q1 = t1 >= 9 ? t1 - 9 : t1;
+  auto task_cell = [&](int own, int q) {
+    return pbc_cy(B, S.cy[own] + q / 3 - 1) * B.Nxc + pbc_cx(B, S.cx[own] + q % 3 - 1);
+  };
+  int p0 = v0 ? S.head[task_cell(o0, q0)] : NIL;
+  int p1 = v1 ? S.head[task_cell(o1, q1)] : NIL;
+  int c0 = 0, c1 = 0;
+  {
+    int guard = 0;                   // the lists hold N disks in all
+    while ((p0 != NIL || p1 != NIL) && guard++ < 2 * B.N) {
+      int n0 = NIL, n1 = NIL;
+      if (p0 != NIL) {
+        if (p0 != o0) { if (c0 < MAXC) sm->reg[t0 * MAXC + c0] = p0; c0++; }
+        n0 = S.d[p0].nxt;
+      }
+      if (p1 != NIL) {
+        if (p1 != o1) { if (c1 < MAXC) sm->reg[t1 * MAXC + c1] = p1; c1++; }
+        n1 = S.d[p1].nxt;
+      }
+      p0 = n0;
+      p1 = n1;
     }
   }
-  bool spill = __any_sync(FULL, cnt > MAXC);
+  const bool spill = G.any(c0 > MAXC || c1 > MAXC);
   Disk A0 = S.d[a0];
   Disk A1 = a1 >= 0 ? S.d[a1] : A0;
   uint64_t bd0 = cand_key(dinit), bd1 = bd0;
@@ -280,23 +355,28 @@ __device__ void predict2(const SysDev& S, SysState& R, int a0, int a1, Pred& r0,
   int la = -1, lb = -1;
   int tot;
   if (!spill) {
-    int incl = cnt;
+    // exclusive prefix of the counts in task order: tasks 0..GW-1, then GW..
+    int in0 = c0, in1 = c1;
 #pragma unroll
-    for (int o = 1; o < 16; o <<= 1) {
-      int v = __shfl_up_sync(FULL, incl, o, 16);
-      if (q >= o) incl += v;
+    for (int o = 1; o < GW; o <<= 1) {
+      const int u0 = G.shfl_up(in0, o), u1 = G.shfl_up(in1, o);
+      if (lane >= o) { in0 += u0; in1 += u1; }
     }
-    int excl = incl - cnt;
-    int tot0 = __shfl_sync(FULL, incl, 15);
-    int tot1 = __shfl_sync(FULL, incl, 31);
-    int base = g ? tot0 : 0;
-    for (int k = 0; k < cnt; k++) {
-      sm->comp[base + excl + k] = reg[k];
-      sm->ord[base + excl + k] = (int16_t)(q * MAXC + k);
+    const int sum0 = G.shfl(in0, GW - 1), sum1 = G.shfl(in1, GW - 1);
+    const int ex0 = in0 - c0, ex1 = sum0 + in1 - c1;
+    // a0's candidates are tasks 0..8: their count is the prefix at task 9
+    const int tot0 = G.shfl(ex0, 9);
+    tot = sum0 + sum1;
+    for (int k = 0; k < c0; k++) {
+      sm->comp[ex0 + k] = sm->reg[t0 * MAXC + k];
+      sm->ord[ex0 + k] = (int16_t)(q0 * MAXC + k);
     }
-    __syncwarp();
-    tot = tot0 + tot1;
-    for (int f = lane; f < tot; f += 32) {
+    for (int k = 0; k < c1; k++) {
+      sm->comp[ex1 + k] = sm->reg[t1 * MAXC + k];
+      sm->ord[ex1 + k] = (int16_t)(q1 * MAXC + k);
+    }
+    G.sync();
+    for (int f = lane; f < tot; f += GW) {
       int p = sm->comp[f];
       int o = sm->ord[f];
       Disk P = S.d[p];
@@ -307,40 +387,43 @@ __device__ void predict2(const SysDev& S, SysState& R, int a0, int a1, Pred& r0,
       if (g1) best_merge(bd1, bo1, bp1, bc1, cand_key(d), o, p, P.coll);
       else best_merge(bd0, bo0, bp0, bc0, cand_key(d), o, p, P.coll);
     }
-    __syncwarp();
+    G.sync();
   } else {
-    // a cell list longer than MAXC: every lane walks its own list
+    // a cell list longer than MAXC: every task walks its own list again,
+    // solving as it goes
     tot = 0;
-    if (a >= 0 && q < 9) {
-      const Disk& AA = g ? A1 : A0;
-      int X = S.cx[a], Y = S.cy[a];
-      int cell = pbc_cy(B, Y + q / 3 - 1) * B.Nxc + pbc_cx(B, X + q % 3 - 1);
-      int p = S.head[cell];
-      int k = 0;
-      while (p != NIL) {
+    for (int w = 0; w < 2; w++) {
+      const int t = w ? t1 : t0;
+      if (t >= ntask) continue;
+      const int own = w ? o1 : o0, q = w ? q1 : q0;
+      const bool g1 = t >= 9;
+      const Disk& AA = g1 ? A1 : A0;
+      int p = S.head[task_cell(own, q)];
+      int k = 0, guard = 0;
+      while (p != NIL && guard++ < B.N) {
         Disk P = S.d[p];
-        if (p != a) {
+        if (p != own) {
           bool ov = false;
-          double d = pair_time(S, AA, a, P, p, R.t, grow, &ov);
-          if (ov) { lovl = true; la = a; lb = p; }
-          if (g) best_merge(bd1, bo1, bp1, bc1, cand_key(d), q * 4096 + k, p, P.coll);
+          double d = pair_time(S, AA, own, P, p, R.t, grow, &ov);
+          if (ov) { lovl = true; la = own; lb = p; }
+          if (g1) best_merge(bd1, bo1, bp1, bc1, cand_key(d), q * 4096 + k, p, P.coll);
           else best_merge(bd0, bo0, bp0, bc0, cand_key(d), q * 4096 + k, p, P.coll);
           k++;
         }
         p = P.nxt;
       }
-      tot = k;
+      tot += k;
     }
-    for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(FULL, tot, o);
+    for (int o = GW / 2; o > 0; o >>= 1) tot += G.shfl_xor(tot, o);
   }
-  // lexicographic (dt, scan order) minimum over the warp
+  // lexicographic (dt, scan order) minimum over the group
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    uint64_t d = __shfl_xor_sync(FULL, bd0, o); int oo = __shfl_xor_sync(FULL, bo0, o);
-    int pp = __shfl_xor_sync(FULL, bp0, o); uint32_t cc = __shfl_xor_sync(FULL, bc0, o);
+  for (int o = GW / 2; o > 0; o >>= 1) {
+    uint64_t d = G.shfl_xor(bd0, o); int oo = G.shfl_xor(bo0, o);
+    int pp = G.shfl_xor(bp0, o); uint32_t cc = G.shfl_xor(bc0, o);
     best_merge(bd0, bo0, bp0, bc0, d, oo, pp, cc);
-    d = __shfl_xor_sync(FULL, bd1, o); oo = __shfl_xor_sync(FULL, bo1, o);
-    pp = __shfl_xor_sync(FULL, bp1, o); cc = __shfl_xor_sync(FULL, bc1, o);
+    d = G.shfl_xor(bd1, o); oo = G.shfl_xor(bo1, o);
+    pp = G.shfl_xor(bp1, o); cc = G.shfl_xor(bc1, o);
     best_merge(bd1, bo1, bp1, bc1, d, oo, pp, cc);
   }
   if (bo0 < 0) bc0 = S.d[0].coll;   // no partner: partner 0 (src/EDMD.c:2830)
@@ -349,12 +432,11 @@ __device__ void predict2(const SysDev& S, SysState& R, int a0, int a1, Pred& r0,
   r1.dt = key_time(bd1); r1.partner = bp1; r1.ca = bc1;
   R.npair += (uint64_t)tot;
   R.npred += (a1 >= 0) ? 2 : 1;
-  unsigned m = __ballot_sync(FULL, lovl);
-  if (m) {
-    int src = __ffs(m) - 1;
+  const int src = G.first(lovl);
+  if (src >= 0) {
     *ovl = true;
-    *ovl_a = __shfl_sync(FULL, la, src);
-    *ovl_b = __shfl_sync(FULL, lb, src);
+    *ovl_a = G.shfl(la, src);
+    *ovl_b = G.shfl(lb, src);
   }
 }
 
@@ -362,24 +444,26 @@ __device__ void predict2(const SysDev& S, SysState& R, int a0, int a1, Pred& r0,
 
 
 // sequential sum over disks, in index order, identical in all lanes
-template <class F>
-__device__ __forceinline__ void seq_sums(const SysDev& S, int lane, int nval, double* out, F f) {
+template <int GW, class F>
+__device__ __forceinline__ void seq_sums(const SysDev& S, const Grp<GW>& G, int nval, double* out, F f) {
+  const int lane = G.lane;
   const int N = S.B.N;
   for (int k = 0; k < nval; k++) out[k] = 0;
-  for (int base = 0; base < N; base += 32) {
+  for (int base = 0; base < N; base += GW) {
     double v[4] = {0, 0, 0, 0};
     int i = base + lane;
     if (i < N) f(i, v);
-    int lim = min(32, N - base);
+    int lim = min(GW, N - base);
     for (int s = 0; s < lim; s++)
-      for (int k = 0; k < nval; k++) out[k] += __shfl_sync(FULL, v[k], s);
+      for (int k = 0; k < nval; k++) out[k] += G.shfl(v[k], s);
   }
 }
 
 // physicalQ (src/EDMD.c:5968-6013): px, py, E
-__device__ __noinline__ void physical_q(const SysDev& S, int lane, double* E, double* px, double* py) {
+template <int GW>
+__device__ __noinline__ void physical_q(const SysDev& S, const Grp<GW>& G, double* E, double* px, double* py) {
   double o[3];
-  seq_sums(S, lane, 3, o, [&](int i, double* v) {
+  seq_sums(S, G, 3, o, [&](int i, double* v) {
     Disk p = S.d[i];
     v[0] = p.vx * p.m;
     v[1] = p.vy * p.m;
@@ -390,15 +474,17 @@ __device__ __noinline__ void physical_q(const SysDev& S, int lane, double* E, do
 }
 
 // takeAThermo + saveThermo (src/EDMD.c:4679, 5232-5697) with Nthermo = 1
-__device__ __noinline__ void do_thermo(const SysDev& S, SysState& R, int lane) {
+template <int GW>
+__device__ __noinline__ void do_thermo(const SysDev& S, SysState& R, const Grp<GW>& G) {
+  const int lane = G.lane;
   const int N = S.B.N;
   double E, px, py;
-  physical_q(S, lane, &E, &px, &py);
+  physical_q(S, G, &E, &px, &py);
   double area = S.B.Lx * S.B.Ly;
   double dT = R.t - R.lastThermo;
   R.lastThermo = R.t;
   double e4[4];
-  seq_sums(S, lane, 4, e4, [&](int i, double* v) {
+  seq_sums(S, G, 4, e4, [&](int i, double* v) {
     Disk p = S.d[i];
     v[0] = p.m * p.vx * p.vx; v[1] = p.m * p.vy * p.vy;
     v[2] = p.m * p.vx * p.vy; v[3] = p.m * p.vy * p.vx;
@@ -412,10 +498,10 @@ __device__ __noinline__ void do_thermo(const SysDev& S, SysState& R, int lane) {
   row[3] = (-1 / (dT)) * (R.collT[0] + R.collT[1]) / (2 * area) + E / area;
   R.collT[0] = R.collT[1] = R.collT[2] = R.collT[3] = 0;
   double vxa;
-  seq_sums(S, lane, 1, &vxa, [&](int i, double* v) { v[0] = S.d[i].vx; });
+  seq_sums(S, G, 1, &vxa, [&](int i, double* v) { v[0] = S.d[i].vx; });
   vxa /= N;
   double v24[2];
-  seq_sums(S, lane, 2, v24, [&](int i, double* v) {
+  seq_sums(S, G, 2, v24, [&](int i, double* v) {
     double d = S.d[i].vx - vxa; double d2 = d * d; v[0] = d2; v[1] = d2 * d2;
   });
   v24[0] /= N; v24[1] /= N;
@@ -428,10 +514,12 @@ __device__ __noinline__ void do_thermo(const SysDev& S, SysState& R, int lane) {
 }
 
 // stopGrow (src/EDMD.c:4740-4800)
-__device__ __noinline__ void do_growstop(const SysDev& S, SysState& R, int lane, WarpSmem* sm,
+template <int GW>
+__device__ __noinline__ void do_growstop(const SysDev& S, SysState& R, const Grp<GW>& G, WarpSmem* sm,
                             bool* ovl, int* oa, int* ob) {
+  const int lane = G.lane;
   const int N = S.B.N;
-  for (int i = lane; i < N; i += 32) {
+  for (int i = lane; i < N; i += GW) {
     Disk p = S.d[i];
     grow_fly(S, p, i, R.t, true);
     p.coll = 0;
@@ -440,60 +528,81 @@ __device__ __noinline__ void do_growstop(const SysDev& S, SysState& R, int lane,
   }
   R.ncol = 0; R.ncross = 0;
   R.grow = 0;
-  __syncwarp();
+  G.sync();
   // normalizePhysicalQ (src/EDMD.c:5723-5764)
   double E, px, py;
-  physical_q(S, lane, &E, &px, &py);
-  for (int i = lane; i < N; i += 32) {
+  physical_q(S, G, &E, &px, &py);
+  for (int i = lane; i < N; i += GW) {
     Disk p = S.d[i];
     p.vx -= px / (N * p.m);
     p.vy -= py / (N * p.m);
     S.d[i] = p;
   }
-  __syncwarp();
-  physical_q(S, lane, &E, &px, &py);
-  for (int i = lane; i < N; i += 32) {
+  G.sync();
+  physical_q(S, G, &E, &px, &py);
+  for (int i = lane; i < N; i += GW) {
     Disk p = S.d[i];
     p.vx /= sqrt(E / N / S.Einit);
     p.vy /= sqrt(E / N / S.Einit);
     S.d[i] = p;
   }
-  __syncwarp();
+  G.sync();
   for (int i = 0; i < N; i++) {
     uint32_t c = S.d[i].coll + 1;
     if (lane == 0) S.d[i].coll = c;
-    __syncwarp();
-    unqueue(S, R, N + i, lane);
+    G.sync();
+    unqueue(S, R, N + i, G);
     Pred r0, r1;
-    predict2(S, R, i, -1, r0, r1, lane, sm, ovl, oa, ob);
-    schedule(S, R, N + i, R.t + r0.dt, r0.partner, r0.ca, 2ull, lane);
-    unqueue(S, R, i, lane);
+    predict2(S, R, i, -1, r0, r1, G, sm, ovl, oa, ob);
+    schedule(S, R, N + i, R.t + r0.dt, r0.partner, r0.ca, 2ull, G);
+    unqueue(S, R, i, G);
     int dir;
     Disk p = S.d[i];
     double tc = crossing_time_i(S.B, p, S.cx[i], S.cy[i], R.t, &dir);
-    schedule(S, R, i, tc, dir, 0, 2ull, lane);
-    __syncwarp();
+    schedule(S, R, i, tc, dir, 0, 2ull, G);
+    G.sync();
   }
-  tree_rebuild(S, lane);
+  tree_rebuild(S, G);
+}
+
+// crossing_time_i with the two divisions on two lanes of the group: the lane
+// with (lane & xmask) == 0 takes the x axis of its disk, its partner lane ^
+// xmask the y axis; both return the disk's crossing
+template <int GW>
+__device__ __forceinline__ double crossing_time_grp(const Box& B, const Disk& p, int cx, int cy, double t,
+                                                    const Grp<GW>& G, int xmask, int* dir) {
+  const bool ydim = (G.lane & xmask) != 0;
+  int d;
+  const double ta = axis_time(B, p, cx, cy, ydim, &d);
+  const double tb = G.shfl_xor(ta, xmask);
+  const int db = G.shfl_xor(d, xmask);
+  const double tx = ydim ? tb : ta, ty = ydim ? ta : tb;
+  const bool ux = lt_i(tx, ty);
+  *dir = ux ? (ydim ? db : d) : (ydim ? d : db);
+  return t + (ux ? tx : ty);
 }
 
 // ---------------------------------------------------------------- run loop
 
 // the four virial sums live on lanes 0..3 (lane l accumulates term l % 4)
 // during the event loop; every lane gets all four back here
-__device__ __forceinline__ void gather_virial(SysState& R, double ctl) {
+template <int GW>
+__device__ __forceinline__ void gather_virial(SysState& R, double ctl, const Grp<GW>& G) {
 #pragma unroll
-  for (int k = 0; k < 4; k++) R.collT[k] = __shfl_sync(FULL, ctl, k);
+  for (int k = 0; k < 4; k++) R.collT[k] = G.shfl(ctl, k);
 }
 
-__device__ void run_system(const SysDev& S, const RunArgs& A, int64_t max_coll, int lane, WarpSmem* sm) {
+template <int GW>
+__device__ void run_system(const SysDev& S, const RunArgs& A, int64_t max_coll, const Grp<GW>& G,
+                           WarpSmem* sm) {
+  const int lane = G.lane;
   const Box& B = S.B;
   const int N = B.N;
   SysState R = *S.st;
   if (R.status != EDMD_OK) return;
   double ctl = R.collT[lane & 3];      // this lane's virial term, see gather_virial
   if (lane == 0) { sm->msum[0] = sm->msum[1] = 0; }   // no mass sum is +0
-  __syncwarp();
+  G.sync();
   const int root = S.lev_off[S.nlev - 1];
   int64_t logged = 0, nev = 0;
   int stop = 0, status = EDMD_OK;
@@ -510,7 +619,7 @@ __device__ void run_system(const SysDev& S, const RunArgs& A, int64_t max_coll, 
       if (r.b == BINF || (uint64_t)r.b >= R.next_wrap) {
         if (r.b == BINF && R.ovf == NIL) { status = EDMD_ERR_BUDGET; break; }
         while (R.k < R.next_wrap) { R.P += B.dtP; R.k++; }
-        do_wrap(S, R, lane);
+        do_wrap(S, R, G);
         R.next_wrap += (uint64_t)N;
         if (++guard > (1 << 20)) { status = EDMD_ERR_BUDGET; break; }
         continue;
@@ -532,7 +641,7 @@ __device__ void run_system(const SysDev& S, const RunArgs& A, int64_t max_coll, 
     nev++;
     R.nevents++;
     if (lane == 0) S.ev[e].st = ST_NONE;
-    __syncwarp();
+    G.sync();
     const bool grow = R.grow != 0;
     int ka = -1, kb = -1, uq = -1;     // disks whose crossing events are scheduled below, event removed
     int pa = -1, pb = -1;              // disks whose collision events are predicted below
@@ -553,14 +662,14 @@ __device__ void run_system(const SysDev& S, const RunArgs& A, int64_t max_coll, 
         const bool odd = lane & 1;
         Disk M = odd ? dj : di;
         grow_fly(S, M, odd ? j : i, R.t, grow);
-        di.x = __shfl_sync(FULL, M.x, 0); di.y = __shfl_sync(FULL, M.y, 0);
-        di.tl = __shfl_sync(FULL, M.tl, 0); di.rad = __shfl_sync(FULL, M.rad, 0);
-        dj.x = __shfl_sync(FULL, M.x, 1); dj.y = __shfl_sync(FULL, M.y, 1);
-        dj.tl = __shfl_sync(FULL, M.tl, 1); dj.rad = __shfl_sync(FULL, M.rad, 1);
+        di.x = G.shfl(M.x, 0); di.y = G.shfl(M.y, 0);
+        di.tl = G.shfl(M.tl, 0); di.rad = G.shfl(M.rad, 0);
+        dj.x = G.shfl(M.x, 1); dj.y = G.shfl(M.y, 1);
+        dj.tl = G.shfl(M.tl, 1); dj.rad = G.shfl(M.rad, 1);
       }
       if (stale) {
         if (lane == 0) S.d[i] = di;
-        __syncwarp();
+        G.sync();
         R.nstale++;
         pa = i;
       } else {
@@ -582,8 +691,8 @@ __device__ void run_system(const SysDev& S, const RunArgs& A, int64_t max_coll, 
         {
           const double d4 = (q4 == 0 ? dj.x : q4 == 1 ? dj.y : q4 == 2 ? dj.vx : dj.vy) -
                             (q4 == 0 ? di.x : q4 == 1 ? di.y : q4 == 2 ? di.vx : di.vy);
-          dx = __shfl_sync(FULL, d4, 0); dy = __shfl_sync(FULL, d4, 1);
-          dvx = __shfl_sync(FULL, d4, 2); dvy = __shfl_sync(FULL, d4, 3);
+          dx = G.shfl(d4, 0); dy = G.shfl(d4, 1);
+          dvx = G.shfl(d4, 2); dvy = G.shfl(d4, 3);
         }
         if (!grow) {   // elastic branch src/EDMD.c:3802-3827
           // 1/(1+1) and x/4 are exact, so these shortcuts round identically
@@ -598,17 +707,17 @@ __device__ void run_system(const SysDev& S, const RunArgs& A, int64_t max_coll, 
           else if (mk == sm->msum[1]) invMass = sm->inv[1];
           else {
             invMass = 1 / msum;
-            __syncwarp();
+            G.sync();
             if (lane == 0) {
               sm->msum[1] = sm->msum[0]; sm->inv[1] = sm->inv[0];
               sm->msum[0] = mk; sm->inv[0] = invMass;
             }
-            __syncwarp();
+            G.sync();
           }
           pbc_i(B, dx, dy);
           // dx*dvx on even lanes, dy*dvy on odd lanes, then their sum
           const double pm = ((q4 & 1) ? dy : dx) * ((q4 & 1) ? dvy : dvx);
-          double collKernel = invMass * (1 + S.res) * (__shfl_sync(FULL, pm, 0) + __shfl_sync(FULL, pm, 1));
+          double collKernel = invMass * (1 + S.res) * (G.shfl(pm, 0) + G.shfl(pm, 1));
           double distSquared = 4 * di.rad * dj.rad;
           double f = __double_as_longlong(distSquared) == 0x4010000000000000ll ? collKernel * 0.25
                                                                                 : collKernel / distSquared;
@@ -631,8 +740,8 @@ __device__ void run_system(const SysDev& S, const RunArgs& A, int64_t max_coll, 
             const double v = yax ? (oj ? dj.vy : di.vy) : (oj ? dj.vx : di.vx);
             const double inc = f * (oj ? di.m : dj.m) * (yax ? dy : dx);
             const double nv = v + flip(inc, oj);
-            di.vx = __shfl_sync(FULL, nv, 0); dj.vx = __shfl_sync(FULL, nv, 1);
-            di.vy = __shfl_sync(FULL, nv, 2); dj.vy = __shfl_sync(FULL, nv, 3);
+            di.vx = G.shfl(nv, 0); dj.vx = G.shfl(nv, 1);
+            di.vy = G.shfl(nv, 2); dj.vy = G.shfl(nv, 3);
           }
         } else {       // growth rule src/EDMD.c:3479-3520
           double delta = 0.1 * 0;
@@ -649,9 +758,9 @@ __device__ void run_system(const SysDev& S, const RunArgs& A, int64_t max_coll, 
           dj.vy -= collKernel * di.m * dyr - 2 * di.m * invMass * delta * dyr;
         }
         if (lane == 0) { S.d[i] = di; S.d[j] = dj; }
-        __syncwarp();
-        unqueue(S, R, i, lane);
-        unqueue(S, R, j, lane);
+        G.sync();
+        unqueue(S, R, i, G);
+        unqueue(S, R, j, G);
         ka = i; kb = j; uq = N + j;
         pa = i;
         pb = j;
@@ -676,7 +785,7 @@ __device__ void run_system(const SysDev& S, const RunArgs& A, int64_t max_coll, 
         case 3: if (cy - 1 == -1) { cy = B.Nyc - 1; dy = -1; } else cy -= 1; break;
         case 4: if (cy + 1 == B.Nyc) { cy = 0; dy = 1; } else cy += 1; break;
       }
-      __syncwarp();
+      G.sync();
       if (lane == 0) {
         int c = cy * B.Nxc + cx;
         int h = S.head[c];
@@ -689,28 +798,28 @@ __device__ void run_system(const SysDev& S, const RunArgs& A, int64_t max_coll, 
         S.head[c] = i;
         if (h != NIL) S.prv[h] = i;
       }
-      __syncwarp();
+      G.sync();
       ka = i; uq = N + i;
       pa = i;
     } else if (e == 2 * N + SP_SCREEN) {
       // ---------------- screenshot (takeAScreenshot 4657): free-fly everything
-      for (int i = lane; i < N; i += 32) {
+      for (int i = lane; i < N; i += GW) {
         Disk p = S.d[i];
         grow_fly(S, p, i, R.t, grow);
         S.d[i] = p;
       }
-      __syncwarp();
+      G.sync();
       se0 = e; sT0 = R.t + S.dtime;
       la = N + SP_SCREEN;
       if (A.flags & EDMD_F_STOP_AT_SCREEN) { stop = EDMD_STOP_SCREEN; }
     } else if (e == 2 * N + SP_THERMO) {
-      gather_virial(R, ctl);
-      do_thermo(S, R, lane);
+      gather_virial(R, ctl, G);
+      do_thermo(S, R, G);
       ctl = R.collT[lane & 3];
       se0 = e; sT0 = R.t + S.dtimeTh;
       la = N + SP_THERMO;
     } else {
-      do_growstop(S, R, lane, sm, &ovl, &oa, &ob);
+      do_growstop(S, R, G, sm, &ovl, &oa, &ob);
       if (A.flags & EDMD_F_STOP_AT_GROW) stop = EDMD_STOP_GROW;
     }
     // the tail shared by the handlers: new crossing events of the one or two
@@ -722,55 +831,57 @@ __device__ void run_system(const SysDev& S, const RunArgs& A, int64_t max_coll, 
       const int k = (lane & 1) && kb >= 0 ? kb : ka;
       const Disk dk = S.d[k];
       int dir;
-      const double tc = crossing_time_lanes(B, dk, S.cx[k], S.cy[k], R.t, lane, 2, &dir);
-      schedule2(S, R, ka, __shfl_sync(FULL, tc, 0), __shfl_sync(FULL, dir, 0), 0,
-                kb, __shfl_sync(FULL, tc, 1), __shfl_sync(FULL, dir, 1), 0, lane);
-      unqueue(S, R, uq, lane);
+      const double tc = crossing_time_grp(B, dk, S.cx[k], S.cy[k], R.t, G, 2, &dir);
+      schedule2(S, R, ka, G.shfl(tc, 0), G.shfl(dir, 0), 0,
+                kb, G.shfl(tc, 1), G.shfl(dir, 1), 0, G);
+      unqueue(S, R, uq, G);
     }
     if (pa >= 0) {
       Pred r0, r1;
-      predict2(S, R, pa, pb, r0, r1, lane, sm, &ovl, &oa, &ob);
+      predict2(S, R, pa, pb, r0, r1, G, sm, &ovl, &oa, &ob);
       const double tn = R.t + ((lane & 1) ? r1.dt : r0.dt);
-      se0 = N + pa; sT0 = __shfl_sync(FULL, tn, 0); sj0 = r0.partner; sca0 = r0.ca;
-      if (pb >= 0) { se1 = N + pb; sT1 = __shfl_sync(FULL, tn, 1); sj1 = r1.partner; sca1 = r1.ca; }
+      se0 = N + pa; sT0 = G.shfl(tn, 0); sj0 = r0.partner; sca0 = r0.ca;
+      if (pb >= 0) { se1 = N + pb; sT1 = G.shfl(tn, 1); sj1 = r1.partner; sca1 = r1.ca; }
       la = pa;
       lb = pb;
     }
-    if (se0 >= 0) schedule2(S, R, se0, sT0, sj0, sca0, se1, sT1, sj1, sca1, lane);
-    __syncwarp();
+    if (se0 >= 0) schedule2(S, R, se0, sT0, sj0, sca0, se1, sT1, sj1, sca1, G);
+    G.sync();
     for (int q = 0; q < 2; q++) {
       const int lf = q ? lb : la;
       if (lf < 0) break;
-      leaf_update(S, lf, lane);
+      leaf_update(S, lf, G);
     }
     if (ovl) { status = EDMD_ERR_OVERLAP; break; }
     if (stop) break;
   }
-  gather_virial(R, ctl);
+  gather_virial(R, ctl, G);
   R.stop_reason = stop;
   R.status = status;
   if (ovl) { R.err_a = oa; R.err_b = ob; }
   if (lane == 0) *S.st = R;
-  __syncwarp();
+  G.sync();
 }
 
-// Persistent launch: warps pull systems from a counter, in A.order, and
-// record each system's run time (globaltimer) for the next call's order.
+// Persistent launch: lane groups (GW lanes, one system each) pull systems
+// from a counter, in A.order, and record each system's run time
+// (globaltimer) for the next call's order.
+template <int GW>
 __global__ void __launch_bounds__(32 * WARPS_PER_BLOCK, 4)
 k_run(const SysDev* __restrict__ sys, RunArgs A) {
-  __shared__ WarpSmem smem[WARPS_PER_BLOCK];
-  const int lane = threadIdx.x & 31;
-  const int w = threadIdx.x >> 5;
+  __shared__ WarpSmem smem[WARPS_PER_BLOCK * (32 / GW)];
+  const Grp<GW> G(threadIdx.x);
+  WarpSmem* sm = &smem[threadIdx.x / GW];
   for (;;) {
     int it = 0;
-    if (lane == 0) it = atomicAdd(A.work, 1);
-    it = __shfl_sync(FULL, it, 0);
+    if (G.lane == 0) it = atomicAdd(A.work, 1);
+    it = G.shfl(it, 0);
     if (it >= A.nsys) break;
     const int s = A.order ? A.order[it] : it;
     unsigned long long t0 = 0, t1 = 0;
     if (A.cost) asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
-    run_system(sys[s], A, A.max_coll, lane, &smem[w]);
-    if (A.cost && lane == 0) {
+    run_system(sys[s], A, A.max_coll, G, sm);
+    if (A.cost && G.lane == 0) {
       asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t1));
       const unsigned long long c = (t1 - t0) >> 10;
       A.cost[s] = c > 0xffffffffull ? 0xffffffffu : (uint32_t)c;
@@ -936,7 +1047,7 @@ __global__ void __launch_bounds__(256) k_tree_build(const SysDev* __restrict__ s
     for (int par = w; par < S.lev_cnt[h]; par += nw) {
       const int ch = (par << 5) + lane;
       Node c = ch < S.lev_cnt[h - 1] ? S.tree[S.lev_off[h - 1] + ch] : empty_node(0x7fffffff);
-      warp_min(c);
+      grp_min(c, Grp<32>(threadIdx.x));
       if (lane == 0) S.tree[S.lev_off[h] + par] = c;
     }
     __syncthreads();
@@ -973,6 +1084,7 @@ __global__ void k_gather(const Disk* __restrict__ d, int64_t total, double* __re
 
 static int g_engine = EDMD_ENGINE_AUTO;
 static int g_lane_threads = 32;
+static int g_group = 32;                        // warp engine: lanes per system
 
 extern "C" int edmd_set_engine(int32_t kind) {
   if (kind < EDMD_ENGINE_AUTO || kind > EDMD_ENGINE_LANE) return EDMD_ERR_ARG;
@@ -983,6 +1095,12 @@ extern "C" int edmd_set_engine(int32_t kind) {
 extern "C" int edmd_set_lane_threads(int32_t threads_per_block) {
   if (threads_per_block < 1 || threads_per_block > 1024) return EDMD_ERR_ARG;
   g_lane_threads = threads_per_block;
+  return EDMD_OK;
+}
+
+extern "C" int edmd_set_warp_group(int32_t lanes) {
+  if (lanes != 16 && lanes != 32) return EDMD_ERR_ARG;
+  g_group = lanes;
   return EDMD_OK;
 }
 
@@ -1203,15 +1321,18 @@ extern "C" int edmd_advance(edmd_ctx* ctx, int64_t max_coll, double t_stop, uint
     CK(cudaGetDevice(&dev));
     CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
     int per_sm = 0;
-    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_run, 32 * WARPS_PER_BLOCK, 0));
-    int want = (ctx->nsys + WARPS_PER_BLOCK - 1) / WARPS_PER_BLOCK;
+    const int gw = g_group;                     // lanes per system: 16 or 32
+    const int per_block = WARPS_PER_BLOCK * (32 / gw);
+    if (gw == 16) CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_run<16>, 32 * WARPS_PER_BLOCK, 0));
+    else CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_run<32>, 32 * WARPS_PER_BLOCK, 0));
+    int want = (ctx->nsys + per_block - 1) / per_block;
     int grid = per_sm * nsm;
     if (grid > want) grid = want;
     if (grid < 1) grid = 1;
     // more systems than resident warps: with one item per system the last
     // wave runs on part of the GPU; chunks of the collision budget let the
     // warps share the remaining work evenly (same events, same results)
-    const int64_t resident = (int64_t)grid * WARPS_PER_BLOCK;
+    const int64_t resident = (int64_t)grid * per_block;
     if (ctx->nsys > resident) {
       // more systems than resident warps: the systems that took longest in
       // the previous call start first (longest processing time first), so the
@@ -1228,7 +1349,8 @@ extern "C" int edmd_advance(edmd_ctx* ctx, int64_t max_coll, double t_stop, uint
       A.order = ctx->order;
     }
     CK(cudaEventRecord(ctx->e0, ctx->stream));
-    k_run<<<grid, 32 * WARPS_PER_BLOCK, 0, ctx->stream>>>(ctx->ds, A);
+    if (gw == 16) k_run<16><<<grid, 32 * WARPS_PER_BLOCK, 0, ctx->stream>>>(ctx->ds, A);
+    else k_run<32><<<grid, 32 * WARPS_PER_BLOCK, 0, ctx->stream>>>(ctx->ds, A);
   }
   CK(cudaGetLastError());
   CK(cudaEventRecord(ctx->e1, ctx->stream));
@@ -1538,7 +1660,7 @@ extern "C" int edmd_run_noalloc(const edmd_system_desc* desc, double* x, double*
   k_tree_build<<<1, 256, 0, st>>>(dsys, 1);
   if (cudaMemsetAsync(work, 0, sizeof(int32_t), st) != cudaSuccess)
     return noalloc_fail(EDMD_ERR_CUDA, "edmd_run_noalloc: memset failed");
-  k_run<<<1, 32 * WARPS_PER_BLOCK, 0, st>>>(dsys, A);
+  k_run<32><<<1, 32 * WARPS_PER_BLOCK, 0, st>>>(dsys, A);
   k_sync<<<1, 256, 0, st>>>(dsys, 1);
   k_noalloc_out<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(dsys, x, y, vx, vy);
   cudaError_t ce = cudaGetLastError();

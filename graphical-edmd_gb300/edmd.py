@@ -58,6 +58,7 @@ EXPORTS = [
     "edmd_get_pcf", "edmd_get_state",
     "edmd_get_states", "edmd_get_counters", "edmd_get_all_counters", "edmd_get_virial",
     "edmd_get_thermo", "edmd_get_trace", "edmd_set_engine", "edmd_set_lane_threads",
+    "edmd_set_warp_group",
     "edmd_get_engine", "edmd_set_device", "edmd_host_alloc", "edmd_host_free", "edmd_run_noalloc",
     "edmd_set_log_capacity", "edmd_clear_log", "edmd_get_log", "edmd_checkpoint_save",
     "edmd_checkpoint_restore", "edmd_tangent_run", "edmd_msd_gradient", "edmd_destroy",
@@ -107,6 +108,7 @@ def load(path=LIB_PATH):
     L.edmd_run_noalloc.argtypes = [C.POINTER(SystemDesc)] + [C.c_void_p] * 6 + [
         C.c_int64, C.c_double, C.POINTER(C.c_int64), C.POINTER(C.c_double), C.c_void_p]
     L.edmd_set_lane_threads.argtypes = [C.c_int32]
+    L.edmd_set_warp_group.argtypes = [C.c_int32]
     L.edmd_get_engine.argtypes = [C.c_void_p]
     L.edmd_sync.argtypes = [C.c_void_p]
     L.edmd_get_state.argtypes = [C.c_void_p, C.c_int32] + [C.c_void_p] * 8
@@ -182,6 +184,13 @@ def default_desc(N, Lx, Ly, vr_base=0.0, tmax=4000.0, dtime=100.0, dtime_thermo=
     d = SystemDesc()
     load().edmd_default_desc(C.byref(d), N, Lx, Ly, vr_base, tmax, dtime, dtime_thermo)
     return d
+
+
+def set_warp_group(lanes):
+    """Lanes per system of the warp engine, 16 or 32 (edmd_set_warp_group)."""
+    rc = load().edmd_set_warp_group(int(lanes))
+    if rc != 0:
+        raise ValueError("lanes must be 16 or 32")
 
 
 # ------------------------------------------------------------------ engine

@@ -215,6 +215,11 @@ int edmd_get_trace(edmd_ctx* ctx, int32_t sys, edmd_collision* out, int64_t cap,
  * the reference's exact order and give bit-identical results. */
 int edmd_set_engine(int32_t kind);
 int edmd_set_lane_threads(int32_t threads_per_block);
+
+/* Lanes per system of the warp engine: 32 (one system per warp, the
+ * default) or 16 (two systems per warp).  Both give identical results; on the
+ * 4096-system batch 32 lanes run 6.2e7 coll/s and 16 lanes 5.9e7. */
+int edmd_set_warp_group(int32_t lanes);
 int edmd_get_engine(const edmd_ctx* ctx);
 
 /* Select the CUDA device used by contexts created afterwards in this thread

@@ -104,3 +104,28 @@ def test_batch_larger_than_resident_warps(edmd, oracle):
         for k in ("x", "y", "vx", "vy"):
             np.testing.assert_array_equal(st[k], o.state()[k])
     eng.close()
+
+
+@pytest.mark.parametrize("lanes", [32, 16])
+def test_warp_group_widths_match_reference(edmd, lanes):
+    """One system per warp (32 lanes) and two per warp (16 lanes each): the
+    same collisions, cells, times and states as the reference."""
+    try:
+        edmd.set_warp_group(lanes)
+        names = golden_names()
+        gs = [golden(n) for n in names]
+        L = min(len(g["ct"]) for g in gs)
+        systems = [system_from_golden(edmd, g) for g in gs] * 5
+        eng = edmd.Engine(systems, trace_cap=L + 16)
+        for g in gs:
+            assert len(g["ct"]) >= L
+        eng.advance(max_coll=L, flags=edmd.F_TRACE)
+        eng.sync()
+        for s, g in enumerate(gs * 5):
+            tr = eng.trace(s)
+            assert len(tr) == L
+            for k, gk in (("i", "ci"), ("j", "cj"), ("cell_i", "ccell_i"), ("cell_j", "ccell_j"), ("t", "ct")):
+                np.testing.assert_array_equal(tr[k], g[gk][:L])
+        eng.close()
+    finally:
+        edmd.set_warp_group(32)
