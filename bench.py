@@ -397,6 +397,37 @@ def measure(edmd, a, workload, engine, coll, steps, warmup, rank, world, dist, d
                           "peak_source": "measured hbm_gbs" if "hbm_gbs" in peaks else "fallback"})
 
 
+def measure_differentiation(edmd, ncoll=10000):
+    """The tangent and adjoint forms on one 1024-disk Hex system at phi = 0.60:
+    32 tangent vectors re-orthonormalised every 100 collisions (Lyapunov
+    spectrum), and the adjoint of the final mean-square displacement with
+    checkpoints every 500 collisions.  Accepted collisions per second of each
+    call, host-timed around the synchronous C-ABI call."""
+    try:
+        s = edmd.hex_start(1024, 0.60, 11)
+        s["desc"] = edmd.default_desc(s["N"], s["Lx"], s["Ly"])
+        eng = edmd.Engine([s])
+        eng.advance(max_coll=2000)                       # untimed: leave the lattice
+        eng.tangent(32, 1000, qr_every=100, seed=17)     # warm-up
+        t0 = time.perf_counter()
+        _, lam = eng.tangent(32, ncoll, qr_every=100, seed=17)
+        t_tan = time.perf_counter() - t0
+        eng.msd_gradient(1000, ckpt_every=500)           # warm-up
+        t0 = time.perf_counter()
+        eng.msd_gradient(ncoll, ckpt_every=500)
+        t_adj = time.perf_counter() - t0
+        eng.close()
+        return {"config": "single Hex system, N=1024, phi=0.60, %d collisions per call" % ncoll,
+                "tangent": {"metric": "collisions/s, 32 tangent vectors, CholQR2 every 100 collisions",
+                            "value": ncoll / t_tan, "unit": UNIT, "lambda_max": float(lam.max())},
+                "adjoint": {"metric": "collisions/s, adjoint of the final MSD (forward + reverse), "
+                                      "checkpoints every 500 collisions",
+                            "value": ncoll / t_adj, "unit": UNIT},
+                "timing": "host wall clock around the synchronous call"}
+    except Exception as e:                               # the main line stands without it
+        return {"error": repr(e)[:200]}
+
+
 def run_ours(a, rank, world, dist):
     cpu_pool = None
     ncores = os.cpu_count() or 1
@@ -422,6 +453,7 @@ def run_ours(a, rank, world, dist):
                                  "ms_per_step": s["ms_per_step"], "e2e": s["e2e"],
                                  "roofline": s["roofline"], "clocks": s["clocks"],
                                  "gpu_launches": s["launches"]}
+        other["differentiation"] = measure_differentiation(edmd)
     if rank != 0:
         if cpu_pool:
             cpu_pool.close()
