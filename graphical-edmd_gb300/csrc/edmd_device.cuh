@@ -146,17 +146,6 @@ __device__ __forceinline__ double pbc_in_y(const Box& B, double d) {  // PBCinsi
 __device__ __forceinline__ int pbc_cx(const Box& B, int a) { return a < 0 ? a + B.Nxc : (a >= B.Nxc ? a - B.Nxc : a); }
 __device__ __forceinline__ int pbc_cy(const Box& B, int a) { return a < 0 ? a + B.Nyc : (a >= B.Nyc ? a - B.Nyc : a); }
 
-// freeFlyNormal src/EDMD.c:4954 / freeFlyGrow 4992 (rad advanced separately)
-__device__ __forceinline__ void free_fly(const Box& B, Disk& p, double t) {
-  double dt = t - p.tl;
-  p.tl = t;
-  p.x += dt * p.vx;
-  p.y += dt * p.vy;
-  if (p.x < 0) p.x += B.Lx;
-  else if (p.x >= B.Lx) p.x -= B.Lx;
-  if (p.y < 0) p.y += B.Ly;
-  else if (p.y >= B.Ly) p.y -= B.Ly;
-}
 
 // collisionTimeNormal src/EDMD.c:2661-2723; p1 is current at t.
 // *overlap is set when the pair overlaps by more than 0.01 (2708-2717).
@@ -262,6 +251,8 @@ __device__ __forceinline__ void pbc_i(const Box& B, double& dx, double& dy) {
   if (ge_pos(dy, B.hLy)) dy -= B.Ly;
   else if (lt_neg(dy, B.hLy)) dy += B.Ly;
 }
+// freeFlyNormal src/EDMD.c:4954 / freeFlyGrow 4992 (rad advanced separately),
+// the wrap tests on the integer pipe
 __device__ __forceinline__ void free_fly_i(const Box& B, Disk& p, double t) {
   double dt = t - p.tl;
   p.tl = t;
