@@ -135,7 +135,8 @@ __device__ void unqueue(const SysDev& S, Lane& W, int e) {
 __device__ void do_wrap(const SysDev& S, Lane& W) {
   int e = W.R.ovf;
   W.R.ovf = NIL;
-  while (e != NIL) {
+  int guard = 0;                       // the overflow list holds at most 2N + 3 events
+  while (e != NIL && guard++ <= 2 * S.B.N + NSPECIAL) {
     int n = S.on[e];
     Ev ev = S.ev[e];
     schedule(S, W, e, ev.t, ev.j, ev.ca, 0ull);
@@ -167,7 +168,8 @@ __device__ void predict(const SysDev& S, Lane& W, int a, double* dt_out, int* p_
   for (int q = 0; q < 9; q++) {
     int cell = pbc_cy(B, Y + q / 3 - 1) * B.Nxc + pbc_cx(B, X + q % 3 - 1);
     int p = S.head[cell];
-    while (p != NIL) {
+    int guard = 0;                     // a list is never longer than N
+    while (p != NIL && guard++ < B.N) {
       Disk P = S.d[p];
       if (p != a) {
         double d = grow ? coll_time_grow(B, A, vra, P, S.vr[p], W.R.t, &ovl)
