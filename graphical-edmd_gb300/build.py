@@ -3,6 +3,8 @@
 Produces, in this directory:
   libedmd_gpu.so  C ABI of include/edmd_gpu.h + include/edmd_host.h
   edmd            drop-in command-line driver (host/edmd_main.c), rpath to the .so
+and, only with `python build.py probe`, the measurement tool peak_probe
+(probe/peak_probe.cu: FP64 issue rate and load latency).
 
 All CUDA is compiled for sm_103a only, with --fmad=false so that no
 floating-point multiply-add is contracted (the event arithmetic must round
@@ -74,10 +76,6 @@ def build(verbose=False):
     if _newer(lib, objs):
         _run_all([[_nvcc(), "-gencode", "arch=compute_103a,code=sm_103a", "-shared", "-o", lib]
                   + objs + ["-lcudart", "-lm"]])
-    probe_src = os.path.join(CSRC, "peak_probe.cu")
-    probe = os.path.join(HERE, "peak_probe")
-    if _newer(probe, [probe_src, __file__]):
-        _run_all([[_nvcc(), "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-o", probe, probe_src]])
     main_src = os.path.join(HOST, "edmd_main.c")
     exe = os.path.join(HERE, "edmd")
     if os.path.exists(main_src) and _newer(exe, [main_src, lib] + headers):
@@ -86,6 +84,16 @@ def build(verbose=False):
     return lib
 
 
+def build_probe():
+    """The FP64/FP32 issue-rate and load-latency microbenchmark behind the
+    engines' FP64 roofline (not part of the library): ./peak_probe."""
+    src = os.path.join(HERE, "probe", "peak_probe.cu")
+    exe = os.path.join(HERE, "peak_probe")
+    if _newer(exe, [src, __file__]):
+        _run_all([[_nvcc(), "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-o", exe, src]])
+    return exe
+
+
 if __name__ == "__main__":
-    print(build(verbose=True))
+    print(build_probe() if sys.argv[1:] == ["probe"] else build(verbose=True))
     sys.exit(0)

@@ -1,6 +1,7 @@
 // edmd_ctx.h -- host-side context shared by the engine translation units
 // (internal; the public interface is include/edmd_gpu.h).
 #pragma once
+#include <cstddef>
 #include <string>
 #include <vector>
 #include <cuda_runtime.h>
@@ -15,6 +16,8 @@ struct edmd_ctx {
   int maxN = 0;
   cudaStream_t stream = nullptr;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaEvent_t c0 = nullptr, c1 = nullptr;  // whole-call timing of the differentiation drivers
+  float last_ms = 0;                       // device time of the last timed call (edmd_get_last_ms)
   std::vector<SysDev> hs;
   std::vector<edmd_system_desc> desc;
   std::vector<int64_t> disk_off, cell_off;
@@ -66,6 +69,55 @@ static inline int set_err(edmd_ctx* c, int code, const std::string& m) {
   } while (0)
 
 static inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+// status, err_a, err_b of every system (three consecutive int32 of SysState)
+// after the context's stream; the first system in an error state sets the
+// context's message, naming the disks involved, and its status is returned.
+// `what` prefixes the message ("initial configuration", "advance", ...).
+static inline int report_status(edmd_ctx* ctx, const char* what) {
+  struct Trip { int32_t status, a, b; };
+  static_assert(offsetof(SysState, err_b) == offsetof(SysState, status) + 8, "status layout");
+  std::vector<Trip> st(ctx->nsys);
+  cudaError_t e = cudaMemcpy2DAsync(st.data(), sizeof(Trip), &ctx->st[0].status, sizeof(SysState), sizeof(Trip),
+                                    ctx->nsys, cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) return set_err(ctx, EDMD_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+  for (int s = 0; s < ctx->nsys; s++) {
+    const Trip& t = st[s];
+    if (t.status == EDMD_OK) continue;
+    std::string m = std::string(what) + ": system " + std::to_string(s);
+    if (t.status == EDMD_ERR_OVERLAP)
+      m += " has overlapping disks " + std::to_string(t.a) + (t.b >= 0 ? " and " + std::to_string(t.b) : "");
+    else if (t.status == EDMD_ERR_BUDGET && (t.a == -2 || t.b == -2))
+      m += " has a corrupt cell list (a list walk exceeded N; seen from disk " +
+           std::to_string(t.a == -2 ? t.b : t.a) + ")";
+    else if (t.status == EDMD_ERR_BUDGET)
+      m += " exhausted its event budget";
+    else if (t.status == EDMD_ERR_ARG)
+      m += " has an invalid disk " + std::to_string(t.a);
+    else
+      m += " stopped with status " + std::to_string(t.status);
+    return set_err(ctx, t.status, m);
+  }
+  return EDMD_OK;
+}
+
+// CUDA events on the context's stream around a whole host-driven call (the
+// differentiation drivers launch many kernels with host work in between):
+// call_begin records the start, call_end the end and stores the elapsed time,
+// idle gaps of the stream included, in last_ms.
+static inline cudaError_t call_begin(edmd_ctx* c) {
+  cudaError_t e = cudaSuccess;
+  if (!c->c0) e = cudaEventCreate(&c->c0);
+  if (e == cudaSuccess && !c->c1) e = cudaEventCreate(&c->c1);
+  return e == cudaSuccess ? cudaEventRecord(c->c0, c->stream) : e;
+}
+static inline cudaError_t call_end(edmd_ctx* c) {
+  cudaError_t e = cudaEventRecord(c->c1, c->stream);
+  if (e == cudaSuccess) e = cudaEventSynchronize(c->c1);
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&c->last_ms, c->c0, c->c1);
+  return e;
+}
 
 // Copies and sets ordered after everything queued on the context's stream.
 // The stream is non-blocking, so a plain cudaMemcpy on the legacy default

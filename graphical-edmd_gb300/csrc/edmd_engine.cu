@@ -255,8 +255,9 @@ __device__ void unqueue(const SysDev& S, SysState& R, int e, const Grp<GW>& G) {
 
 // the overflow bucket is redistributed when the calendar wraps
 // (addNextPaulEvent src/EDMD.c:2287-2300)
+// (false: the list is longer than it can be, i.e. corrupt)
 template <int GW>
-__device__ __noinline__ void do_wrap(const SysDev& S, SysState& R, const Grp<GW>& G) {
+__device__ __noinline__ bool do_wrap(const SysDev& S, SysState& R, const Grp<GW>& G) {
   const int N = S.B.N;
   int e = R.ovf;
   R.ovf = NIL;
@@ -273,11 +274,13 @@ __device__ __noinline__ void do_wrap(const SysDev& S, SysState& R, const Grp<GW>
     leaf_update(S, leaf, G);
     e = n;
   }
+  return e == NIL;
 }
 
 // ---------------------------------------------------------------- prediction
 
 struct Pred { double dt; int32_t partner; uint32_t ca; };
+constexpr int OVL_CORRUPT = -2;  // overlap marker: a cell list longer than N (EDMD_ERR_BUDGET)
 
 __device__ __forceinline__ void grow_fly(const SysDev& S, Disk& p, int i, double t, bool grow) {
   double dt = t - p.tl;
@@ -329,6 +332,7 @@ __device__ void predict2(const SysDev& S, SysState& R, int a0, int a1, Pred& r0,
   int p0 = v0 ? S.head[task_cell(o0, q0)] : NIL;
   int p1 = v1 ? S.head[task_cell(o1, q1)] : NIL;
   int c0 = 0, c1 = 0;
+  bool lcorrupt = false;
   {
     int guard = 0;                   // the lists hold N disks in all
     while ((p0 != NIL || p1 != NIL) && guard++ < 2 * B.N) {
@@ -344,6 +348,9 @@ __device__ void predict2(const SysDev& S, SysState& R, int a0, int a1, Pred& r0,
       p0 = n0;
       p1 = n1;
     }
+    // a list longer than N is corrupt: reported like an overlap, with the
+    // marker OVL_CORRUPT in place of the first disk (EDMD_ERR_BUDGET)
+    if (p0 != NIL || p1 != NIL) { lcorrupt = true; }
   }
   const bool spill = G.any(c0 > MAXC || c1 > MAXC);
   Disk A0 = S.d[a0];
@@ -412,6 +419,7 @@ __device__ void predict2(const SysDev& S, SysState& R, int a0, int a1, Pred& r0,
         }
         p = P.nxt;
       }
+      if (p != NIL) lcorrupt = true;
       tot += k;
     }
     for (int o = GW / 2; o > 0; o >>= 1) tot += G.shfl_xor(tot, o);
@@ -438,6 +446,7 @@ __device__ void predict2(const SysDev& S, SysState& R, int a0, int a1, Pred& r0,
     *ovl_a = G.shfl(la, src);
     *ovl_b = G.shfl(lb, src);
   }
+  if (G.any(lcorrupt)) { *ovl = true; *ovl_a = OVL_CORRUPT; *ovl_b = a0; }
 }
 
 // ---------------------------------------------------------------- handlers
@@ -619,7 +628,7 @@ __device__ void run_system(const SysDev& S, const RunArgs& A, int64_t max_coll, 
       if (r.b == BINF || (uint64_t)r.b >= R.next_wrap) {
         if (r.b == BINF && R.ovf == NIL) { status = EDMD_ERR_BUDGET; break; }
         while (R.k < R.next_wrap) { R.P += B.dtP; R.k++; }
-        do_wrap(S, R, G);
+        if (!do_wrap(S, R, G)) { status = EDMD_ERR_BUDGET; break; }
         R.next_wrap += (uint64_t)N;
         if (++guard > (1 << 20)) { status = EDMD_ERR_BUDGET; break; }
         continue;
@@ -852,7 +861,7 @@ __device__ void run_system(const SysDev& S, const RunArgs& A, int64_t max_coll, 
       if (lf < 0) break;
       leaf_update(S, lf, G);
     }
-    if (ovl) { status = EDMD_ERR_OVERLAP; break; }
+    if (ovl) { status = oa == OVL_CORRUPT ? EDMD_ERR_BUDGET : EDMD_ERR_OVERLAP; break; }
     if (stop) break;
   }
   gather_virial(R, ctl, G);
@@ -917,6 +926,7 @@ __global__ void k_init_events(const SysDev* __restrict__ sys) {
     double bd = grow ? 10000000 : NEVER;
     int bp = 0;
     bool ov = false;
+    int ovp = -1;                     // first partner found overlapping
     int X = S.cx[i], Y = S.cy[i];
     uint64_t np = 0;
     for (int q = 0; q < 9; q++) {
@@ -924,8 +934,11 @@ __global__ void k_init_events(const SysDev* __restrict__ sys) {
       for (int p = S.head[cell]; p != NIL; p = S.d[p].nxt) {
         if (p == i) continue;
         Disk P = S.d[p];
-        double d = grow ? coll_time_grow(B, A, S.vr[i], P, S.vr[p], 0.0, &ov)
-                        : coll_time_normal(B, A, P, 0.0, &ov);
+        bool o2 = false;
+        double d = grow ? coll_time_grow(B, A, S.vr[i], P, S.vr[p], 0.0, &o2)
+                        : coll_time_normal(B, A, P, 0.0, &o2);
+        if (o2 && ovp < 0) ovp = p;
+        ov |= o2;
         np++;
         if (bd > d) { bd = d; bp = p; }
       }
@@ -934,7 +947,11 @@ __global__ void k_init_events(const SysDev* __restrict__ sys) {
     key(el, el.t, (uint64_t)nspec + 2ull * i + 1);
     S.ev[N + i] = el;
     atomicAdd((unsigned long long*)&S.st->npair, (unsigned long long)np);
-    if (ov) { S.st->status = EDMD_ERR_OVERLAP; S.st->err_a = i; }
+    // one thread (the first to claim the status) names the pair
+    if (ov && atomicCAS(&S.st->status, EDMD_OK, EDMD_ERR_OVERLAP) == EDMD_OK) {
+      S.st->err_a = i;
+      S.st->err_b = ovp;
+    }
   } else if (i == N) {
     // thermo, [growth stop], screenshot in eventListInit order
     Ev e; e.j = 0; e.ca = 0;
@@ -1185,16 +1202,7 @@ static int stage_all(edmd_ctx* ctx, const double* x, const double* y, const doub
   else k_tree_build<<<ctx->nsys, 256, 0, sm>>>(ctx->ds, ctx->nsys);
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(sm));   // host staging vectors go out of scope
-  std::vector<int32_t> status(ctx->nsys);
-  for (int s = 0; s < ctx->nsys; s++) status[s] = 0;
-  CK(sync_copy2d(ctx, status.data(), 4, &ctx->st[0].status, sizeof(SysState), 4, ctx->nsys,
-                  cudaMemcpyDeviceToHost));
-  for (int s = 0; s < ctx->nsys; s++)
-    if (status[s] != EDMD_OK)
-      return set_err(ctx, status[s], std::string("initial configuration of system ") + std::to_string(s) +
-                                         (status[s] == EDMD_ERR_OVERLAP ? " has overlapping disks"
-                                                                        : " could not be queued"));
-  return EDMD_OK;
+  return report_status(ctx, "initial configuration");
 }
 
 extern "C" int edmd_create(int32_t nsys, const edmd_system_desc* desc, const double* x,
@@ -1355,17 +1363,9 @@ extern "C" int edmd_advance(edmd_ctx* ctx, int64_t max_coll, double t_stop, uint
   CK(cudaGetLastError());
   CK(cudaEventRecord(ctx->e1, ctx->stream));
   CK(cudaEventSynchronize(ctx->e1));
-  if (elapsed_ms) CK(cudaEventElapsedTime(elapsed_ms, ctx->e0, ctx->e1));
-  std::vector<int32_t> status(ctx->nsys);
-  CK(sync_copy2d(ctx, status.data(), 4, &ctx->st[0].status, sizeof(SysState), 4, ctx->nsys,
-                  cudaMemcpyDeviceToHost));
-  for (int s = 0; s < ctx->nsys; s++)
-    if (status[s] != EDMD_OK) {
-      char b[128];
-      snprintf(b, sizeof b, "system %d stopped with status %d", s, status[s]);
-      return set_err(ctx, status[s], b);
-    }
-  return EDMD_OK;
+  CK(cudaEventElapsedTime(&ctx->last_ms, ctx->e0, ctx->e1));
+  if (elapsed_ms) *elapsed_ms = ctx->last_ms;
+  return report_status(ctx, "advance");
 }
 
 extern "C" int edmd_sync(edmd_ctx* ctx) {
@@ -1497,6 +1497,8 @@ extern "C" int edmd_destroy(edmd_ctx* ctx) {
   if (ctx->logbuf) cudaFree(ctx->logbuf);
   if (ctx->e0) cudaEventDestroy(ctx->e0);
   if (ctx->e1) cudaEventDestroy(ctx->e1);
+  if (ctx->c0) cudaEventDestroy(ctx->c0);
+  if (ctx->c1) cudaEventDestroy(ctx->c1);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
   return EDMD_OK;
@@ -1504,6 +1506,12 @@ extern "C" int edmd_destroy(edmd_ctx* ctx) {
 
 extern "C" int edmd_get_engine(const edmd_ctx* ctx) {
   return ctx ? ctx->engine : -1;
+}
+
+extern "C" int edmd_get_last_ms(const edmd_ctx* ctx, float* ms) {
+  if (!ctx || !ms) return EDMD_ERR_ARG;
+  *ms = ctx->last_ms;
+  return EDMD_OK;
 }
 
 // ==================================================================== allocation-free entry point
@@ -1521,6 +1529,8 @@ constexpr int64_t NOALLOC_MAX_N = 8192;        // disks per call
 constexpr int64_t NOALLOC_MAX_CELLS = 65536;   // Nxcells * Nycells per call
 constexpr size_t NOALLOC_BYTES = (size_t)4 << 20;
 constexpr int NOALLOC_MAX_DEVICES = 64;
+// event budget of one call (see edmd_run_noalloc)
+constexpr int64_t NOALLOC_EVENTS_PER_COLL = 256, NOALLOC_EVENTS_PER_DISK = 256, NOALLOC_EVENTS_BASE = 1 << 20;
 }
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_BYTES];
@@ -1534,7 +1544,12 @@ __global__ void k_noalloc_put(SysDev s, SysDev* dst) {
 }
 
 // disk records, cell lists (index order, push-front as addToCell) and the
-// scalar state from the caller's device arrays; one thread, N <= 8192
+// scalar state from the caller's device arrays; one thread, N <= 8192.
+// A position outside [0, Lx) x [0, Ly) (or a NaN) is an argument error, as in
+// edmd_create: the scalar state gets status EDMD_ERR_ARG with the first such
+// disk in err_a, the event loop then does nothing, and the host reports it.
+// The cell index is still clamped into the grid so that the initial
+// predictions that run before the loop stay inside the arrays.
 __global__ void k_noalloc_stage(const SysDev* __restrict__ sys, const double* x, const double* y,
                                 const double* vx, const double* vy, const double* rad,
                                 const double* m, double first_screen, double first_thermo) {
@@ -1542,16 +1557,18 @@ __global__ void k_noalloc_stage(const SysDev* __restrict__ sys, const double* x,
   const SysDev& S = sys[0];
   const Box& B = S.B;
   const int N = B.N;
+  int bad = -1;
   for (int c = 0; c < B.Nxc * B.Nyc; c++) S.head[c] = NIL;
   for (int i = 0; i < N; i++) {
     Disk q;
     q.x = x[i]; q.y = y[i]; q.vx = vx[i]; q.vy = vy[i]; q.tl = 0; q.rad = rad[i]; q.m = m[i];
     q.coll = 0;
+    if (bad < 0 && !(q.x >= 0 && q.x < B.Lx && q.y >= 0 && q.y < B.Ly)) bad = i;
     int X = (int)(q.x * B.cxf), Y = (int)(q.y * B.cyf);
-    if (X >= B.Nxc) X = B.Nxc - 1;
-    if (Y >= B.Nyc) Y = B.Nyc - 1;
-    if (X < 0) X = 0;
-    if (Y < 0) Y = 0;
+    if (!(X < B.Nxc)) X = B.Nxc - 1;
+    if (!(Y < B.Nyc)) Y = B.Nyc - 1;
+    if (!(X >= 0)) X = 0;
+    if (!(Y >= 0)) Y = 0;
     S.cx[i] = X; S.cy[i] = Y; S.prv[i] = NIL;
     S.crossX[i] = 0; S.crossY[i] = 0;
     S.vr[i] = 0;
@@ -1566,6 +1583,7 @@ __global__ void k_noalloc_stage(const SysDev* __restrict__ sys, const double* x,
   st.lastThermo = first_thermo + 0.000000001;   // read by k_init_events
   st.collT[0] = -1;
   st.collT[1] = first_screen;
+  if (bad >= 0) { st.status = EDMD_ERR_ARG; st.err_a = bad; }
   *S.st = st;
 }
 
@@ -1651,7 +1669,13 @@ extern "C" int edmd_run_noalloc(const edmd_system_desc* desc, double* x, double*
     return noalloc_fail(EDMD_ERR_CAPACITY, "edmd_run_noalloc: system does not fit the 4 MiB scratch array");
   cudaStream_t st = (cudaStream_t)stream;
   RunArgs A;
-  A.max_coll = max_coll; A.t_stop = t_stop; A.flags = 0; A.max_events = (int64_t)1 << 60;
+  // a finite event budget: NOALLOC_EVENTS_PER_COLL events per requested
+  // collision plus NOALLOC_EVENTS_PER_DISK per disk (saturating), so that a
+  // loop whose clock stops advancing ends with EDMD_ERR_BUDGET
+  const int64_t cap = (int64_t)1 << 60;
+  const int64_t per_coll = max_coll > cap / NOALLOC_EVENTS_PER_COLL ? cap : max_coll * NOALLOC_EVENTS_PER_COLL;
+  const int64_t budget = std::min(cap, per_coll + (int64_t)N * NOALLOC_EVENTS_PER_DISK + NOALLOC_EVENTS_BASE);
+  A.max_coll = max_coll; A.t_stop = t_stop; A.flags = 0; A.max_events = budget;
   A.nsys = 1; A.work = work; A.order = nullptr; A.cost = nullptr;
   k_noalloc_put<<<1, 1, 0, st>>>(S, dsys);
   k_noalloc_stage<<<1, 32, 0, st>>>(dsys, x, y, vx, vy, rad, m, D.first_screen, D.first_thermo);
@@ -1671,9 +1695,15 @@ extern "C" int edmd_run_noalloc(const edmd_system_desc* desc, double* x, double*
   if (ce != cudaSuccess) return noalloc_fail(EDMD_ERR_CUDA, cudaGetErrorString(ce));
   if (ncol_out) *ncol_out = (int64_t)R.ncol;
   if (t_out) *t_out = R.t;
-  if (R.status != EDMD_OK)
-    return noalloc_fail(R.status, R.status == EDMD_ERR_OVERLAP ? "edmd_run_noalloc: overlapping disks"
-                                                               : "edmd_run_noalloc: event loop stopped");
+  if (R.status == EDMD_ERR_ARG)
+    return noalloc_fail(R.status, ("edmd_run_noalloc: position of disk " + std::to_string(R.err_a) +
+                                   " outside the box").c_str());
+  if (R.status == EDMD_ERR_OVERLAP)
+    return noalloc_fail(R.status, ("edmd_run_noalloc: overlapping disks " + std::to_string(R.err_a) + " and " +
+                                   std::to_string(R.err_b)).c_str());
+  if (R.status == EDMD_ERR_BUDGET)
+    return noalloc_fail(R.status, "edmd_run_noalloc: event budget exhausted (the state at the stop is written back)");
+  if (R.status != EDMD_OK) return noalloc_fail(R.status, "edmd_run_noalloc: event loop stopped");
   g_noalloc_err.clear();
   return EDMD_OK;
 }

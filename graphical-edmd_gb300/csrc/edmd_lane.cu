@@ -142,6 +142,7 @@ __device__ void do_wrap(const SysDev& S, Lane& W) {
     schedule(S, W, e, ev.t, ev.j, ev.ca, 0ull);
     e = n;
   }
+  if (e != NIL) W.status = EDMD_ERR_BUDGET;   // a longer list is corrupt
 }
 
 __device__ __forceinline__ void fly(const SysDev& S, Disk& p, int i, double t, bool grow) {
@@ -165,6 +166,7 @@ __device__ void predict(const SysDev& S, Lane& W, int a, double* dt_out, int* p_
   const int X = S.cx[a], Y = S.cy[a];
   uint64_t np = 0;
   bool ovl = false;
+  int ovp = -1;                        // first partner found overlapping
   for (int q = 0; q < 9; q++) {
     int cell = pbc_cy(B, Y + q / 3 - 1) * B.Nxc + pbc_cx(B, X + q % 3 - 1);
     int p = S.head[cell];
@@ -172,16 +174,20 @@ __device__ void predict(const SysDev& S, Lane& W, int a, double* dt_out, int* p_
     while (p != NIL && guard++ < B.N) {
       Disk P = S.d[p];
       if (p != a) {
-        double d = grow ? coll_time_grow(B, A, vra, P, S.vr[p], W.R.t, &ovl)
-                        : coll_time_normal_i(B, A, P, W.R.t, &ovl);
+        bool o2 = false;
+        double d = grow ? coll_time_grow(B, A, vra, P, S.vr[p], W.R.t, &o2)
+                        : coll_time_normal_i(B, A, P, W.R.t, &o2);
+        if (o2 && !ovl) ovp = p;
+        ovl |= o2;
         np++;
         if (time_key(bd) > time_key(d)) { bd = d; bp = p; bc = P.coll; any = true; }
       }
       p = P.nxt;
     }
+    if (p != NIL) { W.status = EDMD_ERR_BUDGET; W.R.err_a = -2; W.R.err_b = a; }  // longer than N: corrupt
   }
   if (!any) bc = S.d[0].coll;
-  if (ovl) { W.status = EDMD_ERR_OVERLAP; W.R.err_a = a; }
+  if (ovl) { W.status = EDMD_ERR_OVERLAP; W.R.err_a = a; W.R.err_b = ovp; }
   W.R.npair += np;
   W.R.npred++;
   *dt_out = bd; *p_out = bp; *ca_out = bc;

@@ -53,6 +53,7 @@ constexpr int TX = 32, TY = 8;        // selection tile (cells)
 constexpr int RTILE = 12;             // largest window radius of the tile kernel
 constexpr int MAXDIRTY = 8;           // cells whose minimum one event can change
 constexpr int MAXC = 8;               // candidates buffered per cell list per lane
+constexpr int OB_CORRUPT = -2;        // overlap partner marker: a cell list longer than N (EDMD_ERR_BUDGET)
 constexpr int WPB = 8;                // warps per block of the processing kernel
 constexpr int NSTRIPE = 32;           // copies of each system's counters
 // counters of the round engine, per system and stripe (u64 slots)
@@ -416,6 +417,7 @@ __device__ void predict_warp(const SysDev& S, int a0, const Disk& A0, int X0, in
   const int a = grp ? a1 : a0;
   const int X = grp ? X1 : X0, Y = grp ? Y1 : Y0;
   int cnt = 0;
+  bool lcorrupt = false;
   int32_t* reg = W->reg + lane * MAXC;
   if (a >= 0 && q < 9) {
     int p = S.head[pbc_cy(B, Y + q / 3 - 1) * B.Nxc + pbc_cx(B, X + q % 3 - 1)];
@@ -427,6 +429,7 @@ __device__ void predict_warp(const SysDev& S, int a0, const Disk& A0, int X0, in
       }
       p = S.d[p].nxt;
     }
+    if (p != NIL) { lcorrupt = true; }   // a list longer than N is corrupt
   }
   const bool spill = __any_sync(FULLM, cnt > MAXC);
   const uint64_t knever = time_key(NEVER);
@@ -487,6 +490,7 @@ __device__ void predict_warp(const SysDev& S, int a0, const Disk& A0, int X0, in
         }
         p = P.nxt;
       }
+      if (p != NIL) lcorrupt = true;
     }
     for (int o = 16; o > 0; o >>= 1) mine += __shfl_xor_sync(FULLM, mine, o);
     tot = mine;
@@ -522,6 +526,7 @@ __device__ void predict_warp(const SysDev& S, int a0, const Disk& A0, int X0, in
     *ovl = true;
     *ob = __shfl_sync(FULLM, lb, __ffs(m) - 1);
   }
+  if (__any_sync(FULLM, lcorrupt)) { *ovl = true; *ob = OB_CORRUPT; }
 }
 
 __device__ __forceinline__ void set_event(const SysDev& S, int slot, double t, int j, uint32_t ca,
@@ -832,6 +837,7 @@ __device__ Pred predict_thread(const SysDev& S, const RoundArgs& A, int s, int a
       if (kd < kb) { r.dt = d; kb = kd; r.partner = p; r.ca = P.coll; r.pcell = cell; found = true; }
       p = P.nxt;
     }
+    if (p != NIL) { *ovl = true; *ob = OB_CORRUPT; }   // the lists hold more than N entries: corrupt
   }
   if (!found) r.ca = S.d[0].coll;
   return r;
@@ -1045,7 +1051,7 @@ __global__ void __launch_bounds__(128) k_process_thread(const SysDev* __restrict
         SysState* R = sys[s].st;
         R->err_a = r.a;
         R->err_b = r.ob;
-        R->status = EDMD_ERR_OVERLAP;
+        R->status = r.ob == OB_CORRUPT ? EDMD_ERR_BUDGET : EDMD_ERR_OVERLAP;
       }
     }
     const unsigned m = __match_any_sync(FULLM, s);
@@ -1107,7 +1113,7 @@ __global__ void __launch_bounds__(32 * WPB, 2) k_process(const SysDev* __restric
         SysState* R = sys[s].st;
         R->err_a = r.a;
         R->err_b = r.ob;
-        R->status = EDMD_ERR_OVERLAP;
+        R->status = r.ob == OB_CORRUPT ? EDMD_ERR_BUDGET : EDMD_ERR_OVERLAP;
       }
     }
     __syncwarp();
@@ -1279,7 +1285,7 @@ __global__ void __launch_bounds__(32 * BWPB, 4) k_block_rounds(const SysDev* __r
           if (r.ovl) {
             S.st->err_a = r.a;
             S.st->err_b = r.ob;
-            S.st->status = EDMD_ERR_OVERLAP;
+            S.st->status = r.ob == OB_CORRUPT ? EDMD_ERR_BUDGET : EDMD_ERR_OVERLAP;
           }
         }
         __syncwarp();
@@ -1668,18 +1674,12 @@ extern "C" int edmd_advance_rounds(edmd_ctx* ctx, int64_t max_coll, double t_sto
   }
   CK(cudaEventRecord(ctx->e1, ctx->stream));
   CK(cudaEventSynchronize(ctx->e1));
-  if (elapsed_ms) CK(cudaEventElapsedTime(elapsed_ms, ctx->e0, ctx->e1));
+  CK(cudaEventElapsedTime(&ctx->last_ms, ctx->e0, ctx->e1));
+  if (elapsed_ms) *elapsed_ms = ctx->last_ms;
   if (rounds_out) *rounds_out = rounds;
   if (violations_out) *violations_out = viol_total;
-  std::vector<int32_t> status(ctx->nsys);
-  CK(sync_copy2d(ctx, status.data(), 4, &ctx->st[0].status, sizeof(SysState), 4, ctx->nsys,
-                  cudaMemcpyDeviceToHost));
-  for (int s = 0; s < ctx->nsys; s++)
-    if (status[s] != EDMD_OK) {
-      char b[128];
-      snprintf(b, sizeof b, "system %d stopped with status %d", s, status[s]);
-      return set_err(ctx, status[s], b);
-    }
+  const int rs = report_status(ctx, "advance_rounds");
+  if (rs != EDMD_OK) return rs;
   if (active) return set_err(ctx, EDMD_ERR_BUDGET, "round budget exhausted");
   return EDMD_OK;
 }

@@ -373,6 +373,7 @@ extern "C" int edmd_tangent_run(edmd_ctx* ctx, int32_t s, int32_t K, int64_t n_c
   CK(dalloc(&logdiag, K));
   CK(dalloc(&fail, 1));
   struct Free { void* p[7]; ~Free() { for (void* q : p) if (q) cudaFree(q); } } guard{{T, tl, G, Gp, Rinv, logdiag, fail}};
+  CK(call_begin(ctx));
   double t0;
   if ((rc = current_time(ctx, s, &t0))) return rc;
   // initial vectors: the caller's ([K][N][4]) or seeded random orthonormal ones
@@ -421,6 +422,7 @@ extern "C" int edmd_tangent_run(edmd_ctx* ctx, int32_t s, int32_t K, int64_t n_c
           tangent_io[(size_t)k * 4 * N + 4 * i + c] = v;
         }
   }
+  CK(call_end(ctx));
   return EDMD_OK;
 }
 
@@ -441,6 +443,7 @@ extern "C" int edmd_msd_gradient(edmd_ctx* ctx, int32_t s, int64_t n_coll, int64
   CK(dalloc(&px, N));
   CK(dalloc(&py, N));
   struct Free { void* p[4]; ~Free() { for (void* q : p) if (q) cudaFree(q); } } guard{{A, ta, px, py}};
+  CK(call_begin(ctx));
   double t0, T;
   if ((rc = current_time(ctx, s, &t0))) return rc;
   std::vector<double> x0(N), y0(N), x1(N), y1(N);
@@ -509,5 +512,6 @@ extern "C" int edmd_msd_gradient(edmd_ctx* ctx, int32_t s, int64_t n_coll, int64
     if (g_vy) g_vy[i] = hA[4 * i + 3];
   }
   if (msd_out) *msd_out = msd;
+  CK(call_end(ctx));
   return EDMD_OK;
 }

@@ -59,7 +59,7 @@ EXPORTS = [
     "edmd_get_states", "edmd_get_counters", "edmd_get_all_counters", "edmd_get_virial",
     "edmd_get_thermo", "edmd_get_trace", "edmd_set_engine", "edmd_set_lane_threads",
     "edmd_set_warp_group",
-    "edmd_get_engine", "edmd_set_device", "edmd_host_alloc", "edmd_host_free", "edmd_run_noalloc",
+    "edmd_get_engine", "edmd_get_last_ms", "edmd_set_device", "edmd_host_alloc", "edmd_host_free", "edmd_run_noalloc",
     "edmd_set_log_capacity", "edmd_clear_log", "edmd_get_log", "edmd_checkpoint_save",
     "edmd_checkpoint_restore", "edmd_tangent_run", "edmd_msd_gradient", "edmd_destroy",
     "edmd_last_error", "edmd_device_info",
@@ -110,6 +110,7 @@ def load(path=LIB_PATH):
     L.edmd_set_lane_threads.argtypes = [C.c_int32]
     L.edmd_set_warp_group.argtypes = [C.c_int32]
     L.edmd_get_engine.argtypes = [C.c_void_p]
+    L.edmd_get_last_ms.argtypes = [C.c_void_p, C.POINTER(C.c_float)]
     L.edmd_sync.argtypes = [C.c_void_p]
     L.edmd_get_state.argtypes = [C.c_void_p, C.c_int32] + [C.c_void_p] * 8
     L.edmd_get_counters.argtypes = [C.c_void_p, C.c_int32, C.POINTER(Counters)]
@@ -233,6 +234,12 @@ class Engine:
 
     def last_error(self):
         return self._L.edmd_last_error(self.h).decode()
+
+    def last_ms(self):
+        """Device time of the last advance / round / tangent / adjoint call (edmd_get_last_ms)."""
+        ms = C.c_float()
+        self._ck(self._L.edmd_get_last_ms(self.h, C.byref(ms)))
+        return ms.value
 
     def _ck(self, rc):
         if rc != OK:

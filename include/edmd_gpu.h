@@ -221,6 +221,12 @@ int edmd_set_lane_threads(int32_t threads_per_block);
  * 4096-system batch 32 lanes run 6.2e7 coll/s and 16 lanes 5.9e7. */
 int edmd_set_warp_group(int32_t lanes);
 int edmd_get_engine(const edmd_ctx* ctx);
+/* Device time, in ms, of the last edmd_advance, edmd_advance_rounds,
+ * edmd_tangent_run or edmd_msd_gradient call on ctx: CUDA events recorded on
+ * the context's stream at the call's start and end (for the host-driven
+ * differentiation calls this includes the stream's idle gaps between their
+ * kernels).  No reference counterpart (the reference reports no timings). */
+int edmd_get_last_ms(const edmd_ctx* ctx, float* ms);
 
 /* Select the CUDA device used by contexts created afterwards in this thread
  * (one process per GPU). */
@@ -273,14 +279,23 @@ int edmd_host_free(void* p);
  * exists for callers that cannot call cudaMalloc -- code in a loop where
  * device allocation is forbidden, or a host framework that owns every device
  * buffer.  x, y, vx, vy, rad, m are the CALLER's DEVICE arrays of desc->N
- * entries; the call restarts the system from them (t = 0, normal phase, the
- * -l semantics of edmd_load_state), runs until max_coll accepted collisions,
- * t_stop or desc->tmax, free-flies every disk to the final time and writes x,
- * y, vx, vy back.  ncol_out / t_out (host, may be NULL) receive the collisions
- * run and the final time.  `stream` is a cudaStream_t (NULL: default stream).
+ * entries; the call starts the system from them directly, exactly as
+ * edmd_create with vr = NULL does: t = 0, normal phase, first screenshot and
+ * thermo events at desc->first_screen and desc->first_thermo, positions used
+ * as given (no periodic wrap; a position outside [0, Lx) x [0, Ly) returns
+ * EDMD_ERR_ARG naming the disk).  It runs until max_coll accepted
+ * collisions, t_stop or desc->tmax, free-flies every disk to the final time
+ * and writes x, y, vx, vy back.  ncol_out / t_out (host, may be NULL) receive
+ * the collisions run and the final time.  `stream` is a cudaStream_t (NULL:
+ * default stream).  The call is synchronous: it waits for its stream and
+ * reads the result back before it returns.
  *
  * Limits: N <= 8192, Nxcells*Nycells <= 65536, direct starts only
- * (desc->t_growstop < 0); larger systems return EDMD_ERR_CAPACITY.
+ * (desc->t_growstop < 0); larger systems return EDMD_ERR_CAPACITY.  Each
+ * call may process at most 256 events per requested collision plus 256 per
+ * disk plus 2^20; beyond that it stops with EDMD_ERR_BUDGET and still writes
+ * the state at the stop back (a very dilute system, with many cell crossings
+ * per collision, can continue with another call).
  * It allocates nothing: all engine state lives in one file-scope 4 MiB
  * __device__ array that each GPU using this library keeps until exit.  The
  * first call on a device looks up that array's address (once per device, with

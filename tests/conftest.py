@@ -80,3 +80,33 @@ def has_gpu():
         return torch.cuda.is_available()
     except Exception:
         return False
+
+
+def line_overlap_state(edmd):
+    """59 disks of radius 1 in a 32 x 32 box: a 4-spaced grid with its third
+    row taken out, and on that row disk 0 at x = 5, disk 1 at x = 6.5 (0.5
+    inside disk 0, moving away from it at speed 1) and disk 2 at x = 8.7
+    (moving towards disk 1 at speed 1).  Disks 1 and 2 meet at t = 0.1 and
+    swap velocities; disk 1 then approaches disk 0 while still overlapping
+    it.  Every other disk drifts at speed ~1e-3."""
+    rng = np.random.default_rng(3)
+    pts = [(5.0, 10.0), (6.5, 10.0), (8.7, 10.0)]
+    for b in range(8):
+        if b == 2:
+            continue
+        for a in range(8):
+            pts.append((2.0 + 4 * a, 2.0 + 4 * b))
+    N = len(pts)
+    x = np.array([p[0] for p in pts])
+    y = np.array([p[1] for p in pts])
+    vx = rng.uniform(-1e-3, 1e-3, N)
+    vy = rng.uniform(-1e-3, 1e-3, N)
+    vx[1], vy[1] = 1.0, 0.0
+    vx[2], vy[2] = -1.0, 0.0
+    desc = edmd.default_desc(N, 32.0, 32.0, 0.0, 1e30)
+    return dict(N=N, x=x, y=y, vx=vx, vy=vy, rad=np.ones(N), m=np.ones(N), vr=None, desc=desc)
+
+
+def names_pair(msg, a, b):
+    """True when an engine error message names the overlapping pair (a, b)."""
+    return (f"disks {a} and {b}" in msg) or (f"disks {b} and {a}" in msg)

@@ -2,7 +2,7 @@
 
 Run here (where the reference checkout exists):
 
-    python tests/golden/make_golden.py [--ref /root/reference]
+    python tests/golden/make_golden.py --ref <reference checkout>   (or set EDMD_REFERENCE_DIR)
 
 It builds ``oracle/_ref/ref_trace`` (``make -C oracle ref``), which compiles
 the reference's unmodified src/EDMD.c and satellites with IEEE flags and
@@ -83,8 +83,11 @@ def run_case(exe, args, maxcoll, trace, extra_env=None):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("EDMD_REFERENCE_DIR"),
+                    help="reference checkout (default: $EDMD_REFERENCE_DIR)")
     a = ap.parse_args()
+    if not a.ref:
+        ap.error("give --ref or set EDMD_REFERENCE_DIR to the reference checkout")
     subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "ref", f"REF={a.ref}"], check=True)
     exe = os.path.join(ROOT, "oracle", "_ref", "ref_trace")
     tmp = os.path.join(HERE, "_tmp_trace.txt")

@@ -57,3 +57,42 @@ def test_noalloc_rejects_oversized_systems(edmd):
     rc = L.edmd_run_noalloc(C.byref(desc), *([dummy] * 6), 10, float("inf"), None, None, None)
     assert rc == edmd.ERR_CAPACITY
     assert b"8192" in L.edmd_last_error(None)
+
+
+def _noalloc(L, desc, bufs, max_coll):
+    ncol, tout = C.c_int64(), C.c_double()
+    rc = L.edmd_run_noalloc(C.byref(desc), *[C.c_void_p(bufs[k].data_ptr()) for k in KEYS],
+                            max_coll, float("inf"), C.byref(ncol), C.byref(tout), None)
+    return rc, ncol.value, tout.value
+
+
+def test_noalloc_rejects_positions_outside_the_box_then_runs_again(edmd):
+    import torch
+    L = edmd.load()
+    s = edmd.hex_start(1024, 0.60, 5)
+    desc = edmd.default_desc(s["N"], s["Lx"], s["Ly"])
+    dev = torch.device("cuda:0")
+    bad = {k: s[k].copy() for k in KEYS}
+    bad["x"][7] = s["Lx"] + 0.5
+    bufs = {k: torch.tensor(bad[k], dtype=torch.float64, device=dev) for k in KEYS}
+    rc, ncol, _ = _noalloc(L, desc, bufs, 500)
+    assert rc == edmd.ERR_ARG
+    assert b"disk 7 outside the box" in L.edmd_last_error(None)
+    assert ncol == 0
+    # the shared scratch keeps nothing of the failed call
+    bufs = {k: torch.tensor(s[k], dtype=torch.float64, device=dev) for k in KEYS}
+    rc, ncol, _ = _noalloc(L, desc, bufs, 500)
+    assert rc == edmd.OK and ncol == 500
+
+
+def test_noalloc_reports_an_overlap_met_during_the_run(edmd):
+    import torch
+    from conftest import line_overlap_state, names_pair
+    L = edmd.load()
+    s = line_overlap_state(edmd)
+    bufs = {k: torch.tensor(s[k], dtype=torch.float64, device="cuda:0") for k in KEYS}
+    rc, ncol, tout = _noalloc(L, s["desc"], bufs, 100)
+    msg = L.edmd_last_error(None).decode()
+    assert rc == edmd.ERR_OVERLAP, msg
+    assert names_pair(msg, 0, 1), msg
+    assert ncol == 1 and abs(tout - 0.1) < 1e-12
