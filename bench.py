@@ -28,15 +28,25 @@ end-to-end throughput through the C ABI with host buffers (``e2e``: restart
 from pinned host state, run, read the state back), the roofline of the run
 kernels, the CPU baseline (the oracle restatement on the host cores) and the SM
 clocks sampled during the timed region.  The default run also measures the
-single_large workload and reports it under ``other_workloads``.
-``--impl reference`` times the reference algorithm on the host cores (the
-oracle restatement; the reference's own C cannot be compiled where the
-benchmark runs).
+single_large workload and the differentiation forms, each with its own CPU
+baseline, and reports them under ``other_workloads``.
+
+CPU baselines run the oracle restatement (bit-identical to the reference's C),
+one system per process at a time on every usable host core
+(``os.sched_getaffinity``).  The batched sample is stratified: one system per
+cell of an 8 x 8 grid over (N, phi) of the 4096-system workload, weighted by
+the cell's share; the aggregate is cores / (weighted mean time per collision),
+the rate at which the cores would get through the whole batch.
+
+``--impl reference`` times the same CPU path as the reference arm.  With
+``--gpus N`` (N > 1) outside torchrun, the script re-launches itself under
+``torch.distributed.run`` with N ranks, one GPU each.
 """
 import argparse
 import json
 import multiprocessing as mp
 import os
+import socket
 import statistics
 import subprocess
 import sys
@@ -60,14 +70,37 @@ DEFAULT_COLL = {"batched": 100000, "single_large": 20000000, "single_4m": 100000
 DEFAULT_ENGINE = {"batched": "warp", "single_large": "round", "single_4m": "round", "plain_small": "warp"}
 LARGE_N, LARGE_PHI, LARGE_EQUIL = 1000000, 0.72, 100000
 SINGLE = {"single_large": (LARGE_N, LARGE_PHI), "single_4m": (4000000, 0.78)}
+DIFF_N, DIFF_PHI, DIFF_SEED, DIFF_COLL = 1024, 0.60, 11, 10000
+
+# DRAM traffic and FP64-pipe activity of the dominant kernel, from one ncu
+# capture of the configuration they belong to; reported only for that
+# configuration (workload, engine, lanes per system)
+PROFILED = {
+    ("batched", "warp", 32): dict(
+        kernel="k_run<32>", dram_bytes_per_collision=5744.0, fp64_pipe_active=0.558,
+        capture="ncu --set full --clock-control none -k regex:k_run -s 4 -c 1 python bench.py --workload batched "
+                "--nsys 4096 --coll 2000 --steps 1 --warmup 3 --no-cpu-baseline --no-secondary "
+                "(dram__bytes_read.sum + dram__bytes_write.sum = 47.05 GB for 8.192e6 collisions)"),
+}
+
+
+def usable_cores():
+    try:
+        return max(1, len(os.sched_getaffinity(0)))
+    except (AttributeError, OSError):
+        return os.cpu_count() or 1
 
 
 def _load_edmd():
+    """The engine's Python binding; EDMD_BENCH_ENGINE_MODULE names a stand-in
+    module with the same interface (used by the CPU test of the multi-rank
+    launch, which has no GPU)."""
     import importlib.util
     key = "edmd_gb300_edmd"
     if key in sys.modules:
         return sys.modules[key]
-    spec = importlib.util.spec_from_file_location(key, os.path.join(ROOT, "graphical-edmd_gb300", "edmd.py"))
+    path = os.environ.get("EDMD_BENCH_ENGINE_MODULE") or os.path.join(ROOT, "graphical-edmd_gb300", "edmd.py")
+    spec = importlib.util.spec_from_file_location(key, path)
     mod = importlib.util.module_from_spec(spec)
     sys.modules[key] = mod
     spec.loader.exec_module(mod)
@@ -82,37 +115,62 @@ def batched_params(nsys, seed, rank):
     return [(int(n), float(p), int(s)) for n, p, s in zip(Ns, phis, seeds)]
 
 
+def stratified_sample(params, nb_n=8, nb_phi=8):
+    """One system per cell of an nb_n x nb_phi grid over (N, phi) -- the first
+    system of the workload in that cell -- with the cell's share of the
+    workload as its weight."""
+    cells = {}
+    for N, phi, sd in params:
+        bn = min(nb_n - 1, int((N - 256) * nb_n / (4097 - 256)))
+        bp = min(nb_phi - 1, max(0, int((phi - 0.30) * nb_phi / 0.45)))
+        cells.setdefault((bn, bp), []).append((N, phi, sd))
+    return [(m[0], len(m) / len(params)) for _, m in sorted(cells.items())]
+
+
 # ------------------------------------------------------------------ CPU side
 
-def _cpu_worker(conn, params, coll):
-    """One reference-semantics system per process (the oracle), single-threaded."""
+def _cpu_worker(conn, systems, coll):
+    """Reference-semantics systems (the oracle), single-threaded, one process."""
     from oracle import oracle as orc
-    N, phi, seed, kind = params
-    if kind == "hex":
-        o = orc.Oracle(N=N, phi=phi, seed=seed, start=orc.HEX, tmax=1e30)
-        if N >= LARGE_N:
-            o.run(LARGE_EQUIL, cap=1)                          # equilibration, untimed
-    else:
-        o = orc.Oracle(N=N, phi=phi, seed=seed, start=orc.GROW, xs=XS, q=Q, tmax=1e30)
-        vr = orc.load().orc_vr(o.h)
-        o.run(10 ** 12, t_stop=1 / vr + 1e-9, cap=1)         # growth phase, untimed
+    objs = []
+    for (N, phi, seed, kind, w) in systems:
+        if kind == "hex":
+            o = orc.Oracle(N=N, phi=phi, seed=seed, start=orc.HEX, tmax=1e30)
+            if N >= LARGE_N:
+                o.run(LARGE_EQUIL, cap=1)                      # equilibration, untimed
+        else:
+            o = orc.Oracle(N=N, phi=phi, seed=seed, start=orc.GROW, xs=XS, q=Q, tmax=1e30)
+            vr = orc.load().orc_vr(o.h)
+            o.run(10 ** 12, t_stop=1 / vr + 1e-9, cap=1)     # growth phase, untimed
+        objs.append((o, w))
     conn.send("ready")
     while True:
         msg = conn.recv()
         if msg == "stop":
             break
-        t0 = time.perf_counter()
-        _, n = o.run(coll, cap=1)
-        conn.send((n, time.perf_counter() - t0))
+        res = []
+        for o, w in objs:
+            t0 = time.perf_counter()
+            _, n = o.run(coll, cap=1)
+            res.append((n, time.perf_counter() - t0, w))
+        conn.send(res)
 
 
 class CpuPool:
-    def __init__(self, params, coll):
+    """Processes over the usable host cores, each holding a share of the
+    sample's systems (built untimed).  step() runs every system `coll`
+    collisions and returns (collisions, wall seconds, aggregate rate), the
+    aggregate being cores / (weighted mean seconds per collision)."""
+
+    def __init__(self, systems, coll, ncores):
         ctx = mp.get_context("spawn")
+        self.nproc = max(1, min(ncores, len(systems)))
+        self.coll = coll
+        self.nsys = len(systems)
         self.p = []
-        for prm in params:
+        for k in range(self.nproc):
             a, b = ctx.Pipe()
-            pr = ctx.Process(target=_cpu_worker, args=(b, prm, coll), daemon=True)
+            pr = ctx.Process(target=_cpu_worker, args=(b, systems[k::self.nproc], coll), daemon=True)
             pr.start()
             self.p.append((pr, a))
         for _, a in self.p:
@@ -122,26 +180,136 @@ class CpuPool:
         t0 = time.perf_counter()
         for _, a in self.p:
             a.send("go")
-        res = [a.recv() for _, a in self.p]
+        res = [r for _, a in self.p for r in a.recv()]
         wall = time.perf_counter() - t0
-        return sum(r[0] for r in res), wall, sum(r[0] / r[1] for r in res)
+        wsum = sum(w for _, _, w in res)
+        tau = sum(w * dt / max(n, 1) for n, dt, w in res) / wsum
+        return sum(n for n, _, _ in res), wall, self.nproc / tau
 
     def close(self):
         for pr, a in self.p:
-            a.send("stop")
+            try:
+                a.send("stop")
+            except (BrokenPipeError, OSError):
+                pass
             pr.join(timeout=10)
 
 
-def cpu_sample_params(workload, ncores, seed):
+def cpu_sample(workload, ncores, seed):
+    """Systems (N, phi, seed, start, weight) of the CPU sample of a workload."""
     if workload == "plain_small":
-        return [(2000, 0.70, seed + k, "hex") for k in range(ncores)]
+        return [(2000, 0.70, seed + k, "hex", 1.0) for k in range(ncores)]
     if workload in SINGLE:
-        return [(SINGLE[workload][0], SINGLE[workload][1], seed, "hex")]   # one system: one thread
-    return [(n, p, s, "grow") for n, p, s in batched_params(ncores, seed, 0)]
+        return [(SINGLE[workload][0], SINGLE[workload][1], seed, "hex", 1.0)]   # one system: one thread
+    return [(n, p, s, "grow", w) for (n, p, s), w in stratified_sample(batched_params(4096, seed, 0))]
 
 
 def cpu_sample_coll(workload, a):
-    return a.cpu_coll if workload not in SINGLE else 2000000
+    if workload in SINGLE:
+        return 2000000
+    return a.cpu_coll if workload == "batched" else 1000000
+
+
+def describe_sample(pool, workload, kind="port"):
+    what = {"batched": f"{pool.nsys} systems, one per cell of an 8x8 (N, phi) grid over the 4096-system "
+                       f"workload, weighted by the cell's share",
+            "plain_small": f"{pool.nsys} Hex systems (N=1980, phi=0.70, seeds seed..seed+{pool.nsys - 1})",
+            "single_large": "the 10^6-disk Hex system (phi 0.72) after its 10^5 equilibration collisions",
+            "single_4m": "the 4*10^6-disk Hex system (phi 0.78) after its 10^5 equilibration collisions"}[workload]
+    return (f"{what}; {pool.coll} collisions each per step on {pool.nproc} process(es), one core each; "
+            f"oracle restatement (-O2 IEEE, bit-identical to the reference's C); set-up untimed; "
+            f"aggregate = cores / weighted mean time per collision")
+
+
+def cpu_line(pool, workload, n, wall, rate):
+    return {"value": rate, "unit": UNIT, "cores": pool.nproc, "kind": "port",
+            "sample": describe_sample(pool, workload), "collisions": n, "wall_s": wall}
+
+
+# ---- CPU comparator of the adjoint: central finite differences of the final MSD
+
+def _diff_base_state():
+    """The differentiation configuration: Hex N=1024, phi=0.60, 2000 collisions
+    from the lattice (the same state the GPU arm differentiates)."""
+    from oracle import oracle as orc
+    o = orc.Oracle(N=DIFF_N, phi=DIFF_PHI, seed=DIFF_SEED, start=orc.HEX, tmax=1e30)
+    o.run(2000, cap=1)
+    o.sync()
+    st = o.state()
+    Lx, Ly, _, _ = o.box()
+    init = {k: st[k].copy() for k in ("x", "y", "vx", "vy", "rad", "m", "type")}
+    return init, Lx, Ly
+
+
+def _msd_after(orc, init, Lx, Ly, ncoll, t_obs=None):
+    o = orc.Oracle(arrays=init, Lx=Lx, Ly=Ly, tmax=1e30)
+    if t_obs is None:
+        o.run(ncoll, cap=1)
+        t_obs = o.t
+    else:
+        o.run(10 ** 12, t_stop=t_obs, cap=1)
+    st = o.state()
+    x = st["x"] + st["vx"] * (t_obs - st["tl"])
+    y = st["y"] + st["vy"] * (t_obs - st["tl"])
+    dx = x - init["x"]; dx -= Lx * np.rint(dx / Lx)
+    dy = y - init["y"]; dy -= Ly * np.rint(dy / Ly)
+    dx -= dx.mean(); dy -= dy.mean()
+    return float(np.mean(dx * dx + dy * dy)), t_obs
+
+
+def _fd_worker(conn, comps, ncoll, eps):
+    from oracle import oracle as orc
+    init, Lx, Ly = _diff_base_state()
+    _, t_obs = _msd_after(orc, init, Lx, Ly, ncoll)
+    conn.send("ready")
+    if conn.recv() == "stop":
+        return
+    t0 = time.perf_counter()
+    g = []
+    for c in comps:
+        key, i = ("vx", c) if c < DIFF_N else ("vy", c - DIFF_N)
+        m = []
+        for sign in (1, -1):
+            a = {k: v.copy() for k, v in init.items()}
+            a[key][i] += sign * eps
+            m.append(_msd_after(orc, a, Lx, Ly, ncoll, t_obs)[0])
+        g.append((m[0] - m[1]) / (2 * eps))
+    conn.send((len(comps), time.perf_counter() - t0))
+
+
+def cpu_fd_gradient(ncores, ncoll, ncomp, eps=1e-7):
+    """Wall time of the FP64 central-difference gradient of the final MSD with
+    respect to the initial velocities (2N components, 2 runs each) on the
+    host cores; `ncomp` components are timed and the full gradient's time
+    scaled from them when ncomp < 2N."""
+    ctx = mp.get_context("spawn")
+    comps = list(range(min(ncomp, 2 * DIFF_N)))
+    nproc = max(1, min(ncores, len(comps)))
+    procs = []
+    for k in range(nproc):
+        a, b = ctx.Pipe()
+        pr = ctx.Process(target=_fd_worker, args=(b, comps[k::nproc], ncoll, eps), daemon=True)
+        pr.start()
+        procs.append((pr, a))
+    return procs, comps
+
+
+def cpu_fd_finish(procs, comps):
+    for _, a in procs:
+        assert a.recv() == "ready"
+    t0 = time.perf_counter()
+    for _, a in procs:
+        a.send("go")
+    res = [a.recv() for _, a in procs]
+    wall = time.perf_counter() - t0
+    for pr, _ in procs:
+        pr.join(timeout=10)
+    full = wall * (2 * DIFF_N) / len(comps)
+    return {"gradient_wall_s": full, "timed_components": len(comps), "timed_wall_s": wall,
+            "cores": len(procs), "kind": "port",
+            "sample": (f"central differences (eps 1e-7) of the final MSD after {DIFF_COLL} collisions, "
+                       f"{len(comps)} of the {2 * DIFF_N} velocity components timed, two oracle runs each"
+                       + ("" if len(comps) == 2 * DIFF_N else "; full-gradient time scaled from them"))}
 
 
 # ------------------------------------------------------------------ clocks
@@ -221,6 +389,22 @@ def sum_over_ranks(dist, v):
     return float(t.item())
 
 
+def _free_port():
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    p = s.getsockname()[1]
+    s.close()
+    return p
+
+
+def relaunch_ranks(n):
+    """Run this script under torch.distributed.run with n ranks (one GPU each)."""
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={n}",
+           "--master-addr", "127.0.0.1", "--master-port", str(_free_port()),
+           os.path.abspath(__file__)] + sys.argv[1:]
+    return subprocess.run(cmd).returncode
+
+
 # ------------------------------------------------------------------ reference arm
 
 def describe_workload(workload, systems, TN):
@@ -239,28 +423,26 @@ def describe_workload(workload, systems, TN):
 def run_reference(a, rank, world, dist):
     if rank != 0:
         return 0
-    ncores = os.cpu_count() or 1
+    ncores = usable_cores()
     coll = a.ref_coll if a.workload not in SINGLE else 2000000
-    params = cpu_sample_params(a.workload, ncores, a.seed)
-    pool = CpuPool(params, coll)
+    pool = CpuPool(cpu_sample(a.workload, ncores, a.seed), coll, ncores)
     for _ in range(a.warmup):
         pool.step()
-    tot, wall = 0, 0.0
+    rates, walls = [], []
     for _ in range(a.steps):
-        n, w, _ = pool.step()
-        tot += n; wall += w
+        _, w, r = pool.step()
+        rates.append(r); walls.append(w)
     pool.close()
-    v = tot / wall
-    sample = (f"{len(params)} systems of the workload, one per process, {coll} collisions each per step, "
-              f"oracle restatement (-O2 IEEE), set-up untimed")
+    v = statistics.mean(rates)
+    sample = describe_sample(pool, a.workload)
     line = {"impl": "reference", "metric": METRICS[a.workload],
             "value": v, "unit": UNIT, "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup,
-            "ms_per_step": 1000 * wall / a.steps, "higher_is_better": True, "scaling": "weak",
+            "ms_per_step": 1000 * statistics.mean(walls), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": describe_workload(a.workload, a.nsys or (4096 if a.workload == "batched" else 1),
                                                      SINGLE[a.workload][0] if a.workload in SINGLE else None),
                        "sample": sample},
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": len(params), "kind": "port", "sample": sample},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": pool.nproc, "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
@@ -311,7 +493,6 @@ def measure(edmd, a, workload, engine, coll, steps, warmup, rank, world, dist, d
     edmd.set_warp_group(a.warp_group)
     eng = edmd.Engine(systems, engine=edmd.ENGINE_LANE if engine == "lane" else edmd.ENGINE_WARP)
     TN = sum(s["desc"].N for s in systems)
-    TC = sum(int(s["desc"].Lx / 2) * int(s["desc"].Ly / 2) for s in systems)
     # untimed set-up: growth phase, or equilibration of the large system
     if workload == "batched":
         eng.advance(flags=edmd.F_STOP_AT_GROW)
@@ -353,7 +534,6 @@ def measure(edmd, a, workload, engine, coll, steps, warmup, rank, world, dist, d
     t0 = time.perf_counter()
     e2e_coll = 0
     for _ in range(e2e_steps):
-        ca = eng.all_counters()["ncol"].sum()
         eng.load_state(*(pin[k].a for k in ("x", "y", "vx", "vy", "rad", "m")))
         cb = eng.all_counters()["ncol"].sum()
         st.step()
@@ -376,35 +556,35 @@ def measure(edmd, a, workload, engine, coll, steps, warmup, rank, world, dist, d
     achieved = Bcoll * ncoll / t_dev / 1e9
     peaks = json.load(open(PEAKS)) if os.path.exists(PEAKS) else {}
     peak = peaks.get("hbm_gbs", 6800.0)
-    # DRAM bytes per accepted collision of k_run from one ncu capture of a
-    # 2000-collision step of the batched workload (dram__bytes_read.sum +
-    # dram__bytes_write.sum = 41.51 + 5.54 GB for 8.192e6 collisions), scaled
-    # to a launch; the same capture gives the FP64 pipe's busy fraction, the
-    # resource that bounds this kernel
-    traffic = 5744.0 * ncoll / steps if engine == "warp" else None
+    prof = PROFILED.get((workload, engine, a.warp_group)) if a.nsys is None else None
     kernel = ("k_run (one persistent launch per step)" if engine == "warp" else
               "k_lane_run" if engine == "lane" else
               "round engine graph: k_select + k_process + k_recompute + k_barrier per round")
+    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": prof["dram_bytes_per_collision"] * ncoll / steps if prof else None,
+            "kernel": kernel, "bytes_per_collision": Bcoll, "p_pair": p_pair, "p_pred": p_pred,
+            "peak_source": "measured hbm_gbs (of measured)" if "hbm_gbs" in peaks else "fallback 6.8 TB/s"}
+    if prof:
+        roof.update(traffic_source=("DRAM bytes per accepted collision of %s from one ncu capture of this "
+                                    "configuration, scaled to the launch's collisions: %s"
+                                    % (prof["kernel"], prof["capture"])),
+                    fp64_pipe_active=prof["fp64_pipe_active"],
+                    fp64_pipe_source="sm__pipe_fp64_cycles_active of the same capture")
+    else:
+        roof["traffic_source"] = "no ncu capture of this configuration"
     return dict(value=value, ms_per_step=1000 * t_max / steps, wall=wall, clocks=clocks, launches=launches,
-                systems=len(systems), TN=TN, e2e=e2e, h2d=h2d, d2h=d2h,
-                roofline={"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                          "frac": achieved / peak, "traffic": traffic, "kernel": kernel,
-                          "traffic_source": ("ncu capture of a 2000-collision step, 5.74 KB per collision "
-                                             "(profiles/warp_k_run_batched.md), scaled to the launch"
-                                             if traffic else None),
-                          "fp64_pipe_active": 0.558 if engine == "warp" else None,
-                          "bytes_per_collision": Bcoll, "p_pair": p_pair, "p_pred": p_pred,
-                          "peak_source": "measured hbm_gbs" if "hbm_gbs" in peaks else "fallback"})
+                systems=len(systems), TN=TN, e2e=e2e, h2d=h2d, d2h=d2h, roofline=roof)
 
 
-def measure_differentiation(edmd, ncoll=10000):
-    """The tangent and adjoint forms on one 1024-disk Hex system at phi = 0.60:
-    32 tangent vectors re-orthonormalised every 100 collisions (Lyapunov
-    spectrum), and the adjoint of the final mean-square displacement with
-    checkpoints every 500 collisions.  Accepted collisions per second of each
-    call, host-timed around the synchronous C-ABI call."""
+def measure_differentiation(edmd, ncoll=DIFF_COLL):
+    """The tangent and adjoint forms on one 1024-disk Hex system at phi = 0.60
+    (2000 collisions from the lattice): 32 tangent vectors re-orthonormalised
+    every 100 collisions (Lyapunov spectrum), and the adjoint of the final
+    mean-square displacement with checkpoints every 500 collisions.  Each call
+    is timed twice: device time (CUDA events on the context's stream around
+    the whole call, edmd_get_last_ms) and host wall time."""
     try:
-        s = edmd.hex_start(1024, 0.60, 11)
+        s = edmd.hex_start(DIFF_N, DIFF_PHI, DIFF_SEED)
         s["desc"] = edmd.default_desc(s["N"], s["Lx"], s["Ly"])
         eng = edmd.Engine([s])
         eng.advance(max_coll=2000)                       # untimed: leave the lattice
@@ -412,31 +592,44 @@ def measure_differentiation(edmd, ncoll=10000):
         t0 = time.perf_counter()
         _, lam = eng.tangent(32, ncoll, qr_every=100, seed=17)
         t_tan = time.perf_counter() - t0
+        ms_tan = eng.last_ms()
         eng.msd_gradient(1000, ckpt_every=500)           # warm-up
         t0 = time.perf_counter()
         eng.msd_gradient(ncoll, ckpt_every=500)
         t_adj = time.perf_counter() - t0
+        ms_adj = eng.last_ms()
         eng.close()
         return {"config": "single Hex system, N=1024, phi=0.60, %d collisions per call" % ncoll,
                 "tangent": {"metric": "collisions/s, 32 tangent vectors, CholQR2 every 100 collisions",
-                            "value": ncoll / t_tan, "unit": UNIT, "lambda_max": float(lam.max())},
+                            "value": ncoll / (ms_tan / 1000), "unit": UNIT, "device_ms": ms_tan,
+                            "e2e": {"value": ncoll / t_tan, "unit": UNIT, "wall_s": t_tan},
+                            "lambda_max": float(lam.max())},
                 "adjoint": {"metric": "collisions/s, adjoint of the final MSD (forward + reverse), "
                                       "checkpoints every 500 collisions",
-                            "value": ncoll / t_adj, "unit": UNIT},
-                "timing": "host wall clock around the synchronous call"}
+                            "value": ncoll / (ms_adj / 1000), "unit": UNIT, "device_ms": ms_adj,
+                            "gradient_wall_s": t_adj,
+                            "e2e": {"value": ncoll / t_adj, "unit": UNIT, "wall_s": t_adj}},
+                "timing": "value: CUDA events on the context's stream around the call (edmd_get_last_ms); "
+                          "e2e: host wall clock around the synchronous C-ABI call"}
     except Exception as e:                               # the main line stands without it
         return {"error": repr(e)[:200]}
 
 
 def run_ours(a, rank, world, dist):
-    cpu_pool = None
-    ncores = os.cpu_count() or 1
+    ncores = usable_cores()
     workload = a.workload
     engine = a.engine if a.engine != "auto" else DEFAULT_ENGINE[workload]
     coll = a.coll if a.coll is not None else DEFAULT_COLL[workload]
-    if rank == 0 and world == 1 and not a.no_cpu_baseline:
+    secondary = workload == "batched" and not a.no_secondary
+    pools = {}
+    fd = None
+    if rank == 0 and not a.no_cpu_baseline:
         # spawn the CPU-baseline processes before the first GPU call
-        cpu_pool = CpuPool(cpu_sample_params(workload, ncores, a.seed), cpu_sample_coll(workload, a))
+        pools[workload] = CpuPool(cpu_sample(workload, ncores, a.seed), cpu_sample_coll(workload, a), ncores)
+        if secondary:
+            pools["single_large"] = CpuPool(cpu_sample("single_large", ncores, a.seed),
+                                            cpu_sample_coll("single_large", a), 1)
+            fd = cpu_fd_gradient(ncores, DIFF_COLL, a.fd_components)
     edmd = _load_edmd()
     L = edmd.load()
     dev = int(os.environ.get("LOCAL_RANK", "0"))
@@ -445,7 +638,7 @@ def run_ours(a, rank, world, dist):
     r = measure(edmd, a, workload, engine, coll, a.steps, a.warmup, rank, world, dist, dev,
                 max(1, min(a.steps, 3)))
     other = {}
-    if workload == "batched" and not a.no_secondary:
+    if secondary:
         s = measure(edmd, a, "single_large", "round", DEFAULT_COLL["single_large"], 3, 3, rank, world,
                     dist, dev, 1)
         other["single_large"] = {"metric": METRICS["single_large"], "value": s["value"], "unit": UNIT,
@@ -455,18 +648,23 @@ def run_ours(a, rank, world, dist):
                                  "gpu_launches": s["launches"]}
         other["differentiation"] = measure_differentiation(edmd)
     if rank != 0:
-        if cpu_pool:
-            cpu_pool.close()
         return 0
     cpu = None
-    if cpu_pool:
-        n, w, rate = cpu_pool.step()
-        cpu_pool.close()
-        nproc = len(cpu_pool.p)
-        cpu = {"value": n / w, "unit": UNIT, "cores": nproc, "kind": "port",
-               "sample": f"{nproc} system(s) of the same workload, one per process, "
-                         f"{cpu_sample_coll(workload, a)} collisions each, oracle restatement (-O2 IEEE), "
-                         f"set-up untimed"}
+    if workload in pools:
+        p = pools[workload]
+        n, w, rate = p.step()
+        p.close()
+        cpu = cpu_line(p, workload, n, w, rate)
+    if "single_large" in pools and "single_large" in other:
+        p = pools["single_large"]
+        n, w, rate = p.step()
+        p.close()
+        other["single_large"]["cpu_baseline"] = cpu_line(p, "single_large", n, w, rate)
+    if fd is not None and "differentiation" in other and "adjoint" in other["differentiation"]:
+        fdr = cpu_fd_finish(*fd)
+        fdr["value"] = DIFF_COLL / fdr["gradient_wall_s"]
+        fdr["unit"] = UNIT + " (collisions of the differentiated trajectory per second of gradient time)"
+        other["differentiation"]["adjoint"]["cpu_baseline"] = fdr
     workload_desc = describe_workload(workload, r["systems"], r["TN"])
     line = {
         "metric": METRICS[workload], "value": r["value"], "unit": UNIT, "n_gpus": world,
@@ -502,8 +700,10 @@ def main():
     ap.add_argument("--radius", type=int, default=4)
     ap.add_argument("--nsys", type=int, default=None)
     ap.add_argument("--coll", type=int, default=None)
-    ap.add_argument("--cpu-coll", type=int, default=1000000)
-    ap.add_argument("--ref-coll", type=int, default=300000)
+    ap.add_argument("--cpu-coll", type=int, default=250000, help="collisions per sampled system (CPU baseline)")
+    ap.add_argument("--ref-coll", type=int, default=250000, help="collisions per sampled system (reference arm)")
+    ap.add_argument("--fd-components", type=int, default=2 * DIFF_N,
+                    help="velocity components timed for the finite-difference gradient")
     ap.add_argument("--seed", type=int, default=20261203)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-secondary", action="store_true")
@@ -512,6 +712,8 @@ def main():
     a = ap.parse_args()
     if a.warmup < 3 and a.impl == "ours":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
+    if a.gpus > 1 and "RANK" not in os.environ:
+        return relaunch_ranks(a.gpus)
     rank, world, dist = dist_init(a.gpus)
     if a.impl == "reference":
         return run_reference(a, rank, world, dist)

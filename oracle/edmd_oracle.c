@@ -88,6 +88,7 @@ struct orc_sys {
 	double tmax, dtime, dtimeThermo, firstScreen, firstThermo;
 	double vr;
 	int grow;               /* 1 while the Lubachevsky-Stillinger growth runs */
+	int stop_at_grow;       /* orc_run returns right after the growth-stop event */
 	/* disks */
 	double *x, *y, *vx, *vy, *tl, *rad, *m, *vrd;
 	int32_t *type, *cx, *cy, *prv, *nxt, *crossX, *crossY;
@@ -736,10 +737,13 @@ int64_t orc_run(orc_sys* s, int64_t max_coll, double t_stop,
 			break;
 		case EV_GROWSTOP: stop_grow(s); break;
 		}
+		if (E->type == EV_GROWSTOP && s->stop_at_grow) break;
 	}
 	if (nev) *nev = ne;
 	return logged;
 }
+
+void orc_set_stop_at_grow(orc_sys* s, int on) { s->stop_at_grow = on; }
 
 void orc_sync_all(orc_sys* s) { for (int i = 0; i < s->N; i++) free_fly(s, i); }
 

@@ -99,6 +99,10 @@ void     orc_virial(orc_sys* s, double out[4], int reset);
 /* g(r) histogram (pcf.c:61-120), counts then normalised */
 int      orc_pcf(const orc_sys* s, double dr, double max_r, double* g, int nbins);
 double   orc_vr(const orc_sys* s);
+/* orc_run returns right after processing the growth-stop event (stopGrow,
+ * src/EDMD.c:4740) when on != 0: the point where a growth start enters the
+ * normal phase, as the engine's EDMD_F_STOP_AT_GROW */
+void     orc_set_stop_at_grow(orc_sys* s, int on);
 /* thermo rows (t Ncol E p px py pxy pyx a2), 9 doubles each; returns count */
 int      orc_thermo_rows(const orc_sys* s, double* out, int cap);
 

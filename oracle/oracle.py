@@ -57,6 +57,7 @@ def load():
         L.orc_time.restype = C.c_double
         L.orc_vr.argtypes = [C.c_void_p]
         L.orc_vr.restype = C.c_double
+        L.orc_set_stop_at_grow.argtypes = [C.c_void_p, C.c_int]
         L.orc_growing.argtypes = [C.c_void_p]
         L.orc_box.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double),
                               C.POINTER(C.c_int), C.POINTER(C.c_int)]
@@ -78,7 +79,7 @@ class Oracle:
     """One serial reference-semantics system on the CPU."""
 
     def __init__(self, N=None, phi=0.7, seed=1, start=HEX, xs=0.0, q=0.4, aspect=1.0, tmax=4000.0,
-                 dtime=100.0, dtime_thermo=100.0, arrays=None, Lx=None, Ly=None):
+                 dtime=100.0, dtime_thermo=100.0, arrays=None, Lx=None, Ly=None, first_thermo=None):
         L = load()
         self._L = L
         if arrays is not None:
@@ -91,6 +92,8 @@ class Oracle:
             L.orc_default_params(C.byref(p))
             p.N, p.phi, p.seed, p.start, p.xs, p.q, p.aspect = N, phi, seed, start, xs, q, aspect
             p.tmax, p.dtime, p.dtimeThermo = tmax, dtime, dtime_thermo
+            if first_thermo is not None:
+                p.firstThermo = first_thermo
             self.h = L.orc_create(C.byref(p))
         self.N = L.orc_N(self.h)
 
@@ -101,6 +104,14 @@ class Oracle:
         n = self._L.orc_run(self.h, int(max_coll), float(t_stop), buf.ctypes.data_as(C.c_void_p),
                             len(buf), None, 0, C.byref(nev))
         return buf[: min(n, len(buf))], n
+
+    def run_growth(self):
+        """Run a growth start up to and including its growth-stop event."""
+        self._L.orc_set_stop_at_grow(self.h, 1)
+        try:
+            return self.run(10 ** 15, cap=1)
+        finally:
+            self._L.orc_set_stop_at_grow(self.h, 0)
 
     def sync(self):
         self._L.orc_sync_all(self.h)
