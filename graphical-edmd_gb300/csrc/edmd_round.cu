@@ -411,7 +411,8 @@ __device__ __forceinline__ void merge(double& bd, uint64_t& bk, int& bo, int& bp
 
 __device__ void predict_warp(const SysDev& S, int a0, const Disk& A0, int X0, int Y0, int a1,
                              const Disk& A1, int X1, int Y1, double t, Pred& r0, Pred& r1,
-                             WarpScratch* W, int lane, unsigned long long* npair, bool* ovl, int* ob) {
+                             WarpScratch* W, int lane, unsigned long long* npair, bool* ovl, int* oa,
+                             int* ob) {
   const Box& B = S.B;
   const int grp = lane >> 4, q = lane & 15;
   const int a = grp ? a1 : a0;
@@ -438,7 +439,7 @@ __device__ void predict_warp(const SysDev& S, int a0, const Disk& A0, int X0, in
   int bo0 = -1, bo1 = -1, bp0 = 0, bp1 = 0;
   uint32_t bc0 = 0, bc1 = 0;
   bool lovl = false;
-  int lb = -1;
+  int la = -1, lb = -1;               // the predicting disk and the partner that overlaps it
   unsigned long long tot;
   if (!spill) {
     int incl = cnt;
@@ -463,7 +464,7 @@ __device__ void predict_warp(const SysDev& S, int a0, const Disk& A0, int X0, in
       const bool g1 = f >= tot0;
       bool ov = false;
       const double d = coll_time_normal_i(B, g1 ? A1 : A0, P, t, &ov);
-      if (ov) { lovl = true; lb = p; }
+      if (ov) { lovl = true; la = g1 ? a1 : a0; lb = p; }
       const uint64_t kd = time_key(d);
       if (g1) merge(bd1, bk1, bo1, bp1, bc1, d, kd, o, p, P.coll);
       else merge(bd0, bk0, bo0, bp0, bc0, d, kd, o, p, P.coll);
@@ -481,7 +482,7 @@ __device__ void predict_warp(const SysDev& S, int a0, const Disk& A0, int X0, in
         if (p != a) {
           bool ov = false;
           const double d = coll_time_normal_i(B, AA, P, t, &ov);
-          if (ov) { lovl = true; lb = p; }
+          if (ov) { lovl = true; la = a; lb = p; }
           const uint64_t kd = time_key(d);
           if (grp) merge(bd1, bk1, bo1, bp1, bc1, d, kd, q * (1 << 20) + k, p, P.coll);
           else merge(bd0, bk0, bo0, bp0, bc0, d, kd, q * (1 << 20) + k, p, P.coll);
@@ -524,9 +525,10 @@ __device__ void predict_warp(const SysDev& S, int a0, const Disk& A0, int X0, in
   const unsigned m = __ballot_sync(FULLM, lovl);
   if (m) {
     *ovl = true;
+    *oa = __shfl_sync(FULLM, la, __ffs(m) - 1);
     *ob = __shfl_sync(FULLM, lb, __ffs(m) - 1);
   }
-  if (__any_sync(FULLM, lcorrupt)) { *ovl = true; *ob = OB_CORRUPT; }
+  if (__any_sync(FULLM, lcorrupt)) { *ovl = true; *oa = a0; *ob = OB_CORRUPT; }
 }
 
 __device__ __forceinline__ void set_event(const SysDev& S, int slot, double t, int j, uint32_t ca,
@@ -751,7 +753,8 @@ __device__ void process_event_warp(const SysDev& S, const RoundArgs& A, int s, i
       ctc = crossing_time_lanes(B, od ? Db : Da, od ? pbx : pax, od ? pby : pay, t, lane, 2, &cdir);
     }
     Pred p0, p1;
-    predict_warp(S, a, Da, pax, pay, b, Db, pbx, pby, t, p0, p1, W, lane, &npair, &ovl, &ob);
+    int oa = a;
+    predict_warp(S, a, Da, pax, pay, b, Db, pbx, pby, t, p0, p1, W, lane, &npair, &ovl, &oa, &ob);
     npred = b >= 0 ? 2 : 1;
     const double tca = __shfl_sync(FULLM, ctc, 0), tcb = __shfl_sync(FULLM, ctc, 1);
     const int dira = __shfl_sync(FULLM, cdir, 0), dirb = __shfl_sync(FULLM, cdir, 1);
@@ -772,7 +775,7 @@ __device__ void process_event_warp(const SysDev& S, const RoundArgs& A, int s, i
     res.ct = ct[0];
     res.key = key;
     res.bad = bad; res.ovl = ovl;
-    res.a = a; res.ob = ob;
+    res.a = oa; res.ob = ob;
 }
 
 // ---- one thread per event (rounds with many selected events): the lanes of
@@ -983,7 +986,9 @@ __device__ void process_event_thread(const SysDev& S, const RoundArgs& A, int s,
       const double tc = crossing_time_i(B, Dd, X, Y, t, &dir);
       set_event(S, d, tc, dir, 0, 0, clk);
     }
+    const bool had = res.ovl;
     const Pred pr = predict_thread(S, A, s, d, Dd, X, Y, t, &res.npair, &res.nscreen, &res.ovl, &res.ob);
+    if (res.ovl && !had) res.a = d;        // the disk whose prediction met the overlap
     set_event(S, N + d, t + pr.dt, pr.partner, pr.ca, pr.pcell, clk);
     A.drank[gd] = 2;
     uint64_t k2; int c1, c2;
