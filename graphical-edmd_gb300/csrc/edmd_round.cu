@@ -35,9 +35,11 @@
 // summation order of the virial and the order of the trace differ.  Equal
 // keys are ordered like the serial queue orders them: mutual equal-time
 // predictions inherited from a serial engine carry the rank of their queue
-// keys (k_rank) in the event id, and new ones rank after them; two valid
-// mutual events give bit-identical velocities in either order since the
-// collision rule is odd in (dx, dy) and in (dvx, dvy).
+// keys (k_rank) in the event id; a new event that ties with the inherited
+// event of its partner for the same pair ranks by the serial key it would
+// have been given (new_rank), other new ones rank after inherited ones; two
+// valid mutual events give bit-identical velocities in either order since
+// the collision rule is odd in (dx, dy) and in (dvx, dvy).
 #include <cstdio>
 #include <cstdint>
 #include <cstring>
@@ -54,6 +56,11 @@ constexpr int RTILE = 12;             // largest window radius of the tile kerne
 constexpr int MAXDIRTY = 8;           // cells whose minimum one event can change
 constexpr int MAXC = 8;               // candidates buffered per cell list per lane
 constexpr int OB_CORRUPT = -2;        // overlap partner marker: a cell list longer than N (EDMD_ERR_BUDGET)
+// tie ranks of collision events (the top byte of an event id, see event_id):
+// inherited mutual pairs are 1 (pops first) and 2, events this engine makes
+// are R_NEW, or R_FIRST when the serial queue would pop them before the
+// inherited event of equal time they tie with (new_rank)
+constexpr uint8_t R_FIRST = 0, R_NEW = 3;
 constexpr int WPB = 8;                // warps per block of the processing kernel
 constexpr int NSTRIPE = 32;           // copies of each system's counters
 // counters of the round engine, per system and stripe (u64 slots)
@@ -71,7 +78,9 @@ struct RoundArgs {
   const int64_t* coff;           // cell offset of each system
   uint64_t* dkey;                // time key of each disk's next event (KINF: none)
   int32_t* dpk;                  // its id: serial tie rank << 24 | disk
-  uint8_t* drank;                // tie rank of each disk's collision event
+  uint8_t* drank;                // tie rank of each disk's collision event (R_FIRST .. R_NEW)
+  uint32_t* ikb;                 // serial queue key (bucket, tie) of each disk's collision event
+  uint64_t* iktie;               // as inherited from a serial engine (k_rank)
   int32_t* fc;                   // its two footprint cells (local), 2 per disk
   uint64_t* cmt; int32_t* cmi;   // attributed minimum (key, id) per cell
   uint64_t* lw; uint64_t* lr;    // causality stamps per cell
@@ -183,9 +192,9 @@ __device__ __forceinline__ int32_t event_id(const RoundArgs& A, int64_t g, int s
 // mutual predictions a->b, b->a made by one handler from the same positions
 // (the initial predictions, and stopGrow, src/EDMD.c:4740-4800, whose coll++
 // inside the loop leaves one of the two stale); their serial order is the
-// order of their queue keys (b, tie).  Rank 0 or 1 orders such a pair; events
-// the round engine creates later get rank 2 (a new prediction is never stale,
-// so a tie of two valid mutual events gives the same state either way).
+// order of their queue keys (b, tie).  Rank 1 or 2 orders such a pair, and
+// the serial keys are kept for new_rank: a stale inherited event can tie with
+// the valid new prediction its partner makes later for the same pair.
 __global__ void k_rank(const SysDev* __restrict__ sys, RoundArgs A) {
   const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= A.TN) return;
@@ -194,13 +203,61 @@ __global__ void k_rank(const SysDev* __restrict__ sys, RoundArgs A) {
   const int N = S.B.N;
   const int i = (int)(g - A.doff[s]);
   const Ev e = S.ev[N + i];
-  uint8_t rank = 0;
+  uint8_t rank = 1;
   if (e.st & 3u) {
     const Ev f = S.ev[N + e.j];
     if ((f.st & 3u) && f.j == i && __double_as_longlong(f.t) == __double_as_longlong(e.t))
-      rank = (f.b < e.b || (f.b == e.b && f.tie < e.tie)) ? 1 : 0;
+      rank = (f.b < e.b || (f.b == e.b && f.tie < e.tie)) ? 2 : 1;
   }
   A.drank[g] = rank;
+  A.ikb[g] = e.b;                      // k_prep overwrites b and tie next
+  A.iktie[g] = e.tie;
+}
+
+// Serial order of a new collision event (time tn, inserted at the pop clock
+// clk of the event that made it) against an inherited one of equal time with
+// serial key (bx, tiex): true when the serial queue pops the new one first.
+// The new event's key is what addEventToQueue (src/EDMD.c:2144) would give it:
+// the calendar at the creator's pop is the bucket holding its clock, reached
+// from the inherited calendar state (k, paulTime) by repeated addition of
+// the bucket width as the serial loop does.  Same bucket: class 0 (re-added
+// by a wrap) < 1 (bucket list, last pushed first) < 2 (direct insert, first
+// inserted first); an event in the overflow list is re-added at the wrap, the
+// last pushed first.
+__device__ bool new_before_inherited(const SysDev& S, double tn, uint64_t clk, uint32_t bx, uint64_t tiex) {
+  const Box& B = S.B;
+  const SysState& R = *S.st;
+  const double tc = key_time(clk);
+  uint64_t k = R.k;
+  double P = R.P;
+  for (int guard = 0; guard < (1 << 24) && P + B.dtP <= tc; guard++) { P += B.dtP; k++; }
+  const double dt = tn - P;
+  const bool ovf_new = dt >= B.dtPN;
+  if (bx == BINF) return ovf_new;
+  if (ovf_new) return false;
+  uint64_t by, cy;
+  if (!(dt >= B.dtP)) { by = k; cy = 2; }
+  else { by = k + (uint64_t)bucket_offset(dt, B.dtP, S.rdtP); cy = 1; }
+  const uint64_t cx = tiex >> 62;
+  if (by != (uint64_t)bx) return by < (uint64_t)bx;
+  if (cy != cx) return cy < cx;
+  return cy == 1;
+}
+
+// tie rank of the new collision event of disk d (time tn, partner p) made by
+// an event of pop clock clk whose other disk is `other`: R_FIRST when it ties
+// exactly with p's still inherited event for the mutual pair and the serial
+// queue pops it first (a tie of a stale inherited event, such as stopGrow
+// leaves, with a valid new one decides the trajectory), else R_NEW
+__device__ __forceinline__ uint8_t new_rank(const SysDev& S, const RoundArgs& A, int64_t dbase, int d, int other,
+                                            double tn, int p, uint64_t clk) {
+  if (p == d || p == other) return R_NEW;
+  const int64_t gp = dbase + p;
+  const uint8_t rp = A.drank[gp];
+  if (rp == R_NEW || rp == R_FIRST) return R_NEW;
+  const Ev X = S.ev[S.B.N + p];
+  if (!(X.st & 3u) || X.j != d || __double_as_longlong(X.t) != __double_as_longlong(tn)) return R_NEW;
+  return new_before_inherited(S, tn, clk, A.ikb[gp], A.iktie[gp]) ? R_FIRST : R_NEW;
 }
 
 // serial pop clock and stored partner cell of every pending event, then the
@@ -761,10 +818,12 @@ __device__ void process_event_warp(const SysDev& S, const RoundArgs& A, int s, i
     if (lane == 0) {
       if (cross) set_event(S, a, tca, dira, 0, 0, clk);
       if (b >= 0) set_event(S, b, tcb, dirb, 0, 0, clk);
+      const uint8_t rka = new_rank(S, A, dbase, a, b, t + p0.dt, p0.partner, clk);
+      const uint8_t rkb = b >= 0 ? new_rank(S, A, dbase, b, a, t + p1.dt, p1.partner, clk) : R_NEW;
       set_event(S, N + a, t + p0.dt, p0.partner, p0.ca, p0.pcell, clk);
       if (b >= 0) set_event(S, N + b, t + p1.dt, p1.partner, p1.ca, p1.pcell, clk);
-      A.drank[g] = 2;
-      if (b >= 0) A.drank[gb] = 2;
+      A.drank[g] = rka;
+      if (b >= 0) A.drank[gb] = rkb;
       reattribute(S, A, a, g, base, dc, &nd);
       if (b >= 0) reattribute(S, A, b, gb, base, dc, &nd);
     }
@@ -989,8 +1048,9 @@ __device__ void process_event_thread(const SysDev& S, const RoundArgs& A, int s,
     const bool had = res.ovl;
     const Pred pr = predict_thread(S, A, s, d, Dd, X, Y, t, &res.npair, &res.nscreen, &res.ovl, &res.ob);
     if (res.ovl && !had) res.a = d;        // the disk whose prediction met the overlap
+    const uint8_t rk = new_rank(S, A, dbase, d, q ? a : b, t + pr.dt, pr.partner, clk);
     set_event(S, N + d, t + pr.dt, pr.partner, pr.ca, pr.pcell, clk);
-    A.drank[gd] = 2;
+    A.drank[gd] = rk;
     uint64_t k2; int c1, c2;
     const int sl = attribution(S, d, &k2, &c1, &c2);
     A.dkey[gd] = k2; A.dpk[gd] = event_id(A, gd, sl, N); A.fc[2 * gd] = c1; A.fc[2 * gd + 1] = c2;
@@ -1430,6 +1490,8 @@ struct RoundBufs {
   int32_t *dsys = nullptr, *fc = nullptr, *cmi = nullptr, *safe = nullptr, *nsafe = nullptr;
   int32_t *dcell = nullptr, *selflag = nullptr, *active = nullptr, *dpk = nullptr, *work = nullptr;
   uint8_t *drank = nullptr, *drank_bak = nullptr;
+  uint32_t* ikb = nullptr;
+  uint64_t* iktie = nullptr;
   int32_t *tsys = nullptr, *tx0 = nullptr, *ty0 = nullptr;
   int64_t *doff = nullptr, *coff = nullptr;
   uint64_t *dkey = nullptr, *cmt = nullptr, *lw = nullptr, *lr = nullptr;
@@ -1462,6 +1524,7 @@ int round_init(edmd_ctx* ctx) {
   if (TN > GMASK) return set_err(ctx, EDMD_ERR_CAPACITY, "the round engine supports up to 2^24 disks per context");
   CK(dalloc(&R->dsys, TN)); CK(dalloc(&R->fc, 2 * TN)); CK(dalloc(&R->dkey, TN)); CK(dalloc(&R->dpk, TN));
   CK(dalloc(&R->drank, TN)); CK(dalloc(&R->drank_bak, TN));
+  CK(dalloc(&R->ikb, TN)); CK(dalloc(&R->iktie, TN));
   CK(dalloc(&R->cmi, TC)); CK(dalloc(&R->cmt, TC)); CK(dalloc(&R->lw, TC)); CK(dalloc(&R->lr, TC));
   CK(dalloc(&R->safe, TN)); CK(dalloc(&R->nsafe, 1)); CK(dalloc(&R->dcell, TN * MAXDIRTY));
   CK(dalloc(&R->selflag, ctx->nsys)); CK(dalloc(&R->active, 1)); CK(dalloc(&R->work, 1));
@@ -1509,7 +1572,7 @@ void round_free(edmd_ctx* ctx) {
   void* p[] = {R->dsys, R->fc, R->cmi, R->safe, R->nsafe, R->dcell, R->selflag, R->active,
                R->tsys, R->tx0, R->ty0, R->doff, R->coff, R->dkey, R->cmt, R->lw, R->lr,
                R->lim, R->target, R->freeze, R->tlast, R->cnt, R->viol, R->dpk, R->drank,
-               R->drank_bak, R->work, R->shp, R->sht, R->epoch};
+               R->drank_bak, R->ikb, R->iktie, R->work, R->shp, R->sht, R->epoch};
   for (void* q : p)
     if (q) cudaFree(q);
   delete R;
@@ -1542,7 +1605,7 @@ static int run_rounds(edmd_ctx* ctx, const std::vector<uint64_t>& tgt, double t_
     A.tstop_key = (u >> 63) ? ~u : (u | 0x8000000000000000ull);
   }
   A.dsys = R->dsys; A.doff = R->doff; A.coff = R->coff;
-  A.dkey = R->dkey; A.dpk = R->dpk; A.drank = R->drank; A.fc = R->fc; A.cmt = R->cmt; A.cmi = R->cmi; A.lw = R->lw; A.lr = R->lr;
+  A.dkey = R->dkey; A.dpk = R->dpk; A.drank = R->drank; A.ikb = R->ikb; A.iktie = R->iktie; A.fc = R->fc; A.cmt = R->cmt; A.cmi = R->cmi; A.lw = R->lw; A.lr = R->lr;
   A.safe = R->safe; A.nsafe = R->nsafe; A.dcell = R->dcell; A.selflag = R->selflag;
   A.active = R->active; A.lim = R->lim; A.target = R->target; A.freeze = R->freeze;
   // one thread per event needs enough events to keep every SM busy with one
