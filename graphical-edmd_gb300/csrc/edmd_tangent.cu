@@ -27,10 +27,9 @@ namespace {
 
 // T is row-major [4N][K]: row 4i+c holds component c (dx, dy, dvx, dvy) of disk
 // i for the K tangent vectors, so lane k of a warp reads one coalesced row.
-__global__ void k_tangent_apply(const edmd_log_entry* __restrict__ log, int64_t M,
-                                const Disk* __restrict__ d, double* __restrict__ T,
-                                double* __restrict__ tl, int K) {
-  const int k = threadIdx.x;
+__device__ __forceinline__ void tangent_apply_warp(const edmd_log_entry* __restrict__ log, int64_t M,
+                                                   const Disk* __restrict__ d, double* __restrict__ T,
+                                                   double* __restrict__ tl, int K, int k) {
   for (int64_t n = 0; n < M; n++) {
     const edmd_log_entry L = log[n];
     const int i = L.i, j = L.j;
@@ -61,6 +60,12 @@ __global__ void k_tangent_apply(const edmd_log_entry* __restrict__ log, int64_t 
     if (k == 0) { tl[i] = L.t; tl[j] = L.t; }
     __syncwarp();
   }
+}
+
+__global__ void k_tangent_apply(const edmd_log_entry* __restrict__ log, int64_t M,
+                                const Disk* __restrict__ d, double* __restrict__ T,
+                                double* __restrict__ tl, int K) {
+  tangent_apply_warp(log, M, d, T, tl, K, threadIdx.x);
 }
 
 // value of row e at the common time tq (virtual free flight, T itself unchanged)
@@ -100,9 +105,8 @@ __global__ void k_gram_sum(const double* __restrict__ Gp, int nblocks, int K, do
 }
 
 // Cholesky G = R^T R (R upper), logs of diag(R) accumulated, Rinv = R^-1
-__global__ void k_chol(const double* __restrict__ G, int K, double* __restrict__ Rinv,
-                       double* __restrict__ logdiag, int accumulate, int* __restrict__ fail) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+__device__ void chol_one(const double* __restrict__ G, int K, double* __restrict__ Rinv,
+                         double* __restrict__ logdiag, int accumulate, int* __restrict__ fail) {
   double R[32][32];
   for (int a = 0; a < K; a++)
     for (int b = 0; b < K; b++) R[a][b] = 0;
@@ -129,11 +133,15 @@ __global__ void k_chol(const double* __restrict__ G, int K, double* __restrict__
   }
 }
 
+__global__ void k_chol(const double* __restrict__ G, int K, double* __restrict__ Rinv,
+                       double* __restrict__ logdiag, int accumulate, int* __restrict__ fail) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  chol_one(G, K, Rinv, logdiag, accumulate, fail);
+}
+
 // T <- T' Rinv at the common time tq (every disk's tangent clock set to tq)
-__global__ void k_apply_rinv(double* __restrict__ T, double* __restrict__ tl, int N, int K, double tq,
-                             const double* __restrict__ Rinv) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= N) return;
+__device__ __forceinline__ void apply_rinv_disk(double* __restrict__ T, double* __restrict__ tl, int i, int K,
+                                                double tq, const double* __restrict__ Rinv) {
   double row[4][32];
   for (int c = 0; c < 4; c++)
     for (int k = 0; k < K; k++) row[c][k] = row_at(T, tl, 4 * i + c, k, K, tq);
@@ -146,15 +154,21 @@ __global__ void k_apply_rinv(double* __restrict__ T, double* __restrict__ tl, in
   tl[i] = tq;
 }
 
+__global__ void k_apply_rinv(double* __restrict__ T, double* __restrict__ tl, int N, int K, double tq,
+                             const double* __restrict__ Rinv) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  apply_rinv_disk(T, tl, i, K, tq, Rinv);
+}
+
 // ---------------------------------------------------------------- adjoint kernels
 
 // one thread: sweep a segment of the log backwards, applying the transpose of
 // the collision map and of the free flights between collisions.
 // A is [N][4]: (g_x, g_y, g_vx, g_vy) of each disk at its time ta[i].
-__global__ void k_adjoint_segment(const edmd_log_entry* __restrict__ log, int64_t M,
-                                  const Disk* __restrict__ d, double* __restrict__ A,
-                                  double* __restrict__ ta) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+__device__ void adjoint_segment(const edmd_log_entry* __restrict__ log, int64_t M,
+                                const Disk* __restrict__ d, double* __restrict__ A,
+                                double* __restrict__ ta) {
   for (int64_t n = M - 1; n >= 0; n--) {
     const edmd_log_entry L = log[n];
     const int i = L.i, j = L.j;
@@ -189,6 +203,13 @@ __global__ void k_adjoint_segment(const edmd_log_entry* __restrict__ log, int64_
   }
 }
 
+__global__ void k_adjoint_segment(const edmd_log_entry* __restrict__ log, int64_t M,
+                                  const Disk* __restrict__ d, double* __restrict__ A,
+                                  double* __restrict__ ta) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  adjoint_segment(log, M, d, A, ta);
+}
+
 // every disk's adjoint brought back to t0 (transpose of the first free flight)
 __global__ void k_adjoint_finish(int N, double* __restrict__ A, const double* __restrict__ ta, double t0) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -200,6 +221,170 @@ __global__ void k_adjoint_finish(int N, double* __restrict__ A, const double* __
 __global__ void k_fill(double* p, int64_t n, double v) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) p[i] = v;
+}
+
+// ---------------------------------------------------------------- batched kernels
+// Every system of a context at once: system s owns the disks doff[s] ..
+// doff[s] + N_s - 1 of the concatenated arrays and rows 4 doff[s] .. of T.
+
+// system index of each disk
+__global__ void k_disk_sys(const SysDev* __restrict__ sys, const int64_t* __restrict__ doff, int nsys,
+                           int32_t* __restrict__ dsys) {
+  for (int s = blockIdx.y; s < nsys; s += gridDim.y)
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < sys[s].B.N; i += gridDim.x * blockDim.x)
+      dsys[doff[s] + i] = s;
+}
+
+// every disk's clock set to its system's current time
+__global__ void k_fill_sys_time(const SysDev* __restrict__ sys, const int32_t* __restrict__ dsys, int64_t TN,
+                                double* __restrict__ tl) {
+  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g < TN) tl[g] = sys[dsys[g]].st->t;
+}
+
+// one warp per system: the tangent map over the system's collision log
+__global__ void k_tangent_apply_b(const SysDev* __restrict__ sys, const int64_t* __restrict__ doff,
+                                  double* __restrict__ T, double* __restrict__ tl, int K) {
+  const SysDev& S = sys[blockIdx.x];
+  int64_t M = (int64_t)S.st->nlog;
+  if (M > S.log_cap) M = S.log_cap;
+  const int64_t o = doff[blockIdx.x];
+  tangent_apply_warp((const edmd_log_entry*)S.log, M, S.d, T + (size_t)4 * o * K, tl + o, K, threadIdx.x);
+}
+
+// one block of 32 x 32 threads per system: its Gram matrix at its current
+// time, rows taken 32 at a time in index order (deterministic)
+__global__ void k_gram_b(const SysDev* __restrict__ sys, const int64_t* __restrict__ doff,
+                         const double* __restrict__ T, const double* __restrict__ tl, int K,
+                         double* __restrict__ G) {
+  __shared__ double rows[32][33];
+  const SysDev& S = sys[blockIdx.x];
+  const int N = S.B.N;
+  const double tq = S.st->t;
+  const int64_t o = doff[blockIdx.x];
+  const double* Ts = T + (size_t)4 * o * K;
+  const double* tls = tl + o;
+  const int k = threadIdx.x & 31, l = threadIdx.x >> 5;
+  double acc = 0;
+  for (int e0 = 0; e0 < 4 * N; e0 += 32) {
+    const int e = e0 + l;
+    rows[l][k] = (e < 4 * N && k < K) ? row_at(Ts, tls, e, k, K, tq) : 0.0;
+    __syncthreads();
+    if (k < K && l < K)
+      for (int r = 0; r < 32; r++) acc += rows[r][k] * rows[r][l];
+    __syncthreads();
+  }
+  if (k < K && l < K) G[(size_t)blockIdx.x * K * K + k * K + l] = acc;
+}
+
+__global__ void k_chol_b(const double* __restrict__ G, int nsys, int K, double* __restrict__ Rinv,
+                         double* __restrict__ logdiag, int accumulate, int* __restrict__ fail) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nsys) return;
+  chol_one(G + (size_t)s * K * K, K, Rinv + (size_t)s * K * K, logdiag + (size_t)s * K, accumulate, fail + s);
+}
+
+__global__ void k_apply_rinv_b(const SysDev* __restrict__ sys, const int64_t* __restrict__ doff,
+                               const int32_t* __restrict__ dsys, int64_t TN, double* __restrict__ T,
+                               double* __restrict__ tl, int K, const double* __restrict__ Rinv) {
+  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= TN) return;
+  const int s = dsys[g];
+  const int64_t o = doff[s];
+  apply_rinv_disk(T + (size_t)4 * o * K, tl + o, (int)(g - o), K, sys[s].st->t, Rinv + (size_t)s * K * K);
+}
+
+// one thread per system: the transposed map backwards over its segment log
+__global__ void k_adjoint_segment_b(const SysDev* __restrict__ sys, const int64_t* __restrict__ doff, int nsys,
+                                    double* __restrict__ A, double* __restrict__ ta) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nsys) return;
+  const SysDev& S = sys[s];
+  int64_t M = (int64_t)S.st->nlog;
+  if (M > S.log_cap) M = S.log_cap;
+  adjoint_segment((const edmd_log_entry*)S.log, M, S.d, A + 4 * (size_t)doff[s], ta + doff[s]);
+}
+
+// every disk's position flown (virtually) to its system's current time
+__global__ void k_positions_now_b(const SysDev* __restrict__ sys, const int64_t* __restrict__ doff,
+                                  const int32_t* __restrict__ dsys, int64_t TN, double* __restrict__ x,
+                                  double* __restrict__ y) {
+  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= TN) return;
+  const int s = dsys[g];
+  const Disk p = sys[s].d[g - doff[s]];
+  const double t = sys[s].st->t;
+  x[g] = p.x + p.vx * (t - p.tl);
+  y[g] = p.y + p.vy * (t - p.tl);
+}
+
+// one block per system: MSD = (1/N) sum |u_i - <u>|^2 of the minimum-image
+// displacements u from (x0, y0) to (x1, y1), its gradient with respect to
+// the final positions in A (velocity parts zero) and the direct term
+// 2 (u_i - <u>) / N in (dux, duy); sums over disks by a fixed tree
+__global__ void k_msd_b(const SysDev* __restrict__ sys, const int64_t* __restrict__ doff,
+                        const double* __restrict__ x0, const double* __restrict__ y0,
+                        const double* __restrict__ x1, const double* __restrict__ y1, double* __restrict__ A,
+                        double* __restrict__ ta, double* __restrict__ dux, double* __restrict__ duy,
+                        double* __restrict__ msd) {
+  __shared__ double sx[256], sy[256];
+  const SysDev& S = sys[blockIdx.x];
+  const int N = S.B.N;
+  const double Lx = S.B.Lx, Ly = S.B.Ly, T = S.st->t;
+  const int64_t o = doff[blockIdx.x];
+  auto disp = [&](int i, double* ux, double* uy) {
+    double dx = x1[o + i] - x0[o + i], dy = y1[o + i] - y0[o + i];
+    dx -= Lx * nearbyint(dx / Lx);
+    dy -= Ly * nearbyint(dy / Ly);
+    *ux = dx; *uy = dy;
+  };
+  double ax = 0, ay = 0;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    double ux, uy;
+    disp(i, &ux, &uy);
+    ax += ux; ay += uy;
+  }
+  sx[threadIdx.x] = ax; sy[threadIdx.x] = ay;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) { sx[threadIdx.x] += sx[threadIdx.x + w]; sy[threadIdx.x] += sy[threadIdx.x + w]; }
+    __syncthreads();
+  }
+  const double mx = sx[0] / N, my = sy[0] / N;
+  __syncthreads();
+  double acc = 0;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    double ux, uy;
+    disp(i, &ux, &uy);
+    const double a = ux - mx, b = uy - my;
+    acc += a * a + b * b;
+    double* Ai = A + 4 * (o + i);
+    Ai[0] = 2.0 * a / N; Ai[1] = 2.0 * b / N; Ai[2] = 0; Ai[3] = 0;
+    dux[o + i] = 2.0 * a / N; duy[o + i] = 2.0 * b / N;
+    ta[o + i] = T;
+  }
+  sx[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) sx[threadIdx.x] += sx[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) msd[blockIdx.x] = sx[0] / N;
+}
+
+// every disk's adjoint brought back to its system's initial time t0[s]
+__global__ void k_adjoint_finish_b(const int32_t* __restrict__ dsys, int64_t TN, double* __restrict__ A,
+                                   const double* __restrict__ ta, const double* __restrict__ t0) {
+  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= TN) return;
+  const double t = t0[dsys[g]];
+  A[4 * g + 2] += A[4 * g + 0] * (ta[g] - t);
+  A[4 * g + 3] += A[4 * g + 1] * (ta[g] - t);
+}
+
+__global__ void k_sys_times(const SysDev* __restrict__ sys, int nsys, double* __restrict__ t) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < nsys) t[s] = sys[s].st->t;
 }
 
 // positions of one system flown (virtually) to time t, without touching the state
@@ -512,6 +697,191 @@ extern "C" int edmd_msd_gradient(edmd_ctx* ctx, int32_t s, int64_t n_coll, int64
     if (g_vy) g_vy[i] = hA[4 * i + 3];
   }
   if (msd_out) *msd_out = msd;
+  CK(call_end(ctx));
+  return EDMD_OK;
+}
+
+// ==================================================================== batched drivers
+
+namespace {
+
+// device arrays every batched driver needs: each system's first disk and each
+// disk's system; freed with the scope
+struct BatchIndex {
+  int64_t* doff = nullptr;
+  int32_t* dsys = nullptr;
+  ~BatchIndex() {
+    if (doff) cudaFree(doff);
+    if (dsys) cudaFree(dsys);
+  }
+};
+
+int batch_index(edmd_ctx* ctx, BatchIndex& bi) {
+  CK(dalloc(&bi.doff, ctx->nsys));
+  CK(dalloc(&bi.dsys, ctx->total_N));
+  CK(cudaMemcpyAsync(bi.doff, ctx->disk_off.data(), ctx->nsys * sizeof(int64_t), cudaMemcpyHostToDevice,
+                     ctx->stream));
+  dim3 g((unsigned)((ctx->maxN + 255) / 256), (unsigned)(ctx->nsys < 65535 ? ctx->nsys : 65535));
+  k_disk_sys<<<g, 256, 0, ctx->stream>>>(ctx->ds, bi.doff, ctx->nsys, bi.dsys);
+  CK(cudaGetLastError());
+  return EDMD_OK;
+}
+
+// one advance of every system with the collision log; EDMD_ERR_CAPACITY when
+// a system logged more than the log holds
+int advance_logged_all(edmd_ctx* ctx, int64_t ncoll) {
+  int rc = edmd_clear_log(ctx);
+  if (rc) return rc;
+  rc = edmd_advance(ctx, ncoll, INFINITY, EDMD_F_LOG | EDMD_F_COUNT_NORMAL, (int64_t)1 << 60, nullptr);
+  if (rc) return rc;
+  std::vector<uint64_t> nl(ctx->nsys);
+  CK(sync_copy2d(ctx, nl.data(), 8, &ctx->st[0].nlog, sizeof(SysState), 8, ctx->nsys, cudaMemcpyDeviceToHost));
+  for (uint64_t v : nl)
+    if ((int64_t)v > ctx->log_cap) return set_err(ctx, EDMD_ERR_CAPACITY, "collision log overflow");
+  return EDMD_OK;
+}
+
+int cholqr_b(edmd_ctx* ctx, const BatchIndex& bi, double* T, double* tl, int K, double* G, double* Rinv,
+             double* logdiag, int* fail, bool accumulate) {
+  const int64_t TN = ctx->total_N;
+  for (int pass = 0; pass < 2; pass++) {    // CholQR2: the second pass restores orthogonality
+    k_gram_b<<<ctx->nsys, 1024, 0, ctx->stream>>>(ctx->ds, bi.doff, T, tl, K, G);
+    k_chol_b<<<(ctx->nsys + 63) / 64, 64, 0, ctx->stream>>>(G, ctx->nsys, K, Rinv, logdiag, accumulate ? 1 : 0,
+                                                            fail);
+    k_apply_rinv_b<<<(unsigned)((TN + 127) / 128), 128, 0, ctx->stream>>>(ctx->ds, bi.doff, bi.dsys, TN, T, tl,
+                                                                         K, Rinv);
+    CK(cudaGetLastError());
+  }
+  std::vector<int> h(ctx->nsys);
+  CK(sync_copy(ctx, h.data(), fail, ctx->nsys * sizeof(int), cudaMemcpyDeviceToHost));
+  for (int s = 0; s < ctx->nsys; s++)
+    if (h[s]) return set_err(ctx, EDMD_ERR_ARG, "tangent vectors of system " + std::to_string(s) +
+                                                    " became linearly dependent");
+  return EDMD_OK;
+}
+
+int sys_times(edmd_ctx* ctx, double* host) {
+  CK(sync_copy2d(ctx, host, 8, &ctx->st[0].t, sizeof(SysState), 8, ctx->nsys, cudaMemcpyDeviceToHost));
+  return EDMD_OK;
+}
+
+}  // namespace
+
+extern "C" int edmd_tangent_run_batch(edmd_ctx* ctx, int32_t K, int64_t n_coll, int64_t qr_every, uint64_t seed,
+                                      double* lyap_out) {
+  if (!ctx || K < 1 || K > 32 || n_coll < 0 || qr_every < 0) return EDMD_ERR_ARG;
+  if (ctx->engine != EDMD_ENGINE_WARP) return set_err(ctx, EDMD_ERR_ARG, "tangents need the warp engine");
+  const int64_t TN = ctx->total_N;
+  const int nsys = ctx->nsys;
+  const int64_t chunk = qr_every > 0 ? qr_every : (n_coll > 0 ? n_coll : 1);
+  int rc = edmd_set_log_capacity(ctx, chunk + 16);
+  if (rc) return rc;
+  BatchIndex bi;
+  if ((rc = batch_index(ctx, bi))) return rc;
+  double *T = nullptr, *tl = nullptr, *G = nullptr, *Rinv = nullptr, *logdiag = nullptr;
+  int* fail = nullptr;
+  CK(dalloc(&T, (size_t)4 * TN * K));
+  CK(dalloc(&tl, TN));
+  CK(dalloc(&G, (size_t)nsys * K * K));
+  CK(dalloc(&Rinv, (size_t)nsys * K * K));
+  CK(dalloc(&logdiag, (size_t)nsys * K));
+  CK(dalloc(&fail, nsys));
+  struct Free { void* p[6]; ~Free() { for (void* q : p) if (q) cudaFree(q); } } guard{{T, tl, G, Rinv, logdiag, fail}};
+  // system s starts from the vectors edmd_tangent_run draws from seed + s
+  // (drawn on the host before the timed part of the call)
+  std::vector<double> h((size_t)4 * TN * K);
+  for (int s = 0; s < nsys; s++) {
+    std::mt19937_64 g(seed + (uint64_t)s);
+    std::normal_distribution<double> nd(0.0, 1.0);
+    double* hs = h.data() + (size_t)4 * ctx->disk_off[s] * K;
+    for (size_t e = 0; e < (size_t)4 * ctx->hs[s].B.N * K; e++) hs[e] = nd(g);
+  }
+  CK(call_begin(ctx));
+  std::vector<double> t0(nsys), t1(nsys);
+  if ((rc = sys_times(ctx, t0.data()))) return rc;
+  CK(cudaMemcpyAsync(T, h.data(), h.size() * 8, cudaMemcpyHostToDevice, ctx->stream));
+  k_fill_sys_time<<<(unsigned)((TN + 255) / 256), 256, 0, ctx->stream>>>(ctx->ds, bi.dsys, TN, tl);
+  CK(cudaMemsetAsync(logdiag, 0, (size_t)nsys * K * sizeof(double), ctx->stream));
+  CK(cudaMemsetAsync(fail, 0, nsys * sizeof(int), ctx->stream));
+  if ((rc = cholqr_b(ctx, bi, T, tl, K, G, Rinv, logdiag, fail, false))) return rc;
+  for (int64_t done = 0; done < n_coll;) {
+    const int64_t want = n_coll - done < chunk ? n_coll - done : chunk;
+    if ((rc = advance_logged_all(ctx, want))) return rc;
+    k_tangent_apply_b<<<nsys, 32, 0, ctx->stream>>>(ctx->ds, bi.doff, T, tl, K);
+    CK(cudaGetLastError());
+    if (qr_every > 0 && (rc = cholqr_b(ctx, bi, T, tl, K, G, Rinv, logdiag, fail, true))) return rc;
+    done += want;
+  }
+  if (lyap_out) {
+    std::vector<double> ld((size_t)nsys * K);
+    CK(sync_copy(ctx, ld.data(), logdiag, ld.size() * 8, cudaMemcpyDeviceToHost));
+    if ((rc = sys_times(ctx, t1.data()))) return rc;
+    for (int s = 0; s < nsys; s++)
+      for (int k = 0; k < K; k++)
+        lyap_out[(size_t)s * K + k] = (t1[s] > t0[s]) ? ld[(size_t)s * K + k] / (t1[s] - t0[s]) : 0.0;
+  }
+  CK(call_end(ctx));
+  return EDMD_OK;
+}
+
+extern "C" int edmd_msd_gradient_batch(edmd_ctx* ctx, int64_t n_coll, int64_t ckpt_every, double* msd_out,
+                                       double* g_vx, double* g_vy, double* g_x, double* g_y) {
+  if (!ctx || n_coll < 1 || ckpt_every < 1) return EDMD_ERR_ARG;
+  if (ctx->engine != EDMD_ENGINE_WARP) return set_err(ctx, EDMD_ERR_ARG, "adjoints need the warp engine");
+  const int64_t TN = ctx->total_N;
+  const int nsys = ctx->nsys;
+  int rc = edmd_set_log_capacity(ctx, ckpt_every + 16);
+  if (rc) return rc;
+  BatchIndex bi;
+  if ((rc = batch_index(ctx, bi))) return rc;
+  double *A = nullptr, *ta = nullptr, *x0 = nullptr, *y0 = nullptr, *x1 = nullptr, *y1 = nullptr;
+  double *dux = nullptr, *duy = nullptr, *t0 = nullptr, *msd = nullptr;
+  CK(dalloc(&A, 4 * (size_t)TN));
+  CK(dalloc(&ta, TN)); CK(dalloc(&x0, TN)); CK(dalloc(&y0, TN)); CK(dalloc(&x1, TN)); CK(dalloc(&y1, TN));
+  CK(dalloc(&dux, TN)); CK(dalloc(&duy, TN)); CK(dalloc(&t0, nsys)); CK(dalloc(&msd, nsys));
+  struct Free { void* p[10]; ~Free() { for (void* q : p) if (q) cudaFree(q); } }
+      guard{{A, ta, x0, y0, x1, y1, dux, duy, t0, msd}};
+  CK(call_begin(ctx));
+  const unsigned gT = (unsigned)((TN + 127) / 128);
+  k_sys_times<<<(nsys + 127) / 128, 128, 0, ctx->stream>>>(ctx->ds, nsys, t0);
+  k_positions_now_b<<<gT, 128, 0, ctx->stream>>>(ctx->ds, bi.doff, bi.dsys, TN, x0, y0);
+  CK(cudaGetLastError());
+  // forward sweep: exact engine checkpoints at every segment boundary
+  const int64_t nseg = (n_coll + ckpt_every - 1) / ckpt_every;
+  std::vector<int64_t> seglen(nseg);
+  for (int64_t g = 0; g < nseg; g++) {
+    if ((rc = edmd_checkpoint_save(ctx, (int32_t)g))) return rc;
+    seglen[g] = (g == nseg - 1) ? n_coll - g * ckpt_every : ckpt_every;
+    rc = edmd_advance(ctx, seglen[g], INFINITY, EDMD_F_COUNT_NORMAL, (int64_t)1 << 60, nullptr);
+    if (rc) return rc;
+  }
+  if ((rc = edmd_checkpoint_save(ctx, (int32_t)nseg))) return rc;
+  k_positions_now_b<<<gT, 128, 0, ctx->stream>>>(ctx->ds, bi.doff, bi.dsys, TN, x1, y1);
+  k_msd_b<<<nsys, 256, 0, ctx->stream>>>(ctx->ds, bi.doff, x0, y0, x1, y1, A, ta, dux, duy, msd);
+  CK(cudaGetLastError());
+  // reverse sweep: recompute each segment from its checkpoint, then its adjoint
+  for (int64_t g = nseg - 1; g >= 0; g--) {
+    if ((rc = edmd_checkpoint_restore(ctx, (int32_t)g))) return rc;
+    if ((rc = advance_logged_all(ctx, seglen[g]))) return rc;
+    k_adjoint_segment_b<<<(nsys + 63) / 64, 64, 0, ctx->stream>>>(ctx->ds, bi.doff, nsys, A, ta);
+    CK(cudaGetLastError());
+  }
+  k_adjoint_finish_b<<<gT, 128, 0, ctx->stream>>>(bi.dsys, TN, A, ta, t0);
+  CK(cudaGetLastError());
+  // leave the engine at the end of the run
+  if ((rc = edmd_checkpoint_restore(ctx, (int32_t)nseg))) return rc;
+  std::vector<double> hA(4 * (size_t)TN), hx(TN), hy(TN);
+  CK(sync_copy(ctx, hA.data(), A, hA.size() * 8, cudaMemcpyDeviceToHost));
+  CK(sync_copy(ctx, hx.data(), dux, TN * 8, cudaMemcpyDeviceToHost));
+  CK(sync_copy(ctx, hy.data(), duy, TN * 8, cudaMemcpyDeviceToHost));
+  if (msd_out) CK(sync_copy(ctx, msd_out, msd, nsys * 8, cudaMemcpyDeviceToHost));
+  // u = r(t) - r(0) also depends on the initial positions directly
+  for (int64_t g = 0; g < TN; g++) {
+    if (g_x) g_x[g] = hA[4 * g + 0] - hx[g];
+    if (g_y) g_y[g] = hA[4 * g + 1] - hy[g];
+    if (g_vx) g_vx[g] = hA[4 * g + 2];
+    if (g_vy) g_vy[g] = hA[4 * g + 3];
+  }
   CK(call_end(ctx));
   return EDMD_OK;
 }

@@ -61,7 +61,8 @@ EXPORTS = [
     "edmd_set_warp_group",
     "edmd_get_engine", "edmd_get_last_ms", "edmd_set_device", "edmd_host_alloc", "edmd_host_free", "edmd_run_noalloc",
     "edmd_set_log_capacity", "edmd_clear_log", "edmd_get_log", "edmd_checkpoint_save",
-    "edmd_checkpoint_restore", "edmd_tangent_run", "edmd_msd_gradient", "edmd_destroy",
+    "edmd_checkpoint_restore", "edmd_tangent_run", "edmd_msd_gradient", "edmd_tangent_run_batch",
+    "edmd_msd_gradient_batch", "edmd_destroy",
     "edmd_last_error", "edmd_device_info",
     "edmd_mt_seed", "edmd_mt_u32", "edmd_mt_double", "edmd_hex_size", "edmd_random_size",
     "edmd_grow_rate", "edmd_normalize", "edmd_init_hex", "edmd_init_grow", "edmd_default_desc",
@@ -105,6 +106,8 @@ def load(path=LIB_PATH):
     L.edmd_tangent_run.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int64, C.c_int64, C.c_uint64,
                                    C.c_void_p, C.c_void_p]
     L.edmd_msd_gradient.argtypes = [C.c_void_p, C.c_int32, C.c_int64, C.c_int64, C.c_double] + [C.c_void_p] * 5
+    L.edmd_tangent_run_batch.argtypes = [C.c_void_p, C.c_int32, C.c_int64, C.c_int64, C.c_uint64, C.c_void_p]
+    L.edmd_msd_gradient_batch.argtypes = [C.c_void_p, C.c_int64, C.c_int64] + [C.c_void_p] * 5
     L.edmd_run_noalloc.argtypes = [C.POINTER(SystemDesc)] + [C.c_void_p] * 6 + [
         C.c_int64, C.c_double, C.POINTER(C.c_int64), C.POINTER(C.c_double), C.c_void_p]
     L.edmd_set_lane_threads.argtypes = [C.c_int32]
@@ -340,6 +343,21 @@ class Engine:
         self._ck(self._L.edmd_msd_gradient(self.h, s, int(n_coll), int(ckpt_every), float(t_obs), C.byref(msd),
                                            _ptr(g["vx"]), _ptr(g["vy"]), _ptr(g["x"]), _ptr(g["y"])))
         return msd.value, g
+
+    def tangent_batch(self, K, n_coll, qr_every, seed=1):
+        """Lyapunov exponents of every system ([nsys][K]), system s seeded with seed + s."""
+        lyap = np.zeros(self.n * K)
+        self._ck(self._L.edmd_tangent_run_batch(self.h, K, int(n_coll), int(qr_every), int(seed), _ptr(lyap)))
+        return lyap.reshape(self.n, K)
+
+    def msd_gradient_batch(self, n_coll, ckpt_every=500):
+        """Final MSD of every system and its gradients (concatenated over systems)."""
+        T = sum(self.N)
+        g = {k: np.zeros(T) for k in ("vx", "vy", "x", "y")}
+        msd = np.zeros(self.n)
+        self._ck(self._L.edmd_msd_gradient_batch(self.h, int(n_coll), int(ckpt_every), _ptr(msd), _ptr(g["vx"]),
+                                                 _ptr(g["vy"]), _ptr(g["x"]), _ptr(g["y"])))
+        return msd, g
 
     def counters(self, s=0):
         c = Counters()

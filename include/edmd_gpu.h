@@ -222,7 +222,7 @@ int edmd_set_lane_threads(int32_t threads_per_block);
 int edmd_set_warp_group(int32_t lanes);
 int edmd_get_engine(const edmd_ctx* ctx);
 /* Device time, in ms, of the last edmd_advance, edmd_advance_rounds,
- * edmd_tangent_run or edmd_msd_gradient call on ctx: CUDA events recorded on
+ * edmd_tangent_run(_batch) or edmd_msd_gradient(_batch) call on ctx: CUDA events recorded on
  * the context's stream at the call's start and end (for the host-driven
  * differentiation calls this includes the stream's idle gaps between their
  * kernels).  No reference counterpart (the reference reports no timings). */
@@ -269,6 +269,25 @@ int edmd_tangent_run(edmd_ctx* ctx, int32_t sys, int32_t K, int64_t n_coll, int6
  * of the run.  Single-system contexts; warp engine. */
 int edmd_msd_gradient(edmd_ctx* ctx, int32_t sys, int64_t n_coll, int64_t ckpt_every, double t_obs,
                       double* msd_out, double* g_vx, double* g_vy, double* g_x, double* g_y);
+
+/* Batched tangent-linear run: every system of the context at once, in one
+ * persistent advance per chunk and one tangent launch per chunk for all
+ * systems.  System s propagates K <= 32 random vectors drawn from seed + s
+ * (the vectors edmd_tangent_run draws for that seed), re-orthonormalised by
+ * CholQR2 every qr_every of its collisions; lyap_out (nsys*K, may be NULL)
+ * receives each system's exponents.  No reference counterpart (the reference
+ * has no derivatives).  Warp engine. */
+int edmd_tangent_run_batch(edmd_ctx* ctx, int32_t K, int64_t n_coll, int64_t qr_every, uint64_t seed,
+                           double* lyap_out);
+
+/* Batched adjoint of the final mean-square displacement of every system: the
+ * forward sweep with whole-context checkpoints every ckpt_every collisions
+ * and the reverse sweep one thread per system.  The observable of system s is
+ * taken at the time of its last processed event; msd_out (nsys) and the
+ * gradients (total N, concatenated in system order like edmd_get_states) may
+ * be NULL.  No reference counterpart.  Warp engine. */
+int edmd_msd_gradient_batch(edmd_ctx* ctx, int64_t n_coll, int64_t ckpt_every, double* msd_out,
+                            double* g_vx, double* g_vy, double* g_x, double* g_y);
 
 /* Page-locked host buffers for fast host<->device staging. */
 int edmd_host_alloc(void** p, int64_t bytes);

@@ -212,3 +212,148 @@ def test_torch_autograd_wrapper(edmd, oracle, setup):
     assert okp and okm
     fd = (msd_of(setup, sp[:, :2]) - msd_of(setup, sm[:, :2])) / (2 * EPS)
     assert abs(vx.grad[k].item() - fd) <= 1e-6 * abs(fd) + 1e-9
+
+
+def cpu_tangent_spectrum(log, m, T, tl, qr_every):
+    """CPU restatement of the tangent map of the collision log (the same
+    Dellago-Posch-Hoover formulas as the engine: free flight to the contact,
+    then the collision map) with CholQR2 re-orthonormalisation after every
+    qr_every collisions at the time of the last one; T is [N][4][K] at the
+    per-disk times tl.  Returns the accumulated log R_kk."""
+    K = T.shape[2]
+    logdiag = np.zeros(K)
+
+    def qr(tq):
+        nonlocal T
+        Y = T.copy()
+        Y[:, 0] += Y[:, 2] * (tq - tl)[:, None]
+        Y[:, 1] += Y[:, 3] * (tq - tl)[:, None]
+        tl[:] = tq
+        Y = Y.reshape(-1, K)
+        for _ in range(2):
+            R = np.linalg.cholesky(Y.T @ Y).T
+            logdiag[:] += np.log(np.diag(R))
+            Y = Y @ np.linalg.inv(R)
+        T = Y.reshape(-1, 4, K)
+
+    for n, L in enumerate(log):
+        i, j, t = int(L["i"]), int(L["j"]), float(L["t"])
+        dx, dy, dvx, dvy, f = (float(L[k]) for k in ("dx", "dy", "dvx", "dvy", "f"))
+        mi, mj = m[i], m[j]
+        xi = T[i, 0] + T[i, 2] * (t - tl[i]); yi = T[i, 1] + T[i, 3] * (t - tl[i])
+        xj = T[j, 0] + T[j, 2] * (t - tl[j]); yj = T[j, 1] + T[j, 3] * (t - tl[j])
+        vxi, vyi, vxj, vyj = T[i, 2].copy(), T[i, 3].copy(), T[j, 2].copy(), T[j, 3].copy()
+        rv = dx * dvx + dy * dvy
+        drx, dry, ddvx, ddvy = xj - xi, yj - yi, vxj - vxi, vyj - vyi
+        dtc = -(dx * drx + dy * dry) / rv
+        rcx, rcy = drx + dvx * dtc, dry + dvy * dtc
+        df = (f / rv) * (dvx * rcx + dvy * rcy + dx * ddvx + dy * ddvy)
+        wx, wy = df * dx + f * rcx, df * dy + f * rcy
+        T[i, 0] = xi - f * mj * dx * dtc; T[i, 1] = yi - f * mj * dy * dtc
+        T[j, 0] = xj + f * mi * dx * dtc; T[j, 1] = yj + f * mi * dy * dtc
+        T[i, 2] = vxi + mj * wx; T[i, 3] = vyi + mj * wy
+        T[j, 2] = vxj - mi * wx; T[j, 3] = vyj - mi * wy
+        tl[i] = tl[j] = t
+        if (n + 1) % qr_every == 0:
+            qr(t)
+    return logdiag
+
+
+def test_lyapunov_spectrum_pinned_to_cpu_restatement(edmd, oracle, setup):
+    """Config 4's spectrum (32 vectors, CholQR2 every 100 collisions, 10^4
+    collisions) against the CPU restatement of the tangent map applied to the
+    collision log of the same run; the log's collisions are first checked
+    against the oracle's (the reference's) sequence."""
+    N, K, M, Q = setup["N"], 32, 10000, 100
+    eng = engine(edmd, setup)
+    L = edmd.load()
+    L.edmd_set_log_capacity(eng.h, M + 16)
+    L.edmd_clear_log(eng.h)
+    eng.advance(max_coll=M, flags=edmd.F_LOG)
+    log = eng.log(0, cap=M + 16)
+    eng.close()
+    assert len(log) == M
+    o = oracle.Oracle(arrays=setup["init"], Lx=setup["Lx"], Ly=setup["Ly"])
+    tr, n = o.run(M)
+    assert n == M
+    np.testing.assert_array_equal(log["t"], tr["t"])
+    np.testing.assert_array_equal(log["i"], tr["i"])
+    np.testing.assert_array_equal(log["j"], tr["j"])
+    rng = np.random.default_rng(23)
+    V = rng.normal(size=(K, N, 4))
+    eng = engine(edmd, setup)
+    _, lam = eng.tangent(K, M, qr_every=Q, vectors=V)
+    T_end = eng.counters(0)["t"]
+    eng.close()
+    assert T_end == log["t"][-1]
+    ld = cpu_tangent_spectrum(log, setup["init"]["m"], np.ascontiguousarray(V.transpose(1, 2, 0)),
+                              np.zeros(N), Q)
+    lam_cpu = ld / T_end
+    assert np.all(np.abs(lam - lam_cpu) <= 1e-8 * np.abs(lam_cpu).max()), np.abs(lam - lam_cpu).max()
+
+
+def test_duality_over_ten_thousand_collisions(edmd, setup):
+    """Config 4's run length: the adjoint gradient (checkpoints every 500
+    collisions, each segment recomputed) and the tangent map agree on
+    d MSD along a random direction after 10^4 collisions."""
+    N, M = setup["N"], 10000
+    d = np.random.default_rng(29).normal(size=(N, 4))
+    eng = engine(edmd, setup)
+    vec, _ = eng.tangent(1, M, vectors=d[None])
+    T = eng.counters(0)["t"]
+    eng.sync()                                       # positions at T
+    st = eng.state(0)
+    eng.close()
+    eng2 = engine(edmd, setup)
+    msd, g = eng2.msd_gradient(M, ckpt_every=500)
+    assert eng2.counters(0)["t"] == T
+    eng2.close()
+    u = min_image(setup, np.stack([st["x"], st["y"]], 1) -
+                  np.stack([setup["init"]["x"], setup["init"]["y"]], 1))
+    u -= u.mean(0)
+    dmsd_tangent = (2.0 / N) * (u * (vec[0][:, :2] - d[:, :2])).sum()
+    adj = np.stack([g["x"], g["y"], g["vx"], g["vy"]], 1)
+    assert abs((adj * d).sum() - dmsd_tangent) <= 1e-8 * abs(dmsd_tangent)
+
+
+def batch_setups(edmd, oracle, seeds=(11, 12, 13, 14)):
+    """Replicas of config 4 with their own seeds, each 2000 collisions from the lattice."""
+    out = []
+    for sd in seeds:
+        s = edmd.hex_start(1024, 0.60, sd)
+        o = oracle.Oracle(arrays={k: s[k] for k in ("x", "y", "vx", "vy", "rad", "m", "type")},
+                          Lx=s["Lx"], Ly=s["Ly"])
+        o.run(2000, cap=1)
+        o.sync()
+        st = o.state()
+        out.append(dict(desc=edmd.default_desc(s["N"], s["Lx"], s["Ly"]), vr=None,
+                        **{k: st[k].copy() for k in ("x", "y", "vx", "vy", "rad", "m")}))
+    return out
+
+
+def test_batched_tangent_matches_single_systems(edmd, oracle):
+    systems = batch_setups(edmd, oracle)
+    eng = edmd.Engine(systems)
+    lam = eng.tangent_batch(8, 1000, 100, seed=40)
+    eng.close()
+    for s, sysd in enumerate(systems):
+        e1 = edmd.Engine([sysd])
+        _, l1 = e1.tangent(8, 1000, qr_every=100, seed=40 + s)
+        e1.close()
+        np.testing.assert_allclose(lam[s], l1, rtol=1e-9, atol=1e-9 * np.abs(l1).max())
+
+
+def test_batched_adjoint_matches_single_systems(edmd, oracle):
+    systems = batch_setups(edmd, oracle)
+    eng = edmd.Engine(systems)
+    msd, g = eng.msd_gradient_batch(1000, ckpt_every=250)
+    eng.close()
+    off = np.cumsum([0] + [s["desc"].N for s in systems])
+    for s, sysd in enumerate(systems):
+        e1 = edmd.Engine([sysd])
+        m1, g1 = e1.msd_gradient(1000, ckpt_every=250)
+        e1.close()
+        assert abs(msd[s] - m1) <= 1e-12 * m1
+        for k in ("vx", "vy", "x", "y"):
+            a, b = g[k][off[s]:off[s + 1]], g1[k]
+            np.testing.assert_allclose(a, b, rtol=1e-9, atol=1e-9 * np.abs(b).max())
