@@ -227,7 +227,7 @@ __device__ void schedule(const SysDev& S, SysState& R, int e, double T, int32_t 
 // placement of e0 on even lanes and of e1 on odd lanes in shared
 // instructions, then the insertions
 template <int GW>
-__device__ __forceinline__ void schedule2(const SysDev& S, SysState& R, int e0, double T0, int32_t j0, uint32_t ca0,
+__device__ void schedule2(const SysDev& S, SysState& R, int e0, double T0, int32_t j0, uint32_t ca0,
                           int e1, double T1, int32_t j1, uint32_t ca1, const Grp<GW>& G) {
   const int lane = G.lane;
   const int pl = sched_place(S, R, (lane & 1) && e1 >= 0 ? T1 : T0);
@@ -238,7 +238,7 @@ __device__ __forceinline__ void schedule2(const SysDev& S, SysState& R, int e0, 
 
 // removeEventFromQueue (src/EDMD.c:2209) in key form
 template <int GW>
-__device__ __forceinline__ void unqueue(const SysDev& S, SysState& R, int e, const Grp<GW>& G) {
+__device__ void unqueue(const SysDev& S, SysState& R, int e, const Grp<GW>& G) {
   const int lane = G.lane;
   uint32_t st = S.ev[e].st;
   if (st == ST_OVF) {
@@ -314,7 +314,7 @@ __device__ __forceinline__ void best_merge(uint64_t& bk, int& bo, int& bp, uint3
 // t % GW, a lane with two tasks walks both lists at once.  The candidates are
 // then packed over the group in task order and solved GW at a time.
 template <int GW>
-__device__ __forceinline__ void predict2(const SysDev& S, SysState& R, int a0, int a1, Pred& r0, Pred& r1,
+__device__ void predict2(const SysDev& S, SysState& R, int a0, int a1, Pred& r0, Pred& r1,
                          const Grp<GW>& G, WarpSmem* sm, bool* ovl, int* ovl_a, int* ovl_b) {
   const Box& B = S.B;
   const int lane = G.lane;
@@ -609,9 +609,6 @@ __device__ void run_system(const SysDev& S, const RunArgs& A, int64_t max_coll, 
   const int N = B.N;
   SysState R = *S.st;
   if (R.status != EDMD_OK) return;
-  // the out-of-line handlers (wrap, thermo, growth stop) work on this copy,
-  // so that R's address never leaves the event loop and R stays in registers
-  SysState Rw;
   double ctl = R.collT[lane & 3];      // this lane's virial term, see gather_virial
   if (lane == 0) { sm->msum[0] = sm->msum[1] = 0; }   // no mass sum is +0
   G.sync();
@@ -631,11 +628,7 @@ __device__ void run_system(const SysDev& S, const RunArgs& A, int64_t max_coll, 
       if (r.b == BINF || (uint64_t)r.b >= R.next_wrap) {
         if (r.b == BINF && R.ovf == NIL) { status = EDMD_ERR_BUDGET; break; }
         while (R.k < R.next_wrap) { R.P += B.dtP; R.k++; }
-        bool wrap_ok;
-        Rw = R;
-        wrap_ok = do_wrap(S, Rw, G);
-        R = Rw;
-        if (!wrap_ok) { status = EDMD_ERR_BUDGET; break; }
+        if (!do_wrap(S, R, G)) { status = EDMD_ERR_BUDGET; break; }
         R.next_wrap += (uint64_t)N;
         if (++guard > (1 << 20)) { status = EDMD_ERR_BUDGET; break; }
         continue;
@@ -830,16 +823,12 @@ __device__ void run_system(const SysDev& S, const RunArgs& A, int64_t max_coll, 
       if (A.flags & EDMD_F_STOP_AT_SCREEN) { stop = EDMD_STOP_SCREEN; }
     } else if (e == 2 * N + SP_THERMO) {
       gather_virial(R, ctl, G);
-      Rw = R;
-      do_thermo(S, Rw, G);
-      R = Rw;
+      do_thermo(S, R, G);
       ctl = R.collT[lane & 3];
       se0 = e; sT0 = R.t + S.dtimeTh;
       la = N + SP_THERMO;
     } else {
-      Rw = R;
-      do_growstop(S, Rw, G, sm, &ovl, &oa, &ob);
-      R = Rw;
+      do_growstop(S, R, G, sm, &ovl, &oa, &ob);
       if (A.flags & EDMD_F_STOP_AT_GROW) stop = EDMD_STOP_GROW;
     }
     // the tail shared by the handlers: new crossing events of the one or two
