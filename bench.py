@@ -475,12 +475,16 @@ class Stepper:
     def __init__(self, edmd, eng, engine, coll, radius):
         self.edmd, self.eng, self.engine, self.coll, self.radius = edmd, eng, engine, coll, radius
         self.launches = 0
+        self.rounds = 0
+        self.violations = 0
 
     def step(self):
         if self.engine == "round":
-            _, ms, rounds, _ = self.eng.advance_rounds(max_coll=self.coll, radius=self.radius,
-                                                       flags=self.edmd.F_EXACT)
+            _, ms, rounds, viol = self.eng.advance_rounds(max_coll=self.coll, radius=self.radius,
+                                                          flags=self.edmd.F_EXACT)
             self.launches += 6 * rounds + 4
+            self.rounds += rounds
+            self.violations += viol
             return ms
         _, ms = self.eng.advance(max_coll=self.coll, flags=self.edmd.F_COUNT_NORMAL)
         self.launches += 1
@@ -507,7 +511,7 @@ def measure(edmd, a, workload, engine, coll, steps, warmup, rank, world, dist, d
     clk = ClockSampler(dev)
     barrier(dist)
     clk.start()
-    st.launches = 0
+    st.launches = st.rounds = st.violations = 0
     kern_ms = []
     t0 = time.perf_counter()
     for _ in range(steps):
@@ -515,6 +519,7 @@ def measure(edmd, a, workload, engine, coll, steps, warmup, rank, world, dist, d
     wall = time.perf_counter() - t0
     clocks = clk.stop()
     launches = st.launches
+    rounds, violations = st.rounds, st.violations
     c1 = eng.all_counters()
     ncoll = int((c1["ncol"] - c0["ncol"]).sum())
     npair = int((c1["npair"] - c0["npair"]).sum())
@@ -572,6 +577,9 @@ def measure(edmd, a, workload, engine, coll, steps, warmup, rank, world, dist, d
                     fp64_pipe_source="sm__pipe_fp64_cycles_active of the same capture")
     else:
         roof["traffic_source"] = "no ncu capture of this configuration"
+    if engine == "round":
+        roof["rounds_per_step"] = rounds / steps
+        roof["causality_violations_replayed"] = violations
     return dict(value=value, ms_per_step=1000 * t_max / steps, wall=wall, clocks=clocks, launches=launches,
                 systems=len(systems), TN=TN, e2e=e2e, h2d=h2d, d2h=d2h, roofline=roof)
 

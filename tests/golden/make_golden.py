@@ -42,6 +42,16 @@ CASES = {
 # a short run whose dump and thermo files are kept verbatim (format pin)
 FILES_CASE = ("files_hex64", "--hex -N 64 --phi 0.5 -x 0 -v 9 -t 1200 -D 100 -o 50")
 
+# restarts with -l (src/EDMD.c:980-995, 1366-1451): from a .txt state (the
+# final positions of the files case; velocities drawn anew) and from the
+# last frame of the files case's dump (velocities kept); {golden} is this
+# directory.  Their dump and thermo files are kept verbatim too.
+LOAD_TXT = "load64.txt"
+LOAD_CASES = {
+    "load_txt64": "-l {golden}/load64.txt -t 1200 -D 100 -o 50 -v 9",
+    "load_dump64": "-l {golden}/files_hex64.dump -t 1200 -D 100 -o 50 -v 9",
+}
+
 
 def hx(s):
     return float.fromhex(s)
@@ -124,6 +134,22 @@ def main():
     np.savez_compressed(os.path.join(HERE, name + ".npz"), args=np.array(args), N=head["N"],
                         ncol=tfin[1], t_final=tfin[0])
     print(name, "N", head["N"], "collisions", len(c))
+    # the .txt restart state: "N Lx Ly", then "type x y rad m" per disk
+    with open(os.path.join(HERE, LOAD_TXT), "w") as f:
+        f.write("%d %.17g %.17g\n" % (head["N"], head["Lx"], head["Ly"]))
+        for row in state:
+            f.write("1 %.17g %.17g %.17g 1\n" % (row[0], row[1], row[4]))
+    for name, args in LOAD_CASES.items():
+        dump = os.path.join(HERE, name + ".dump")
+        thermo = os.path.join(HERE, name + ".thermo")
+        run_case(exe, args.format(golden=HERE), 10**12, tmp, {"DUMP_OUT": dump, "THERMO_OUT": thermo})
+        head, init, c, vir, tfin, state = parse_trace(tmp)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), args=np.array(args), N=head["N"],
+                            ncol=tfin[1], t_final=tfin[0],
+                            x0=init[:, 0].astype(np.float64), y0=init[:, 1].astype(np.float64),
+                            vx0=init[:, 2].astype(np.float64), vy0=init[:, 3].astype(np.float64),
+                            xf=state[:, 0].astype(np.float64), yf=state[:, 1].astype(np.float64))
+        print(name, "N", head["N"], "collisions", len(c))
     os.remove(tmp)
 
 

@@ -29,3 +29,21 @@ def test_dump_and_thermo_files_identical(built, tmp_path):
     assert os.path.basename(dumps[0]).startswith("N_64res_1.000phi_0.500000q_0.000rat_0.400Lx_")
     assert open(dumps[0]).read() == open(os.path.join(GOLDEN, "files_hex64.dump")).read()
     assert open(thermos[0]).read() == open(os.path.join(GOLDEN, "files_hex64.thermo")).read()
+
+
+@pytest.mark.parametrize("name", ["load_txt64", "load_dump64"])
+def test_restart_files_identical(built, tmp_path, name):
+    """-l restarts (src/EDMD.c:980-995, 1366-1451): from a .txt state, with
+    velocities drawn from the seed, and from the last frame of a dump, with
+    its velocities.  The reference's own run of the same command line wrote
+    the golden dump and thermo files (tests/golden/make_golden.py)."""
+    g = dict(np.load(os.path.join(GOLDEN, name + ".npz")))
+    args = str(g["args"]).format(golden=GOLDEN).split()
+    exe = os.path.join(PKG, "edmd")
+    r = subprocess.run([exe] + args + ["--quiet"], cwd=tmp_path, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 1, r.stderr
+    dumps = glob.glob(str(tmp_path / "dump" / "*.dump"))
+    thermos = glob.glob(str(tmp_path / "dump" / "*.thermo"))
+    assert len(dumps) == 1 and len(thermos) == 1
+    assert open(dumps[0]).read() == open(os.path.join(GOLDEN, name + ".dump")).read()
+    assert open(thermos[0]).read() == open(os.path.join(GOLDEN, name + ".thermo")).read()
