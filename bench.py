@@ -762,8 +762,8 @@ def main():
     ap.add_argument("--seed", type=int, default=20261203)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-secondary", action="store_true")
-    ap.add_argument("--warp-group", type=int, default=32, choices=[16, 32],
-                    help="warp engine lanes per system (16: two systems per warp)")
+    ap.add_argument("--warp-group", type=int, default=32, choices=[4, 8, 16, 32],
+                    help="warp engine lanes per system (16: two systems per warp, 8: four, 4: eight)")
     a = ap.parse_args()
     if a.warmup < 3 and a.impl == "ours":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)

@@ -321,38 +321,47 @@ __device__ void predict2(const SysDev& S, SysState& R, int a0, int a1, Pred& r0,
   const bool grow = R.grow != 0;
   const double dinit = grow ? 10000000 : NEVER;
   const int ntask = a1 >= 0 ? 18 : 9;
-  // the (up to) two tasks of this lane: t0 = lane, t1 = lane + GW
-  const int t0 = lane, t1 = lane + GW;
-  const bool v0 = t0 < ntask, v1 = t1 < ntask;
-  const int o0 = t0 >= 9 ? a1 : a0, o1 = t1 >= 9 ? a1 : a0;
-  const int q0 = t0 >= 9 ? t0 - 9 : t0, q1 = t1 >= 9 ? t1 - 9 : t1;
+  // the tasks of this lane: t = lane + k GW, k < NT (a warp: one task per
+  // lane; 16 lanes: two; 8 lanes: three; 4 lanes: five)
+  constexpr int NT = (18 + GW - 1) / GW;
   auto task_cell = [&](int own, int q) {
     return pbc_cy(B, S.cy[own] + q / 3 - 1) * B.Nxc + pbc_cx(B, S.cx[own] + q % 3 - 1);
   };
-  int p0 = v0 ? S.head[task_cell(o0, q0)] : NIL;
-  int p1 = v1 ? S.head[task_cell(o1, q1)] : NIL;
-  int c0 = 0, c1 = 0;
+  int pt[NT], ct[NT], ot[NT], qt[NT];
+#pragma unroll
+  for (int k = 0; k < NT; k++) {
+    const int t = lane + k * GW;
+    ot[k] = t >= 9 ? a1 : a0;
+    qt[k] = t >= 9 ? t - 9 : t;
+    pt[k] = t < ntask ? S.head[task_cell(ot[k], qt[k])] : NIL;
+    ct[k] = 0;
+  }
   bool lcorrupt = false;
   {
     int guard = 0;                   // the lists hold N disks in all
-    while ((p0 != NIL || p1 != NIL) && guard++ < 2 * B.N) {
-      int n0 = NIL, n1 = NIL;
-      if (p0 != NIL) {
-        if (p0 != o0) { if (c0 < MAXC) sm->reg[t0 * MAXC + c0] = p0; c0++; }
-        n0 = S.d[p0].nxt;
+    bool more = true;
+    while (more && guard++ < 2 * B.N) {
+      more = false;
+#pragma unroll
+      for (int k = 0; k < NT; k++) {
+        if (pt[k] != NIL) {
+          const int t = lane + k * GW;
+          if (pt[k] != ot[k]) { if (ct[k] < MAXC) sm->reg[t * MAXC + ct[k]] = pt[k]; ct[k]++; }
+          pt[k] = S.d[pt[k]].nxt;
+          more |= pt[k] != NIL;
+        }
       }
-      if (p1 != NIL) {
-        if (p1 != o1) { if (c1 < MAXC) sm->reg[t1 * MAXC + c1] = p1; c1++; }
-        n1 = S.d[p1].nxt;
-      }
-      p0 = n0;
-      p1 = n1;
     }
     // a list longer than N is corrupt: reported like an overlap, with the
     // marker OVL_CORRUPT in place of the first disk (EDMD_ERR_BUDGET)
-    if (p0 != NIL || p1 != NIL) { lcorrupt = true; }
+#pragma unroll
+    for (int k = 0; k < NT; k++)
+      if (pt[k] != NIL) lcorrupt = true;
   }
-  const bool spill = G.any(c0 > MAXC || c1 > MAXC);
+  bool over = false;
+#pragma unroll
+  for (int k = 0; k < NT; k++) over |= ct[k] > MAXC;
+  const bool spill = G.any(over);
   Disk A0 = S.d[a0];
   Disk A1 = a1 >= 0 ? S.d[a1] : A0;
   uint64_t bd0 = cand_key(dinit), bd1 = bd0;
@@ -363,24 +372,29 @@ __device__ void predict2(const SysDev& S, SysState& R, int a0, int a1, Pred& r0,
   int tot;
   if (!spill) {
     // exclusive prefix of the counts in task order: tasks 0..GW-1, then GW..
-    int in0 = c0, in1 = c1;
+    int ex[NT];
+    int base = 0;
 #pragma unroll
-    for (int o = 1; o < GW; o <<= 1) {
-      const int u0 = G.shfl_up(in0, o), u1 = G.shfl_up(in1, o);
-      if (lane >= o) { in0 += u0; in1 += u1; }
+    for (int k = 0; k < NT; k++) {
+      int in = ct[k];
+#pragma unroll
+      for (int o = 1; o < GW; o <<= 1) {
+        const int u = G.shfl_up(in, o);
+        if (lane >= o) in += u;
+      }
+      ex[k] = base + in - ct[k];
+      base += G.shfl(in, GW - 1);
     }
-    const int sum0 = G.shfl(in0, GW - 1), sum1 = G.shfl(in1, GW - 1);
-    const int ex0 = in0 - c0, ex1 = sum0 + in1 - c1;
     // a0's candidates are tasks 0..8: their count is the prefix at task 9
-    const int tot0 = G.shfl(ex0, 9);
-    tot = sum0 + sum1;
-    for (int k = 0; k < c0; k++) {
-      sm->comp[ex0 + k] = sm->reg[t0 * MAXC + k];
-      sm->ord[ex0 + k] = (int16_t)(q0 * MAXC + k);
-    }
-    for (int k = 0; k < c1; k++) {
-      sm->comp[ex1 + k] = sm->reg[t1 * MAXC + k];
-      sm->ord[ex1 + k] = (int16_t)(q1 * MAXC + k);
+    const int tot0 = G.shfl(ex[9 / GW], 9 % GW);
+    tot = base;
+#pragma unroll
+    for (int k = 0; k < NT; k++) {
+      const int t = lane + k * GW;
+      for (int m = 0; m < ct[k]; m++) {
+        sm->comp[ex[k] + m] = sm->reg[t * MAXC + m];
+        sm->ord[ex[k] + m] = (int16_t)(qt[k] * MAXC + m);
+      }
     }
     G.sync();
     for (int f = lane; f < tot; f += GW) {
@@ -399,10 +413,11 @@ __device__ void predict2(const SysDev& S, SysState& R, int a0, int a1, Pred& r0,
     // a cell list longer than MAXC: every task walks its own list again,
     // solving as it goes
     tot = 0;
-    for (int w = 0; w < 2; w++) {
-      const int t = w ? t1 : t0;
+#pragma unroll
+    for (int w = 0; w < NT; w++) {
+      const int t = lane + w * GW;
       if (t >= ntask) continue;
-      const int own = w ? o1 : o0, q = w ? q1 : q0;
+      const int own = ot[w], q = qt[w];
       const bool g1 = t >= 9;
       const Disk& AA = g1 ? A1 : A0;
       int p = S.head[task_cell(own, q)];
@@ -1116,7 +1131,7 @@ extern "C" int edmd_set_lane_threads(int32_t threads_per_block) {
 }
 
 extern "C" int edmd_set_warp_group(int32_t lanes) {
-  if (lanes != 16 && lanes != 32) return EDMD_ERR_ARG;
+  if (lanes != 4 && lanes != 8 && lanes != 16 && lanes != 32) return EDMD_ERR_ARG;
   g_group = lanes;
   return EDMD_OK;
 }
@@ -1256,7 +1271,18 @@ extern "C" int edmd_create(int32_t nsys, const edmd_system_desc* desc, const dou
   }
   ctx->total_N = TN; ctx->total_C = TC;
   ctx->engine = g_engine;
-  if (ctx->engine == EDMD_ENGINE_AUTO) ctx->engine = EDMD_ENGINE_WARP;
+  if (ctx->engine == EDMD_ENGINE_AUTO) {
+    // One thread per system issues each FP64 instruction for up to 32
+    // systems, but needs enough systems to hide its dependent loads: measured
+    // on GB300 (Hex starts at phi 0.55, 2000 collisions a call), the lane
+    // engine runs 2.9e7 / 5.2e7 / 9.3e7 / 1.6e8 coll/s at 4096 / 8192 /
+    // 16384 / 32768 systems of 256 disks against 7.5e7 / 7.5e7 / 8.4e7 /
+    // 8.5e7 for one warp per system (16384 systems of 1024 disks: 9.4e7
+    // against 7.6e7).  Its calendar costs ~2 KB per disk.
+    const bool many = nsys >= 16384 && 2 * (int64_t)ctx->maxN + NSPECIAL <= 65535 &&
+                      TN * (int64_t)(CAL_SUB * CAL_LINE * 2 + 2) <= ((int64_t)32 << 30);
+    ctx->engine = many ? EDMD_ENGINE_LANE : EDMD_ENGINE_WARP;
+  }
   if (ctx->engine == EDMD_ENGINE_LANE && 2 * (int64_t)ctx->maxN + NSPECIAL > 65535)
     return set_err(ctx, EDMD_ERR_ARG, "thread-per-system engine supports N <= 32766");
   CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
@@ -1329,9 +1355,11 @@ extern "C" int edmd_advance(edmd_ctx* ctx, int64_t max_coll, double t_stop, uint
     CK(cudaGetDevice(&dev));
     CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
     int per_sm = 0;
-    const int gw = g_group;                     // lanes per system: 16 or 32
+    const int gw = g_group;                     // lanes per system: 4, 8, 16 or 32
     const int per_block = WARPS_PER_BLOCK * (32 / gw);
-    if (gw == 16) CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_run<16>, 32 * WARPS_PER_BLOCK, 0));
+    if (gw == 4) CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_run<4>, 32 * WARPS_PER_BLOCK, 0));
+    else if (gw == 8) CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_run<8>, 32 * WARPS_PER_BLOCK, 0));
+    else if (gw == 16) CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_run<16>, 32 * WARPS_PER_BLOCK, 0));
     else CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_run<32>, 32 * WARPS_PER_BLOCK, 0));
     int want = (ctx->nsys + per_block - 1) / per_block;
     int grid = per_sm * nsm;
@@ -1357,7 +1385,9 @@ extern "C" int edmd_advance(edmd_ctx* ctx, int64_t max_coll, double t_stop, uint
       A.order = ctx->order;
     }
     CK(cudaEventRecord(ctx->e0, ctx->stream));
-    if (gw == 16) k_run<16><<<grid, 32 * WARPS_PER_BLOCK, 0, ctx->stream>>>(ctx->ds, A);
+    if (gw == 4) k_run<4><<<grid, 32 * WARPS_PER_BLOCK, 0, ctx->stream>>>(ctx->ds, A);
+    else if (gw == 8) k_run<8><<<grid, 32 * WARPS_PER_BLOCK, 0, ctx->stream>>>(ctx->ds, A);
+    else if (gw == 16) k_run<16><<<grid, 32 * WARPS_PER_BLOCK, 0, ctx->stream>>>(ctx->ds, A);
     else k_run<32><<<grid, 32 * WARPS_PER_BLOCK, 0, ctx->stream>>>(ctx->ds, A);
   }
   CK(cudaGetLastError());

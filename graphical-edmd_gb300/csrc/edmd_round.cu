@@ -51,7 +51,7 @@ constexpr uint64_t KINF = ~0ull;
 constexpr int32_t IINF = 0x7fffffff;
 constexpr int32_t GMASK = 0xffffff;   // disk index inside an event id (rank in the top byte)
 constexpr unsigned FULLM = 0xffffffffu;
-constexpr int TX = 32, TY = 8;        // selection tile (cells)
+constexpr int TX = 32, TY = 16;       // selection tile (cells): 1.8 halo cells per cell at radius 4
 constexpr int RTILE = 12;             // largest window radius of the tile kernel
 constexpr int MAXDIRTY = 8;           // cells whose minimum one event can change
 constexpr int MAXC = 8;               // candidates buffered per cell list per lane
@@ -337,7 +337,7 @@ __device__ __forceinline__ int wrapi(int v, int n) {
 }
 
 // window minima of one tile in shared memory and selection of its events
-__global__ void __launch_bounds__(256) k_select(const SysDev* __restrict__ sys, RoundArgs A) {
+__global__ void __launch_bounds__(TX * TY) k_select(const SysDev* __restrict__ sys, RoundArgs A) {
   extern __shared__ unsigned char smem[];
   for (int t = blockIdx.x; t < A.ntiles; t += gridDim.x) {
   const int s = A.tsys[t];

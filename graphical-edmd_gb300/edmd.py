@@ -191,10 +191,10 @@ def default_desc(N, Lx, Ly, vr_base=0.0, tmax=4000.0, dtime=100.0, dtime_thermo=
 
 
 def set_warp_group(lanes):
-    """Lanes per system of the warp engine, 16 or 32 (edmd_set_warp_group)."""
+    """Lanes per system of the warp engine, 4, 8, 16 or 32 (edmd_set_warp_group)."""
     rc = load().edmd_set_warp_group(int(lanes))
     if rc != 0:
-        raise ValueError("lanes must be 16 or 32")
+        raise ValueError("lanes must be 4, 8, 16 or 32")
 
 
 # ------------------------------------------------------------------ engine

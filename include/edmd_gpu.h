@@ -46,7 +46,10 @@ extern "C" {
 #define EDMD_STOP_GROW      5   /* stopped right after the growth stop        */
 
 /* engines (edmd_set_engine) */
-#define EDMD_ENGINE_AUTO    0   /* the warp engine (fastest measured)         */
+#define EDMD_ENGINE_AUTO    0   /* the thread-per-system engine for contexts of at
+                                   least 16384 systems of N <= 32766 (faster there),
+                                   else the warp engine; the differentiation calls
+                                   need EDMD_ENGINE_WARP */
 #define EDMD_ENGINE_WARP    1   /* one warp per system: single large systems  */
 #define EDMD_ENGINE_LANE    2   /* one thread per system: large batches, N <= 32766 */
 
@@ -217,8 +220,8 @@ int edmd_set_engine(int32_t kind);
 int edmd_set_lane_threads(int32_t threads_per_block);
 
 /* Lanes per system of the warp engine: 32 (one system per warp, the
- * default) or 16 (two systems per warp).  Both give identical results; on the
- * 4096-system batch 32 lanes run 6.2e7 coll/s and 16 lanes 5.9e7. */
+ * default), 16, 8 or 4 (two, four or eight systems per warp, each group of
+ * lanes running its own system).  All give identical results. */
 int edmd_set_warp_group(int32_t lanes);
 int edmd_get_engine(const edmd_ctx* ctx);
 /* Device time, in ms, of the last edmd_advance, edmd_advance_rounds,

@@ -58,7 +58,9 @@ def golden(name):
 
 
 def golden_names():
-    return sorted(f[:-4] for f in os.listdir(GOLDEN) if f.endswith(".npz") and not f.startswith("files_"))
+    """Trace fixtures (the files_* and load_* fixtures pin output files instead)."""
+    return sorted(f[:-4] for f in os.listdir(GOLDEN)
+                  if f.endswith(".npz") and not f.startswith(("files_", "load_")))
 
 
 def parse_args(args):

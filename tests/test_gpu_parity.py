@@ -106,10 +106,11 @@ def test_batch_larger_than_resident_warps(edmd, oracle):
     eng.close()
 
 
-@pytest.mark.parametrize("lanes", [32, 16])
+@pytest.mark.parametrize("lanes", [32, 16, 8, 4])
 def test_warp_group_widths_match_reference(edmd, lanes):
-    """One system per warp (32 lanes) and two per warp (16 lanes each): the
-    same collisions, cells, times and states as the reference."""
+    """One system per warp (32 lanes) and two, four or eight per warp (16, 8
+    or 4 lanes each): the same collisions, cells, times and states as the
+    reference."""
     try:
         edmd.set_warp_group(lanes)
         names = golden_names()
