@@ -91,6 +91,19 @@ def usable_cores():
         return os.cpu_count() or 1
 
 
+def _load_pkg(name):
+    """A module of the engine package (graphical-edmd_gb300/<name>.py)."""
+    import importlib.util
+    key = "edmd_gb300_" + name
+    if key in sys.modules:
+        return sys.modules[key]
+    spec = importlib.util.spec_from_file_location(key, os.path.join(ROOT, "graphical-edmd_gb300", name + ".py"))
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules[key] = mod
+    spec.loader.exec_module(mod)
+    return mod
+
+
 def _load_edmd():
     """The engine's Python binding; EDMD_BENCH_ENGINE_MODULE names a stand-in
     module with the same interface (used by the CPU test of the multi-rank
@@ -477,6 +490,7 @@ class Stepper:
         self.launches = 0
         self.rounds = 0
         self.violations = 0
+        self.extra_flags = 0
 
     def step(self):
         if self.engine == "round":
@@ -486,7 +500,7 @@ class Stepper:
             self.rounds += rounds
             self.violations += viol
             return ms
-        _, ms = self.eng.advance(max_coll=self.coll, flags=self.edmd.F_COUNT_NORMAL)
+        _, ms = self.eng.advance(max_coll=self.coll, flags=self.edmd.F_COUNT_NORMAL | self.extra_flags)
         self.launches += 1
         return ms
 
@@ -504,7 +518,26 @@ def measure(edmd, a, workload, engine, coll, steps, warmup, rank, world, dist, d
         assert not c["growing"].any(), "growth did not finish"
     elif workload in SINGLE:
         eng.advance_rounds(max_coll=LARGE_EQUIL, radius=a.radius, flags=edmd.F_EXACT)
+    tuned = None
+    extra = edmd.F_SMEM if (getattr(a, "smem", False) and engine == "warp") else 0
+    if workload == "batched" and engine == "warp" and getattr(a, "tune", False):
+        # untimed: every candidate engine and launch shape on the grown
+        # systems themselves (all give the same trajectories); the timed
+        # steps run the fastest
+        tune = _load_pkg("tune")
+        eng.sync()
+        descs = [edmd.default_desc(s["desc"].N, s["desc"].Lx, s["desc"].Ly, 0.0, 1e30) for s in systems]
+        grown = tune.systems_from_states(descs, eng.states(), [s["desc"].N for s in systems])
+        tuned = tune.tune(edmd, grown, coll=2000)
+        if (tuned["engine"], tuned["lanes"]) != ("warp", a.warp_group):
+            eng.close()
+            if tuned["lanes"] is not None:
+                edmd.set_warp_group(tuned["lanes"])
+            eng = edmd.Engine(grown, engine=edmd.ENGINE_LANE if tuned["engine"] == "lane" else edmd.ENGINE_WARP)
+            engine = tuned["engine"]
+        extra = tuned["flags"]
     st = Stepper(edmd, eng, engine, coll, a.radius)
+    st.extra_flags = extra
     for _ in range(warmup):
         st.step()
     c0 = eng.all_counters()
@@ -561,7 +594,8 @@ def measure(edmd, a, workload, engine, coll, steps, warmup, rank, world, dist, d
     achieved = Bcoll * ncoll / t_dev / 1e9
     peaks = json.load(open(PEAKS)) if os.path.exists(PEAKS) else {}
     peak = peaks.get("hbm_gbs", 6800.0)
-    prof = PROFILED.get((workload, engine, a.warp_group)) if a.nsys is None else None
+    lanes_used = (tuned["lanes"] if tuned else a.warp_group) if engine == "warp" else None
+    prof = PROFILED.get((workload, engine, lanes_used)) if (a.nsys is None and not extra) else None
     kernel = ("k_run (one persistent launch per step)" if engine == "warp" else
               "k_lane_run" if engine == "lane" else
               "round engine graph: k_select + k_process + k_recompute + k_barrier per round")
@@ -581,6 +615,8 @@ def measure(edmd, a, workload, engine, coll, steps, warmup, rank, world, dist, d
         roof["rounds_per_step"] = rounds / steps
         roof["causality_violations_replayed"] = violations
     return dict(value=value, ms_per_step=1000 * t_max / steps, wall=wall, clocks=clocks, launches=launches,
+                engine=engine, lanes=(tuned["lanes"] if tuned else a.warp_group) if engine == "warp" else None,
+                smem=bool(extra), tuned=tuned,
                 systems=len(systems), TN=TN, e2e=e2e, h2d=h2d, d2h=d2h, roofline=roof)
 
 
@@ -725,11 +761,12 @@ def run_ours(a, rank, world, dist):
         "metric": METRICS[workload], "value": r["value"], "unit": UNIT, "n_gpus": world,
         "steps": a.steps, "warmup": a.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": workload_desc, "engine": engine, "systems_per_gpu": r["systems"],
+        "config": {"workload": workload_desc, "engine": r["engine"], "systems_per_gpu": r["systems"],
                    "disks_per_gpu": r["TN"], "collisions_per_system_per_step": coll,
                    "l2": "state (~%.0f MB/GPU) larger than L2, no flush" % (r["TN"] * 160 / 1e6),
                    "parallelism": f"replicas x{world}",
-                   "lanes_per_system": a.warp_group if engine == "warp" else None},
+                   "lanes_per_system": r["lanes"], "shared_memory_kernel": r["smem"],
+                   "tuned": r["tuned"]},
         "e2e": {"value": r["e2e"], "unit": UNIT, "h2d_bytes_per_step": r["h2d"], "d2h_bytes_per_step": r["d2h"],
                 "path": "edmd_load_state (pinned host) + advance + edmd_sync + edmd_get_states (pinned host)"},
         "roofline": r["roofline"],
@@ -760,6 +797,10 @@ def main():
     ap.add_argument("--fd-components", type=int, default=2 * DIFF_N,
                     help="velocity components timed for the finite-difference gradient")
     ap.add_argument("--seed", type=int, default=20261203)
+    ap.add_argument("--smem", action="store_true",
+                    help="warp engine: systems that fit a block's shared memory run from there (EDMD_F_SMEM)")
+    ap.add_argument("--no-tune", dest="tune", action="store_false",
+                    help="batched workload: skip the untimed choice of engine and launch shape")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-secondary", action="store_true")
     ap.add_argument("--warp-group", type=int, default=32, choices=[4, 8, 16, 32],

@@ -913,6 +913,105 @@ k_run(const SysDev* __restrict__ sys, RunArgs A) {
   }
 }
 
+// ---------------------------------------------------------------- shared-memory kernel
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ void record_cost(const RunArgs& A, int s, unsigned long long t0) {
+  const unsigned long long c = (global_ns() - t0) >> 10;
+  A.cost[s] = c > 0xffffffffull ? 0xffffffffu : (uint32_t)c;
+}
+
+// where one system's engine state sits in a block's dynamic shared memory:
+// disk records, event slots, tree, cell coordinates and links, cell heads and
+// overflow links; the scalar state, growth rates, trace, log and thermo rows
+// stay in global memory
+struct SmemLayout {
+  size_t d, ev, tree, cx, cy, prv, crossX, crossY, head, on, op, total;
+};
+
+__host__ __device__ inline SmemLayout smem_layout(const SysDev& S) {
+  const size_t N = (size_t)S.B.N, E = 2 * N + NSPECIAL, C = (size_t)S.B.Nxc * S.B.Nyc;
+  size_t nodes = 0;
+  for (int h = 0; h < S.nlev; h++) nodes += (size_t)S.lev_cnt[h];
+  SmemLayout L;
+  size_t o = 0;
+  auto take = [&](size_t bytes) { const size_t r = o; o += (bytes + 63) & ~(size_t)63; return r; };
+  L.d = take(N * sizeof(Disk));
+  L.ev = take(E * sizeof(Ev));
+  L.tree = take(nodes * sizeof(Node));
+  L.cx = take(N * 4); L.cy = take(N * 4); L.prv = take(N * 4);
+  L.crossX = take(N * 4); L.crossY = take(N * 4);
+  L.head = take(C * 4);
+  L.on = take(E * 4); L.op = take(E * 4);
+  L.total = o;
+  return L;
+}
+
+// words of one array between global and shared memory, over the warp
+__device__ __forceinline__ void warp_copy(void* dst, const void* src, size_t bytes, int lane) {
+  uint32_t* d = (uint32_t*)dst;
+  const uint32_t* s = (const uint32_t*)src;
+  for (size_t k = lane; k < bytes / 4; k += 32) d[k] = s[k];
+}
+
+// One warp per block: each system of `list` is copied into the block's
+// shared memory, run by the same event loop as k_run through a descriptor
+// whose arrays point there (every access in it is a generic-address access),
+// and copied back.  Dependent accesses then cost shared-memory latency
+// instead of L2/HBM latency, at the price of one resident system per ~100 KB.
+__global__ void __launch_bounds__(32) k_run_smem(const SysDev* __restrict__ sys, RunArgs A,
+                                                 const int32_t* __restrict__ list, int nlist,
+                                                 int32_t* __restrict__ work) {
+  extern __shared__ __align__(128) unsigned char dyn[];
+  __shared__ WarpSmem wsm;
+  const Grp<32> G(threadIdx.x);
+  const int lane = G.lane;
+  for (;;) {
+    int it = 0;
+    if (lane == 0) it = atomicAdd(work, 1);
+    it = G.shfl(it, 0);
+    if (it >= nlist) break;
+    const int s = list[it];
+    const unsigned long long t0 = A.cost ? global_ns() : 0;
+    const SysDev& S = sys[s];
+    const SmemLayout Y = smem_layout(S);
+    const size_t N = (size_t)S.B.N, E = 2 * N + NSPECIAL, C = (size_t)S.B.Nxc * S.B.Nyc;
+    size_t nodes = 0;
+    for (int h = 0; h < S.nlev; h++) nodes += (size_t)S.lev_cnt[h];
+    SysDev L = S;
+    L.d = (Disk*)(dyn + Y.d); L.ev = (Ev*)(dyn + Y.ev); L.tree = (Node*)(dyn + Y.tree);
+    L.cx = (int32_t*)(dyn + Y.cx); L.cy = (int32_t*)(dyn + Y.cy); L.prv = (int32_t*)(dyn + Y.prv);
+    L.crossX = (int32_t*)(dyn + Y.crossX); L.crossY = (int32_t*)(dyn + Y.crossY);
+    L.head = (int32_t*)(dyn + Y.head); L.on = (int32_t*)(dyn + Y.on); L.op = (int32_t*)(dyn + Y.op);
+    warp_copy(L.d, S.d, N * sizeof(Disk), lane);
+    warp_copy(L.ev, S.ev, E * sizeof(Ev), lane);
+    warp_copy(L.tree, S.tree, nodes * sizeof(Node), lane);
+    warp_copy(L.cx, S.cx, N * 4, lane); warp_copy(L.cy, S.cy, N * 4, lane);
+    warp_copy(L.prv, S.prv, N * 4, lane);
+    warp_copy(L.crossX, S.crossX, N * 4, lane); warp_copy(L.crossY, S.crossY, N * 4, lane);
+    warp_copy(L.head, S.head, C * 4, lane);
+    warp_copy(L.on, S.on, E * 4, lane); warp_copy(L.op, S.op, E * 4, lane);
+    G.sync();
+    run_system(L, A, A.max_coll, G, &wsm);
+    G.sync();
+    warp_copy(S.d, L.d, N * sizeof(Disk), lane);
+    warp_copy(S.ev, L.ev, E * sizeof(Ev), lane);
+    warp_copy(S.tree, L.tree, nodes * sizeof(Node), lane);
+    warp_copy(S.cx, L.cx, N * 4, lane); warp_copy(S.cy, L.cy, N * 4, lane);
+    warp_copy(S.prv, L.prv, N * 4, lane);
+    warp_copy(S.crossX, L.crossX, N * 4, lane); warp_copy(S.crossY, L.crossY, N * 4, lane);
+    warp_copy(S.head, L.head, C * 4, lane);
+    warp_copy(S.on, L.on, E * 4, lane); warp_copy(S.op, L.op, E * 4, lane);
+    G.sync();
+    if (A.cost && lane == 0) record_cost(A, s, t0);
+  }
+}
+
 // ---------------------------------------------------------------- init kernels
 
 // initial predictions of eventListInit (src/EDMD.c:2007-2012): all disks are
@@ -1336,6 +1435,70 @@ extern "C" int edmd_load_state(edmd_ctx* ctx, const double* x, const double* y, 
   return stage_all(ctx, x, y, vx, vy, rad, m, nullptr, true);
 }
 
+// EDMD_F_SMEM: the systems whose engine state fits one block's shared memory
+// go to k_run_smem on a second stream, the others to k_run on the context's
+// stream (longest first by the previous call's run times, as without the
+// flag); both start after e0 and the context's stream waits for the second
+// one before e1.
+static int advance_smem_split(edmd_ctx* ctx, RunArgs A, int kgrid_max, int nsm) {
+  int dev = 0, optin = 0;
+  CK(cudaGetDevice(&dev));
+  CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  const size_t limit = (size_t)optin - sizeof(WarpSmem) - 1024;
+  std::vector<uint32_t> cost(ctx->nsys);
+  CK(sync_copy(ctx, cost.data(), ctx->cost, ctx->nsys * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+  std::vector<int32_t> fit, rest;
+  size_t need = 0;
+  for (int s = 0; s < ctx->nsys; s++) {
+    const size_t b = smem_layout(ctx->hs[s]).total;
+    if (b <= limit) { fit.push_back(s); need = b > need ? b : need; }
+    else rest.push_back(s);
+  }
+  auto longest_first = [&](std::vector<int32_t>& v) {
+    std::stable_sort(v.begin(), v.end(), [&](int32_t a, int32_t b) { return cost[a] > cost[b]; });
+  };
+  longest_first(fit);
+  longest_first(rest);
+  if (!ctx->smem_list) {
+    CK(dalloc(&ctx->smem_list, ctx->nsys));
+    CK(dalloc(&ctx->smem_work, 1));
+    CK(cudaStreamCreateWithFlags(&ctx->stream2, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&ctx->e2, cudaEventDisableTiming));
+  }
+  if (!rest.empty())
+    CK(cudaMemcpyAsync(ctx->order, rest.data(), rest.size() * sizeof(int32_t), cudaMemcpyHostToDevice,
+                       ctx->stream));
+  if (!fit.empty())
+    CK(cudaMemcpyAsync(ctx->smem_list, fit.data(), fit.size() * sizeof(int32_t), cudaMemcpyHostToDevice,
+                       ctx->stream));
+  CK(cudaMemsetAsync(ctx->smem_work, 0, sizeof(int32_t), ctx->stream));
+  CK(cudaEventRecord(ctx->e0, ctx->stream));
+  if (!fit.empty()) {
+    CK(cudaFuncSetAttribute(k_run_smem, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need));
+    int per = 0;
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_run_smem, 32, need));
+    int g = per * nsm;
+    if (g > (int)fit.size()) g = (int)fit.size();
+    if (g < 1) g = 1;
+    CK(cudaStreamWaitEvent(ctx->stream2, ctx->e0, 0));
+    k_run_smem<<<g, 32, need, ctx->stream2>>>(ctx->ds, A, ctx->smem_list, (int)fit.size(), ctx->smem_work);
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(ctx->e2, ctx->stream2));
+  }
+  if (!rest.empty()) {
+    RunArgs B = A;
+    B.nsys = (int32_t)rest.size();
+    B.order = ctx->order;
+    const int per_block = WARPS_PER_BLOCK;
+    int grid = ((int)rest.size() + per_block - 1) / per_block;
+    if (grid > kgrid_max) grid = kgrid_max;
+    k_run<32><<<grid, 32 * WARPS_PER_BLOCK, 0, ctx->stream>>>(ctx->ds, B);
+    CK(cudaGetLastError());
+  }
+  if (!fit.empty()) CK(cudaStreamWaitEvent(ctx->stream, ctx->e2, 0));
+  return EDMD_OK;
+}
+
 extern "C" int edmd_advance(edmd_ctx* ctx, int64_t max_coll, double t_stop, uint32_t flags,
                             int64_t max_events, float* elapsed_ms) {
   if (!ctx) return EDMD_ERR_ARG;
@@ -1384,11 +1547,16 @@ extern "C" int edmd_advance(edmd_ctx* ctx, int64_t max_coll, double t_stop, uint
                          ctx->stream));
       A.order = ctx->order;
     }
+    if ((flags & EDMD_F_SMEM) && gw == 32) {
+      int rc = advance_smem_split(ctx, A, per_sm * nsm, nsm);
+      if (rc) return rc;
+    } else {
     CK(cudaEventRecord(ctx->e0, ctx->stream));
     if (gw == 4) k_run<4><<<grid, 32 * WARPS_PER_BLOCK, 0, ctx->stream>>>(ctx->ds, A);
     else if (gw == 8) k_run<8><<<grid, 32 * WARPS_PER_BLOCK, 0, ctx->stream>>>(ctx->ds, A);
     else if (gw == 16) k_run<16><<<grid, 32 * WARPS_PER_BLOCK, 0, ctx->stream>>>(ctx->ds, A);
     else k_run<32><<<grid, 32 * WARPS_PER_BLOCK, 0, ctx->stream>>>(ctx->ds, A);
+    }
   }
   CK(cudaGetLastError());
   CK(cudaEventRecord(ctx->e1, ctx->stream));
@@ -1528,6 +1696,10 @@ extern "C" int edmd_destroy(edmd_ctx* ctx) {
   if (ctx->e0) cudaEventDestroy(ctx->e0);
   if (ctx->e1) cudaEventDestroy(ctx->e1);
   if (ctx->c0) cudaEventDestroy(ctx->c0);
+  if (ctx->e2) cudaEventDestroy(ctx->e2);
+  if (ctx->stream2) cudaStreamDestroy(ctx->stream2);
+  if (ctx->smem_list) cudaFree(ctx->smem_list);
+  if (ctx->smem_work) cudaFree(ctx->smem_work);
   if (ctx->c1) cudaEventDestroy(ctx->c1);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;

@@ -23,6 +23,7 @@ OK, ERR_ARG, ERR_CUDA, ERR_OVERLAP, ERR_BUDGET, ERR_CAPACITY, ERR_NODEV = range(
 STOP_COLL, STOP_TIME, STOP_TMAX, STOP_SCREEN, STOP_GROW = 1, 2, 3, 4, 5
 F_STOP_AT_SCREEN, F_STOP_AT_GROW, F_TRACE, F_COUNT_NORMAL, F_LOG, F_EXACT = 1, 2, 4, 8, 16, 32
 F_ROUND_GRID, F_ROUND_BLOCK, F_SCREEN, F_ROUND_THREAD, F_ROUND_WARP = 64, 128, 256, 512, 1024
+F_SMEM = 2048
 ENGINE_AUTO, ENGINE_WARP, ENGINE_LANE = 0, 1, 2
 
 

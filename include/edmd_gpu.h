@@ -65,6 +65,9 @@ extern "C" {
 #define EDMD_F_SCREEN        256u  /* edmd_advance_rounds: FP32 screen of separating pairs before FP64 */
 #define EDMD_F_ROUND_THREAD  512u  /* edmd_advance_rounds: one thread per selected event in every round */
 #define EDMD_F_ROUND_WARP   1024u  /* edmd_advance_rounds: one warp per selected event in every round */
+#define EDMD_F_SMEM         2048u  /* edmd_advance, warp engine with 32 lanes: systems whose engine state
+                                      fits one block's shared memory run from shared memory, in a kernel
+                                      of their own beside the others (same results) */
 
 /*
  * One periodic 2D system.  Replaces the globals that constantInit

@@ -105,7 +105,7 @@ def test_bench_launches_two_ranks_itself(tmp_path):
         env.pop(k, None)
     out = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--gpus", "2", "--steps", "2",
                           "--warmup", "3", "--nsys", "16", "--coll", "100", "--no-cpu-baseline",
-                          "--no-secondary"], capture_output=True, text=True, timeout=600, cwd=ROOT, env=env)
+                          "--no-secondary", "--no-tune"], capture_output=True, text=True, timeout=600, cwd=ROOT, env=env)
     assert out.returncode == 0, out.stderr[-3000:]
     lines = [l for l in out.stdout.splitlines() if l.strip().startswith("{")]
     assert len(lines) == 1, out.stdout

@@ -130,3 +130,21 @@ def test_warp_group_widths_match_reference(edmd, lanes):
         eng.close()
     finally:
         edmd.set_warp_group(32)
+
+
+def test_shared_memory_kernel_matches_reference(edmd):
+    """EDMD_F_SMEM: the systems whose state fits a block's shared memory run
+    from there (the 10^4-disk fixture does not fit and runs in the regular
+    kernel beside them); every system still reproduces the reference."""
+    by_len = {}
+    for n in golden_names():
+        g = golden(n)
+        by_len.setdefault(len(g["ct"]), []).append(g)
+    for L, gs in sorted(by_len.items()):
+        systems = [system_from_golden(edmd, g) for g in gs] * 3
+        eng = edmd.Engine(systems, trace_cap=L + 16)
+        eng.advance(max_coll=L, flags=edmd.F_TRACE | edmd.F_SMEM)
+        eng.sync()
+        for s in range(len(systems)):
+            check_against_golden(eng, s, gs[s % len(gs)])
+        eng.close()
