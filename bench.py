@@ -495,7 +495,7 @@ class Stepper:
     def step(self):
         if self.engine == "round":
             _, ms, rounds, viol = self.eng.advance_rounds(max_coll=self.coll, radius=self.radius,
-                                                          flags=self.edmd.F_EXACT)
+                                                          flags=self.edmd.F_EXACT | self.extra_flags)
             self.launches += 6 * rounds + 4
             self.rounds += rounds
             self.violations += viol
@@ -561,6 +561,9 @@ def measure(edmd, a, workload, engine, coll, steps, warmup, rank, world, dist, d
     t_max = max_over_ranks(dist, t_dev)
     coll_all = sum_over_ranks(dist, ncoll)
     value = coll_all / t_max
+    screen = None
+    if workload == "single_4m" and getattr(a, "screen_compare", False):
+        screen = compare_screen(edmd, a, systems[0], eng, steps, coll, c1)
     # ---- end to end through the C ABI with pinned host buffers
     eng.sync()
     stt = eng.states()
@@ -614,10 +617,55 @@ def measure(edmd, a, workload, engine, coll, steps, warmup, rank, world, dist, d
     if engine == "round":
         roof["rounds_per_step"] = rounds / steps
         roof["causality_violations_replayed"] = violations
+    if screen:
+        roof["fp32_screen"] = screen
     return dict(value=value, ms_per_step=1000 * t_max / steps, wall=wall, clocks=clocks, launches=launches,
                 engine=engine, lanes=(tuned["lanes"] if tuned else a.warp_group) if engine == "warp" else None,
                 smem=bool(extra), tuned=tuned,
                 systems=len(systems), TN=TN, e2e=e2e, h2d=h2d, d2h=d2h, roofline=roof)
+
+
+def _kinetic(st):
+    return 0.5 * float(np.sum(st["m"] * (st["vx"] ** 2 + st["vy"] ** 2)))
+
+
+def compare_screen(edmd, a, sysd, eng_fp64, steps, coll, c_fp64):
+    """The precision configuration: the same system, equilibration and timed
+    steps again with the FP32 screen of separating pairs (EDMD_F_SCREEN),
+    against the all-FP64 run just measured.  Missed collisions show as a
+    different collision count or final state (identical states mean the
+    FP64 run has the same drift and Z); also reported: the relative energy
+    drift over the timed steps and Z = P A / (N kT) from their virial."""
+    eng_fp64.sync()
+    st64 = eng_fp64.states()
+    e2 = edmd.Engine([sysd])
+    e2.advance_rounds(max_coll=LARGE_EQUIL, radius=a.radius, flags=edmd.F_EXACT)
+    for _ in range(a.warmup):
+        e2.advance_rounds(max_coll=coll, radius=a.radius, flags=edmd.F_EXACT | edmd.F_SCREEN)
+    e2.sync()
+    e_start = _kinetic(e2.states())
+    t0 = e2.counters(0)["t"]
+    e2.virial(0, reset=True)
+    c0 = e2.counters(0)
+    ms = 0.0
+    for _ in range(steps):
+        ms += e2.advance_rounds(max_coll=coll, radius=a.radius, flags=edmd.F_EXACT | edmd.F_SCREEN)[1]
+    c1 = e2.counters(0)
+    e2.sync()
+    st32 = e2.states()
+    vir = e2.virial(0)
+    dt = c1["t"] - t0
+    E = _kinetic(st32)
+    z = 1.0 - (vir[0] + vir[1]) / (2.0 * E * dt) if dt > 0 else None
+    same = all(np.array_equal(st32[k], st64[k]) for k in ("x", "y", "vx", "vy"))
+    out = {"value": (c1["ncol"] - c0["ncol"]) / (ms / 1000.0), "unit": UNIT,
+           "collisions": int(c1["ncol"] - c0["ncol"]), "pairs_screened": int(c1["nscreen"] - c0["nscreen"]),
+           "pairs_tested": int(c1["npair"] - c0["npair"]),
+           "collisions_fp64": int(c_fp64["ncol"].sum()), "identical_final_state": bool(same),
+           "missed_collisions": int(abs(int(c1["ncol"]) - int(c_fp64["ncol"].sum()))) if same else None,
+           "energy_drift": E / e_start - 1.0, "Z": z, "t_span": dt}
+    e2.close()
+    return out
 
 
 def measure_differentiation(edmd, ncoll=DIFF_COLL):
@@ -801,6 +849,8 @@ def main():
                     help="warp engine: systems that fit a block's shared memory run from there (EDMD_F_SMEM)")
     ap.add_argument("--no-tune", dest="tune", action="store_false",
                     help="batched workload: skip the untimed choice of engine and launch shape")
+    ap.add_argument("--screen-compare", action="store_true",
+                    help="single_4m: rerun the timed steps with the FP32 screen and compare with the FP64 run")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-secondary", action="store_true")
     ap.add_argument("--warp-group", type=int, default=32, choices=[4, 8, 16, 32],
