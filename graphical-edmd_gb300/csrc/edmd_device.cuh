@@ -66,7 +66,8 @@ struct Box {
   double Lx, Ly, hLx, hLy;     // box and halves (boxConstantHelper src/EDMD.c:679)
   double cxs, cys, cxf, cyf;   // cell sizes and reciprocals
   double dtP, dtPN;            // calendar bucket width 5/N and width*N
-  int32_t Nxc, Nyc, N, pad;
+  int32_t Nxc, Nyc, N;
+  int32_t additive;            // contact distance r1 + r2 instead of 2 sqrt(r1 r2)
 };
 
 constexpr int MAXLEV = 8;
@@ -147,6 +148,22 @@ __device__ __forceinline__ int pbc_cx(const Box& B, int a) { return a < 0 ? a + 
 __device__ __forceinline__ int pbc_cy(const Box& B, int a) { return a < 0 ? a + B.Nyc : (a >= B.Nyc ? a - B.Nyc : a); }
 
 
+// Contact distance and its square, DIST / DIST2 (src/EDMD.c:35-43): the
+// reference's default (NONADDITIVE 0) is 2 sqrt(r1 r2); additive contact
+// (NONADDITIVE 1) is r1 + r2.  Same operation order as the macros.  The
+// switch is per system and uniform over a warp's system.
+__device__ __forceinline__ double contact2(const Box& B, double r1, double r2) {
+  if (B.additive) {
+    const double s = r1 + r2;
+    return s * s;
+  }
+  return 4 * r1 * r2;
+}
+__device__ __forceinline__ double contact(const Box& B, double r1, double r2) {
+  if (B.additive) return r1 + r2;
+  return sqrt(4 * r1 * r2);
+}
+
 // collisionTimeNormal src/EDMD.c:2661-2723; p1 is current at t.
 // *overlap is set when the pair overlaps by more than 0.01 (2708-2717).
 __device__ __forceinline__ double coll_time_normal(const Box& B, const Disk& p1, const Disk& p2,
@@ -160,7 +177,7 @@ __device__ __forceinline__ double coll_time_normal(const Box& B, const Disk& p1,
   double b = dx * dvx + dy * dvy;
   if (b > 0) return NEVER;
   double v2 = dvx * dvx + dvy * dvy;
-  double d2 = dx * dx + dy * dy - 4 * p1.rad * p2.rad;
+  double d2 = dx * dx + dy * dy - contact2(B, p1.rad, p2.rad);
   double det = b * b - v2 * d2;
   if (d2 < -0.01) { *overlap = true; return NEVER; }
   if (det < 0) return NEVER;
@@ -177,7 +194,7 @@ __device__ __forceinline__ double coll_time_grow(const Box& B, const Disk& p1, d
   double dvr = vr1 + vr2;
   double dx = (p2.x + lat2 * p2.vx) - p1.x;
   double dy = (p2.y + lat2 * p2.vy) - p1.y;
-  double dr = sqrt(4 * (p1.rad) * (p2.rad + lat2 * vr2));
+  double dr = contact(B, p1.rad, p2.rad + lat2 * vr2);
   pbc(B, dx, dy);
   double b = dx * dvx + dy * dvy - dvr * dr;
   double v2 = dvx * dvx + dvy * dvy;
@@ -276,7 +293,7 @@ __device__ __forceinline__ double coll_time_normal_i(const Box& B, const Disk& p
   double b = dx * dvx + dy * dvy;
   if (is_pos(b)) return NEVER;
   double v2 = dvx * dvx + dvy * dvy;
-  double d2 = dx * dx + dy * dy - 4 * p1.rad * p2.rad;
+  double d2 = dx * dx + dy * dy - contact2(B, p1.rad, p2.rad);
   double det = b * b - v2 * d2;
   if (lt_neg(d2, 0.01)) { *overlap = true; return NEVER; }
   if (is_neg(det)) return NEVER;

@@ -742,7 +742,7 @@ __device__ void run_system(const SysDev& S, const RunArgs& A, int64_t max_coll, 
           // dx*dvx on even lanes, dy*dvy on odd lanes, then their sum
           const double pm = ((q4 & 1) ? dy : dx) * ((q4 & 1) ? dvy : dvx);
           double collKernel = invMass * (1 + S.res) * (G.shfl(pm, 0) + G.shfl(pm, 1));
-          double distSquared = 4 * di.rad * dj.rad;
+          double distSquared = contact2(B, di.rad, dj.rad);
           double f = __double_as_longlong(distSquared) == 0x4010000000000000ll ? collKernel * 0.25
                                                                                 : collKernel / distSquared;
           double ct = di.m * dj.m * f;
@@ -1340,11 +1340,14 @@ extern "C" int edmd_create(int32_t nsys, const edmd_system_desc* desc, const dou
   int64_t TN = 0, TC = 0, TE = 0, TT = 0;
   for (int s = 0; s < nsys; s++) {
     const edmd_system_desc& D = desc[s];
-    if (D.N < 2 || !(D.Lx > 0) || !(D.Ly > 0)) return set_err(ctx, EDMD_ERR_ARG, "bad system descriptor");
+    if (D.N < 2 || !(D.Lx > 0) || !(D.Ly > 0) || (D.contact != EDMD_CONTACT_NONADDITIVE &&
+                                                     D.contact != EDMD_CONTACT_ADDITIVE))
+      return set_err(ctx, EDMD_ERR_ARG, "bad system descriptor");
     SysDev& S = ctx->hs[s];
     memset(&S, 0, sizeof(S));
     Box& B = S.B;
     B.N = D.N; B.Lx = D.Lx; B.Ly = D.Ly;
+    B.additive = D.contact == EDMD_CONTACT_ADDITIVE;
     B.hLx = D.Lx / 2; B.hLy = D.Ly / 2;                      // boxConstantHelper 679-714
     B.Nyc = (int)(B.hLy); B.Nxc = (int)(B.hLx);
     if (B.Nxc < 1 || B.Nyc < 1) return set_err(ctx, EDMD_ERR_ARG, "box smaller than one cell");
@@ -1656,6 +1659,14 @@ extern "C" int edmd_get_thermo(edmd_ctx* ctx, int32_t s, double* rows, int32_t c
   return nr > S.rows_cap ? EDMD_ERR_CAPACITY : EDMD_OK;
 }
 
+extern "C" int edmd_take_thermo(edmd_ctx* ctx, int32_t s, double* rows, int32_t cap, int32_t* n) {
+  const int rc = edmd_get_thermo(ctx, s, rows, cap, n);
+  if (rc != EDMD_OK && rc != EDMD_ERR_CAPACITY) return rc;
+  const int32_t zero = 0;
+  CK(sync_copy(ctx, &ctx->hs[s].st->nrows, &zero, 4, cudaMemcpyHostToDevice));
+  return rc;
+}
+
 extern "C" int edmd_get_trace(edmd_ctx* ctx, int32_t s, edmd_collision* out, int64_t cap, int64_t* n) {
   if (!ctx || s < 0 || s >= ctx->nsys || !n) return EDMD_ERR_ARG;
   const SysDev& S = ctx->hs[s];
@@ -1815,10 +1826,13 @@ extern "C" int edmd_run_noalloc(const edmd_system_desc* desc, double* x, double*
     return noalloc_fail(EDMD_ERR_ARG, "edmd_run_noalloc: growth starts are not supported");
   if (D.N < 2 || D.N > NOALLOC_MAX_N)
     return noalloc_fail(EDMD_ERR_CAPACITY, "edmd_run_noalloc: N must be in [2, 8192]");
+  if (D.contact != EDMD_CONTACT_NONADDITIVE && D.contact != EDMD_CONTACT_ADDITIVE)
+    return noalloc_fail(EDMD_ERR_ARG, "edmd_run_noalloc: bad contact rule");
   SysDev S;
   memset(&S, 0, sizeof(S));
   Box& B = S.B;
   B.N = D.N; B.Lx = D.Lx; B.Ly = D.Ly;
+  B.additive = D.contact == EDMD_CONTACT_ADDITIVE;
   B.hLx = D.Lx / 2; B.hLy = D.Ly / 2;                      // boxConstantHelper 679-714
   B.Nyc = (int)(B.hLy); B.Nxc = (int)(B.hLx);
   if (!(D.Lx > 0) || !(D.Ly > 0) || B.Nxc < 1 || B.Nyc < 1)

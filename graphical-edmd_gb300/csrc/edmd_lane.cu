@@ -405,7 +405,7 @@ __device__ void lane_run(const SysDev& S, const RunArgs& A) {
         double invMass = __double_as_longlong(msum) == 0x4000000000000000ll ? 0.5 : 1 / msum;
         pbc(B, dx, dy);
         double collKernel = invMass * (1 + S.res) * (dx * dvx + dy * dvy);
-        double distSquared = 4 * Da.rad * Db.rad;
+        double distSquared = contact2(B, Da.rad, Db.rad);
         double f = __double_as_longlong(distSquared) == 0x4010000000000000ll
             ? collKernel * 0.25 : collKernel / distSquared;
         double ct = Da.m * Db.m * f;

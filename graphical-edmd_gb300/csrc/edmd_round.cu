@@ -722,7 +722,7 @@ __device__ void process_event_warp(const SysDev& S, const RoundArgs& A, int s, i
         const double invMass = __double_as_longlong(msum) == 0x4000000000000000ll ? 0.5 : 1 / msum;
         pbc_i(B, dx, dy);
         const double collKernel = invMass * (1 + S.res) * (dx * dvx + dy * dvy);
-        const double distSquared = 4 * Da.rad * Db.rad;
+        const double distSquared = contact2(B, Da.rad, Db.rad);
         const double f = __double_as_longlong(distSquared) == 0x4010000000000000ll
             ? collKernel * 0.25 : collKernel / distSquared;
         const double cf = Da.m * Db.m * f;
@@ -970,7 +970,7 @@ __device__ void process_event_thread(const SysDev& S, const RoundArgs& A, int s,
       const double invMass = __double_as_longlong(msum) == 0x4000000000000000ll ? 0.5 : 1 / msum;
       pbc_i(B, dx, dy);
       const double collKernel = invMass * (1 + S.res) * (dx * dvx + dy * dvy);
-      const double distSquared = 4 * Da.rad * Db.rad;
+      const double distSquared = contact2(B, Da.rad, Db.rad);
       const double f = __double_as_longlong(distSquared) == 0x4010000000000000ll
           ? collKernel * 0.25 : collKernel / distSquared;
       const double cf = Da.m * Db.m * f;

@@ -31,7 +31,12 @@ class SystemDesc(C.Structure):
     _fields_ = [("N", C.c_int32), ("Lx", C.c_double), ("Ly", C.c_double), ("res", C.c_double),
                 ("Einit", C.c_double), ("first_screen", C.c_double), ("dtime", C.c_double),
                 ("first_thermo", C.c_double), ("dtime_thermo", C.c_double),
-                ("t_growstop", C.c_double), ("tmax", C.c_double)]
+                ("t_growstop", C.c_double), ("tmax", C.c_double), ("contact", C.c_int32)]
+
+
+# contact rules (edmd_system_desc.contact): 2 sqrt(r1 r2) or r1 + r2
+CONTACT_NONADDITIVE = 0
+CONTACT_ADDITIVE = 1
 
 
 class Collision(C.Structure):
@@ -58,7 +63,7 @@ EXPORTS = [
     "edmd_create", "edmd_load_state", "edmd_advance", "edmd_advance_rounds", "edmd_sync",
     "edmd_get_pcf", "edmd_get_state",
     "edmd_get_states", "edmd_get_counters", "edmd_get_all_counters", "edmd_get_virial",
-    "edmd_get_thermo", "edmd_get_trace", "edmd_set_engine", "edmd_set_lane_threads",
+    "edmd_get_thermo", "edmd_take_thermo", "edmd_get_trace", "edmd_set_engine", "edmd_set_lane_threads",
     "edmd_set_warp_group",
     "edmd_get_engine", "edmd_get_last_ms", "edmd_set_device", "edmd_host_alloc", "edmd_host_free", "edmd_run_noalloc",
     "edmd_set_log_capacity", "edmd_clear_log", "edmd_get_log", "edmd_checkpoint_save",
@@ -120,6 +125,7 @@ def load(path=LIB_PATH):
     L.edmd_get_counters.argtypes = [C.c_void_p, C.c_int32, C.POINTER(Counters)]
     L.edmd_get_virial.argtypes = [C.c_void_p, C.c_int32, _dp, C.c_int32]
     L.edmd_get_thermo.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.POINTER(C.c_int32)]
+    L.edmd_take_thermo.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.POINTER(C.c_int32)]
     L.edmd_get_trace.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_int64, C.POINTER(C.c_int64)]
     L.edmd_destroy.argtypes = [C.c_void_p]
     L.edmd_last_error.argtypes = [C.c_void_p]
@@ -185,9 +191,11 @@ def grow_start(N, phi, seed, xs=0.3, q=0.4, aspect=1.0):
                 type=typ, vr=vr, vr_base=vrb.value)
 
 
-def default_desc(N, Lx, Ly, vr_base=0.0, tmax=4000.0, dtime=100.0, dtime_thermo=100.0):
+def default_desc(N, Lx, Ly, vr_base=0.0, tmax=4000.0, dtime=100.0, dtime_thermo=100.0,
+                 contact=CONTACT_NONADDITIVE):
     d = SystemDesc()
     load().edmd_default_desc(C.byref(d), N, Lx, Ly, vr_base, tmax, dtime, dtime_thermo)
+    d.contact = contact
     return d
 
 
@@ -370,10 +378,13 @@ class Engine:
         self._ck(self._L.edmd_get_virial(self.h, s, v, int(reset)))
         return v
 
-    def thermo(self, s=0, cap=1024):
+    def thermo(self, s=0, cap=1024, take=False):
+        """Thermo rows of system s; take=True empties its row buffer too
+        (edmd_take_thermo)."""
         rows = np.zeros((cap, 9))
         n = C.c_int32()
-        rc = self._L.edmd_get_thermo(self.h, s, _ptr(rows), cap, C.byref(n))
+        f = self._L.edmd_take_thermo if take else self._L.edmd_get_thermo
+        rc = f(self.h, s, _ptr(rows), cap, C.byref(n))
         if rc not in (OK, ERR_CAPACITY):
             self._ck(rc)
         return rows[: min(n.value, cap)]

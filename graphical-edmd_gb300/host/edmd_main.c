@@ -12,7 +12,8 @@
  * -r/--res, -v/--version (seed and file version), -l/--load (.txt or a dump
  * ending in 'p').  Added: --hex (triangular-lattice start, the reference's
  * Hex = 1 global), --max-coll n (stop after n accepted collisions),
- * --quiet.
+ * --quiet, --additive (contact distance r1 + r2: the reference built with
+ * NONADDITIVE 1, src/EDMD.c:35-43).
  */
 #include "../../include/edmd_gpu.h"
 #include "../../include/edmd_host.h"
@@ -29,7 +30,7 @@
 typedef struct {
 	int N; double phi, xs, q, aspect, tmax, dtime, dtimeThermo, Einit, res;
 	unsigned seed; int version; int hex; int load; char loadfile[512];
-	long long max_coll; int quiet;
+	long long max_coll; int quiet; int additive;
 } opts;
 
 static void die(const char* m, edmd_ctx* c)
@@ -128,14 +129,14 @@ static int load_dump(const char* fn, double** arr, int32_t** type, double* Lx, d
 
 int main(int argc, char* argv[])
 {
-	opts o = {500, 0.38, 0.3, 0.4, 1.0, 4000, 100, 100, 1, 1, 0, 1, 0, 0, "", -1, 0};
+	opts o = {500, 0.38, 0.3, 0.4, 1.0, 4000, 100, 100, 1, 1, 0, 1, 0, 0, "", -1, 0, 0};
 	int seeded = 0;
 	static struct option lo[] = {
 		{"load", 1, 0, 'l'}, {"number", 1, 0, 'N'}, {"phi", 1, 0, 'p'}, {"res", 1, 0, 'r'},
 		{"time", 1, 0, 't'}, {"dt", 1, 0, 'D'}, {"initial-energy", 1, 0, 'E'}, {"xs", 1, 0, 'x'},
 		{"sizeratio", 1, 0, 'q'}, {"aspect", 1, 0, 'a'}, {"dtimeThermo", 1, 0, 'o'},
 		{"version", 1, 0, 'v'}, {"hex", 0, 0, 1000}, {"max-coll", 1, 0, 1001}, {"quiet", 0, 0, 1002},
-		{0, 0, 0, 0}};
+		{"additive", 0, 0, 1003}, {0, 0, 0, 0}};
 	int c;
 	while ((c = getopt_long(argc, argv, "l:N:p:r:t:D:E:x:q:a:o:v:", lo, NULL)) != -1) {
 		switch (c) {
@@ -159,6 +160,7 @@ int main(int argc, char* argv[])
 		case 1000: o.hex = 1; break;
 		case 1001: o.max_coll = atoll(optarg); break;
 		case 1002: o.quiet = 1; break;
+		case 1003: o.additive = 1; break;
 		default: fprintf(stderr, "edmd: unknown option\n"); return 1;
 		}
 	}
@@ -214,6 +216,7 @@ int main(int argc, char* argv[])
 	edmd_system_desc d;
 	edmd_default_desc(&d, N, Lx, Ly, o.load ? 0 : vr_base, o.tmax, o.dtime, o.dtimeThermo);
 	d.res = o.res; d.Einit = o.Einit;
+	d.contact = o.additive ? EDMD_CONTACT_ADDITIVE : EDMD_CONTACT_NONADDITIVE;
 	edmd_ctx* ctx = NULL;
 	int rc = edmd_create(1, &d, a[0], a[1], a[2], a[3], a[4], a[5], vr_base > 0 ? a[6] : NULL, 0, &ctx);
 	if (rc != EDMD_OK) die("engine creation failed", ctx);

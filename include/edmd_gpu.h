@@ -84,7 +84,16 @@ typedef struct edmd_system_desc {
 	double  dtime_thermo;  /* thermo period (-o)                               */
 	double  t_growstop;    /* 1/vr for a growth start, < 0 for a direct start  */
 	double  tmax;          /* loop bound (-t, +1/vr for a growth start)        */
+	int32_t contact;       /* contact rule, EDMD_CONTACT_* (zero-initialise:
+	                          0 is the reference's default)                    */
 } edmd_system_desc;
+
+/* Contact distance of disks of radii r1, r2 (DIST / DIST2, src/EDMD.c:35-43).
+ * The reference selects it at compile time with NONADDITIVE (0 by default);
+ * here it is per system, in every engine and phase (pair solves
+ * collisionTimeNormal / collisionTimeGrow and the elastic collision rule). */
+#define EDMD_CONTACT_NONADDITIVE 0   /* 2 sqrt(r1 r2): NONADDITIVE 0 */
+#define EDMD_CONTACT_ADDITIVE    1   /* r1 + r2:       NONADDITIVE 1 */
 
 /* one accepted collision, as logged by the reference harness */
 typedef struct edmd_collision {
@@ -212,6 +221,12 @@ int edmd_get_virial(edmd_ctx* ctx, int32_t sys, double out[4], int32_t reset);
 /* Thermo rows of one system (t Ncol E p px py pxy pyx a2, saveThermo
  * src/EDMD.c:5232-5697 with Nthermo = 1); returns the row count in *n. */
 int edmd_get_thermo(edmd_ctx* ctx, int32_t sys, double* rows, int32_t cap, int32_t* n);
+
+/* edmd_get_thermo, then empty the system's row buffer, so that a long run
+ * can drain its rows between calls (each system holds 1024 rows; rows made
+ * beyond that are counted in *n but lost, and the call returns
+ * EDMD_ERR_CAPACITY). */
+int edmd_take_thermo(edmd_ctx* ctx, int32_t sys, double* rows, int32_t cap, int32_t* n);
 
 /* Collision trace of one system recorded since creation (EDMD_F_TRACE). */
 int edmd_get_trace(edmd_ctx* ctx, int32_t sys, edmd_collision* out, int64_t cap, int64_t* n);

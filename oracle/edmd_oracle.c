@@ -89,6 +89,7 @@ struct orc_sys {
 	double vr;
 	int grow;               /* 1 while the Lubachevsky-Stillinger growth runs */
 	int stop_at_grow;       /* orc_run returns right after the growth-stop event */
+	int additive;           /* contact distance r1 + r2 instead of 2 sqrt(r1 r2) */
 	/* disks */
 	double *x, *y, *vx, *vy, *tl, *rad, *m, *vrd;
 	int32_t *type, *cx, *cy, *prv, *nxt, *crossX, *crossY;
@@ -279,6 +280,27 @@ static void free_fly(orc_sys* s, int i)
 /* ------------------------------------------------------------------ */
 /* predictions                                                        */
 /* ------------------------------------------------------------------ */
+/* contact distance and its square, DIST / DIST2 (EDMD.c:35-43): the
+ * reference's default NONADDITIVE 0 gives 2 sqrt(r1 r2); NONADDITIVE 1 gives
+ * r1 + r2.  Same operation order as the macros. */
+static int g_additive = 0;
+int orc_set_contact(int additive)
+{
+	int old = g_additive;
+	g_additive = additive != 0;
+	return old;
+}
+
+static inline double contact(const orc_sys* s, double r1, double r2)
+{
+	return s->additive ? (r1) + (r2) : sqrt(4 * (r1) * (r2));
+}
+
+static inline double contact2(const orc_sys* s, double r1, double r2)
+{
+	return s->additive ? ((r1) + (r2)) * ((r1) + (r2)) : 4 * (r1) * (r2);
+}
+
 static double coll_time_normal(orc_sys* s, int a, int b)    /* collisionTimeNormal 2661 */
 {
 	s->npair++;
@@ -291,7 +313,7 @@ static double coll_time_normal(orc_sys* s, int a, int b)    /* collisionTimeNorm
 	double bb = dx * dvx + dy * dvy;
 	if (bb > 0) return NEVER;
 	double v2 = dvx * dvx + dvy * dvy;
-	double d2 = dx * dx + dy * dy - 4 * s->rad[a] * s->rad[b];
+	double d2 = dx * dx + dy * dy - contact2(s, s->rad[a], s->rad[b]);
 	double det = bb * bb - v2 * d2;
 	if (d2 < -0.01) {
 		fprintf(stderr, "oracle: overlap between %d and %d at t=%.17g\n", a, b, s->t);
@@ -310,7 +332,7 @@ static double coll_time_grow(orc_sys* s, int a, int b)      /* collisionTimeGrow
 	double dvr = s->vrd[a] + s->vrd[b];
 	double dx = (s->x[b] + lat2 * s->vx[b]) - s->x[a];
 	double dy = (s->y[b] + lat2 * s->vy[b]) - s->y[a];
-	double dr = sqrt(4 * (s->rad[a]) * (s->rad[b] + lat2 * s->vrd[b]));
+	double dr = contact(s, s->rad[a], s->rad[b] + lat2 * s->vrd[b]);
 	pbc(s, &dx, &dy);
 	double bb = dx * dvx + dy * dvy - dvr * dr;
 	double v2 = dvx * dvx + dvy * dvy;
@@ -410,7 +432,7 @@ static void do_collision(orc_sys* s, int i, int j, uint64_t collActual)  /* doTh
 		double invMass = 1 / (s->m[i] + s->m[j]);
 		pbc(s, &dx, &dy);
 		double collKernel = invMass * (1 + s->res) * (dx * dvx + dy * dvy);
-		double distSquared = 4 * s->rad[i] * s->rad[j];
+		double distSquared = contact2(s, s->rad[i], s->rad[j]);
 		double f = collKernel / distSquared;
 		double ct = s->m[i] * s->m[j] * f;
 		s->collT[0] += ct * dx * dx;
@@ -550,6 +572,7 @@ static orc_sys* alloc_sys(int N)
 {
 	orc_sys* s = (orc_sys*)calloc(1, sizeof(orc_sys));
 	s->N = N;
+	s->additive = g_additive;
 #define A(f, T) s->f = (T*)calloc((size_t)N, sizeof(T))
 	A(x, double); A(y, double); A(vx, double); A(vy, double); A(tl, double);
 	A(rad, double); A(m, double); A(vrd, double);

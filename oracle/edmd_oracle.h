@@ -103,6 +103,10 @@ double   orc_vr(const orc_sys* s);
  * src/EDMD.c:4740) when on != 0: the point where a growth start enters the
  * normal phase, as the engine's EDMD_F_STOP_AT_GROW */
 void     orc_set_stop_at_grow(orc_sys* s, int on);
+/* contact rule of systems created from now on: 0 = 2 sqrt(r1 r2) (the
+ * reference's NONADDITIVE 0, EDMD.c:35-39), 1 = r1 + r2 (NONADDITIVE 1,
+ * EDMD.c:40-42).  Returns the previous setting. */
+int      orc_set_contact(int additive);
 /* thermo rows (t Ncol E p px py pxy pyx a2), 9 doubles each; returns count */
 int      orc_thermo_rows(const orc_sys* s, double* out, int cap);
 

@@ -58,6 +58,8 @@ def load():
         L.orc_vr.argtypes = [C.c_void_p]
         L.orc_vr.restype = C.c_double
         L.orc_set_stop_at_grow.argtypes = [C.c_void_p, C.c_int]
+        L.orc_set_contact.argtypes = [C.c_int]
+        L.orc_set_contact.restype = C.c_int
         L.orc_growing.argtypes = [C.c_void_p]
         L.orc_box.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double),
                               C.POINTER(C.c_int), C.POINTER(C.c_int)]
@@ -79,9 +81,20 @@ class Oracle:
     """One serial reference-semantics system on the CPU."""
 
     def __init__(self, N=None, phi=0.7, seed=1, start=HEX, xs=0.0, q=0.4, aspect=1.0, tmax=4000.0,
-                 dtime=100.0, dtime_thermo=100.0, arrays=None, Lx=None, Ly=None, first_thermo=None):
+                 dtime=100.0, dtime_thermo=100.0, arrays=None, Lx=None, Ly=None, first_thermo=None,
+                 additive=False):
         L = load()
         self._L = L
+        old = L.orc_set_contact(1 if additive else 0)
+        try:
+            self._create(L, N, phi, seed, start, xs, q, aspect, tmax, dtime, dtime_thermo, arrays, Lx, Ly,
+                         first_thermo)
+        finally:
+            L.orc_set_contact(old)
+        self.N = L.orc_N(self.h)
+
+    def _create(self, L, N, phi, seed, start, xs, q, aspect, tmax, dtime, dtime_thermo, arrays, Lx, Ly,
+                first_thermo):
         if arrays is not None:
             a = {k: np.ascontiguousarray(v) for k, v in arrays.items()}
             self.h = L.orc_create_from_arrays(len(a["x"]), Lx, Ly, a["x"], a["y"], a["vx"], a["vy"],
@@ -95,7 +108,6 @@ class Oracle:
             if first_thermo is not None:
                 p.firstThermo = first_thermo
             self.h = L.orc_create(C.byref(p))
-        self.N = L.orc_N(self.h)
 
     def run(self, max_coll, t_stop=float("inf"), cap=None):
         cap = max_coll if cap is None else cap

@@ -39,8 +39,25 @@ CASES = {
     "grow300_v5": ("-N 300 --phi 0.3 -x 0.5 -q 0.7142857 -v 5", 20000, True),
 }
 
+# the same kind of runs with additive contact, r1 + r2 (the reference's own
+# switch NONADDITIVE set to 1 at src/EDMD.c:35; built by
+# `make -C oracle ref-additive`); their fixtures carry contact = 1
+ADDITIVE_CASES = {
+    "add_grow256_v7": ("-N 256 --phi 0.5 -x 0.5 -q 0.7142857 -v 7", 20000, True),
+    "add_grow400_v11": ("-N 400 --phi 0.74 -x 0.5 -q 0.7142857 -v 11", 20000, True),
+    "add_grow300_v5": ("-N 300 --phi 0.3 -x 0.5 -q 0.4 -v 5", 20000, True),
+}
+
 # a short run whose dump and thermo files are kept verbatim (format pin)
 FILES_CASE = ("files_hex64", "--hex -N 64 --phi 0.5 -x 0 -v 9 -t 1200 -D 100 -o 50")
+
+# bidisperse growth starts whose dump and thermo files are kept verbatim, with
+# the reference's contact rule and with additive contact (contact = 1: the
+# drop-in program runs them with --additive)
+FILES_GROW_CASES = {
+    "files_grow64": ("-N 64 --phi 0.5 -x 0.5 -q 0.4 -v 9 -t 1100 -D 100 -o 25", 0),
+    "files_add_grow64": ("-N 64 --phi 0.5 -x 0.5 -q 0.4 -v 9 -t 1100 -D 100 -o 25", 1),
+}
 
 # restarts with -l (src/EDMD.c:980-995, 1366-1451): from a .txt state (the
 # final positions of the files case; velocities drawn anew) and from the
@@ -98,14 +115,17 @@ def main():
     a = ap.parse_args()
     if not a.ref:
         ap.error("give --ref or set EDMD_REFERENCE_DIR to the reference checkout")
-    subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "ref", f"REF={a.ref}"], check=True)
+    subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "ref", "ref-additive", f"REF={a.ref}"],
+                   check=True)
     exe = os.path.join(ROOT, "oracle", "_ref", "ref_trace")
+    exe_add = os.path.join(ROOT, "oracle", "_ref", "ref_trace_additive")
     tmp = os.path.join(HERE, "_tmp_trace.txt")
-    for name, (args, maxcoll, full) in CASES.items():
-        run_case(exe, args, maxcoll, tmp)
+    cases = [(n, c, exe, 0) for n, c in CASES.items()] + [(n, c, exe_add, 1) for n, c in ADDITIVE_CASES.items()]
+    for name, (args, maxcoll, full), case_exe, contact in cases:
+        run_case(case_exe, args, maxcoll, tmp)
         head, init, c, vir, tfin, state = parse_trace(tmp)
         out = dict(
-            args=np.array(args), N=head["N"], Lx=head["Lx"], Ly=head["Ly"],
+            args=np.array(args), contact=contact, N=head["N"], Lx=head["Lx"], Ly=head["Ly"],
             Nxc=head["Nxc"], Nyc=head["Nyc"],
             x0=init[:, 0].astype(np.float64), y0=init[:, 1].astype(np.float64),
             vx0=init[:, 2].astype(np.float64), vy0=init[:, 3].astype(np.float64),
@@ -134,6 +154,14 @@ def main():
     np.savez_compressed(os.path.join(HERE, name + ".npz"), args=np.array(args), N=head["N"],
                         ncol=tfin[1], t_final=tfin[0])
     print(name, "N", head["N"], "collisions", len(c))
+    for name, (args, contact) in FILES_GROW_CASES.items():
+        dump = os.path.join(HERE, name + ".dump")
+        thermo = os.path.join(HERE, name + ".thermo")
+        run_case(exe_add if contact else exe, args, 10**12, tmp, {"DUMP_OUT": dump, "THERMO_OUT": thermo})
+        h, _, cc, _, tf, _ = parse_trace(tmp)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), args=np.array(args), contact=contact,
+                            N=h["N"], ncol=tf[1], t_final=tf[0])
+        print(name, "N", h["N"], "collisions", len(cc))
     # the .txt restart state: "N Lx Ly", then "type x y rad m" per disk
     with open(os.path.join(HERE, LOAD_TXT), "w") as f:
         f.write("%d %.17g %.17g\n" % (head["N"], head["Lx"], head["Ly"]))

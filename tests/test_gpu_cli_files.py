@@ -1,9 +1,10 @@
 """The drop-in program writes the reference's dump and thermo files byte for byte.
 
-tests/golden/files_hex64.{dump,thermo} were written by the reference's own
+tests/golden/files_*.{dump,thermo} were written by the reference's own
 saveTXT / saveThermo (tests/golden/make_golden.py).  The program runs the same
 command line on the GPU; since the trajectory is bit-identical, the text
-files must be identical too (134,574 collisions, 12 frames, 5 thermo rows).
+files must be identical too (the hexagonal case: 134,574 collisions, 12
+frames, 5 thermo rows).
 """
 import glob
 import os
@@ -39,6 +40,25 @@ def test_restart_files_identical(built, tmp_path, name):
     the golden dump and thermo files (tests/golden/make_golden.py)."""
     g = dict(np.load(os.path.join(GOLDEN, name + ".npz")))
     args = str(g["args"]).format(golden=GOLDEN).split()
+    exe = os.path.join(PKG, "edmd")
+    r = subprocess.run([exe] + args + ["--quiet"], cwd=tmp_path, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 1, r.stderr
+    dumps = glob.glob(str(tmp_path / "dump" / "*.dump"))
+    thermos = glob.glob(str(tmp_path / "dump" / "*.thermo"))
+    assert len(dumps) == 1 and len(thermos) == 1
+    assert open(dumps[0]).read() == open(os.path.join(GOLDEN, name + ".dump")).read()
+    assert open(thermos[0]).read() == open(os.path.join(GOLDEN, name + ".thermo")).read()
+
+
+@pytest.mark.parametrize("name", ["files_grow64", "files_add_grow64"])
+def test_growth_start_files_identical(built, tmp_path, name):
+    """Bidisperse growth start (particlesInit 1690-1829, growth to the
+    growth stop, then the constant-radius phase): dump and thermo files as the
+    reference writes them, with its default contact rule and with additive
+    contact (the reference built with NONADDITIVE 1, src/EDMD.c:35-43; the
+    program's --additive)."""
+    g = dict(np.load(os.path.join(GOLDEN, name + ".npz")))
+    args = str(g["args"]).split() + (["--additive"] if int(g["contact"]) else [])
     exe = os.path.join(PKG, "edmd")
     r = subprocess.run([exe] + args + ["--quiet"], cwd=tmp_path, capture_output=True, text=True, timeout=600)
     assert r.returncode == 1, r.stderr

@@ -6,6 +6,9 @@ last one.  The engine starts from the same state and must reproduce the
 ordered (i, j) pairs, the cells, the times, the virial sums, the counters and
 the final positions/velocities exactly (integer and index results bit-exact;
 positions are compared exactly, which is stricter than the 1e-12 bound).
+The add_* fixtures come from the reference built with additive contact
+(NONADDITIVE 1, src/EDMD.c:35-43) and run with edmd_system_desc.contact =
+EDMD_CONTACT_ADDITIVE; batches mix them with the default-contact systems.
 """
 import numpy as np
 import pytest
@@ -24,7 +27,7 @@ def system_from_golden(edmd, g):
         s = edmd.grow_start(a["N"], a["phi"], a["seed"], xs=a["xs"], q=a["q"])
         vr, vr_base = s["vr"], s["vr_base"]
     desc = edmd.default_desc(N, float(g["Lx"]), float(g["Ly"]), vr_base, a["tmax"], a["dtime"],
-                             a["dtime_thermo"])
+                             a["dtime_thermo"], contact=int(g["contact"]))
     return dict(desc=desc, x=g["x0"], y=g["y0"], vx=g["vx0"], vy=g["vy0"], rad=g["rad0"], m=g["m0"], vr=vr)
 
 

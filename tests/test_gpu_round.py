@@ -122,13 +122,17 @@ def test_rounds_batch_matches_oracle(edmd, oracle):
     eng.close()
 
 
-def test_rounds_bidisperse_batch_after_growth(edmd, oracle):
-    """Growth on the serial engine, then the constant-radius phase in rounds."""
+@pytest.mark.parametrize("contact", ["default", "additive", "mixed"])
+def test_rounds_bidisperse_batch_after_growth(edmd, oracle, contact):
+    """Growth on the serial engine, then the constant-radius phase in rounds;
+    with the reference's contact rule, additive contact (r1 + r2), or the two
+    mixed in one batch."""
     starts = [edmd.grow_start(n, phi, seed, xs=0.5, q=0.7142857)
               for n, phi, seed in ((400, 0.70, 3), (1000, 0.55, 4), (256, 0.35, 5))]
+    add = [{"default": 0, "additive": 1, "mixed": k % 2}[contact] for k in range(len(starts))]
     systems = []
-    for s in starts:
-        d = edmd.default_desc(s["N"], s["Lx"], s["Ly"], s["vr_base"])
+    for k, s in enumerate(starts):
+        d = edmd.default_desc(s["N"], s["Lx"], s["Ly"], s["vr_base"], contact=add[k])
         systems.append(dict(desc=d, **{k: s[k] for k in ("x", "y", "vx", "vy", "rad", "m", "vr")}))
     eng = edmd.Engine(systems)
     eng.advance(flags=edmd.F_STOP_AT_GROW)
@@ -137,7 +141,7 @@ def test_rounds_bidisperse_batch_after_growth(edmd, oracle):
     eng.sync()
     for k, s in enumerate(starts):
         o = oracle.Oracle(N=s["N"], phi=[0.70, 0.55, 0.35][k], seed=[3, 4, 5][k], start=oracle.GROW,
-                          xs=0.5, q=0.7142857)
+                          xs=0.5, q=0.7142857, additive=bool(add[k]))
         o.run(10 ** 12, t_stop=t_stop, cap=1)
         o.sync()
         st, ost = eng.state(k), o.state()

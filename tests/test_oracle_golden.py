@@ -16,7 +16,7 @@ def test_oracle_matches_reference(oracle, name):
     g = golden(name)
     a = parse_args(g["args"])
     o = oracle.Oracle(N=a["N"], phi=a["phi"], seed=a["seed"], start=oracle.HEX if a["hex"] else oracle.GROW,
-                      xs=a["xs"], q=a["q"], tmax=a["tmax"])
+                      xs=a["xs"], q=a["q"], tmax=a["tmax"], additive=bool(g["contact"]))
     assert o.N == int(g["N"])
     Lx, Ly, nx, ny = o.box()
     assert (Lx, Ly, nx, ny) == (float(g["Lx"]), float(g["Ly"]), int(g["Nxc"]), int(g["Nyc"]))
@@ -68,3 +68,22 @@ def test_oracle_no_overlaps(oracle):
     d2 = dx * dx + dy * dy
     np.fill_diagonal(d2, np.inf)
     assert d2.min() > 4 - 1e-8     # EDMD_VERIFY_OVERLAPS tolerance (src/EDMD.c:4646)
+
+
+def test_oracle_contact_rules(oracle):
+    """Equal radii: (r + r)^2 == 4 r r exactly, so additive contact leaves a
+    monodisperse run bit-identical; a bidisperse growth start differs."""
+    runs = {}
+    for add in (False, True):
+        o = oracle.Oracle(N=400, phi=0.6, seed=2, start=oracle.HEX, additive=add)
+        tr, n = o.run(3000)
+        o.sync()
+        runs[add] = (tr.copy(), o.state())
+    np.testing.assert_array_equal(runs[False][0]["t"], runs[True][0]["t"])
+    np.testing.assert_array_equal(runs[False][1]["x"], runs[True][1]["x"])
+    grown = []
+    for add in (False, True):
+        o = oracle.Oracle(N=200, phi=0.5, seed=4, start=oracle.GROW, xs=0.5, q=0.4, additive=add)
+        tr, n = o.run(3000)
+        grown.append(tr["t"].copy())
+    assert not np.array_equal(grown[0], grown[1])

@@ -96,3 +96,33 @@ def test_noalloc_reports_an_overlap_met_during_the_run(edmd):
     assert rc == edmd.ERR_OVERLAP, msg
     assert names_pair(msg, 0, 1), msg
     assert ncol == 1 and abs(tout - 0.1) < 1e-12
+
+
+def test_noalloc_additive_contact_matches_oracle(edmd, oracle):
+    """A bidisperse packing grown with additive contact (r1 + r2) continues
+    in the allocation-free entry point exactly as in the oracle."""
+    import torch
+    L = edmd.load()
+    g = oracle.Oracle(N=300, phi=0.6, seed=8, start=oracle.GROW, xs=0.5, q=0.4, additive=True)
+    g.run_growth()
+    g.sync()
+    st = g.state()
+    Lx, Ly, _, _ = g.box()
+    start = {k: np.ascontiguousarray(st[k]) for k in KEYS}
+    assert set(np.round(start["rad"], 6)) == {0.4, 1.0}
+    o = oracle.Oracle(arrays=dict(start, type=st["type"]), Lx=Lx, Ly=Ly, additive=True)
+    o.run(2000, cap=1)
+    o.sync()
+    desc = edmd.default_desc(300, Lx, Ly, contact=edmd.CONTACT_ADDITIVE)
+    dev = torch.device("cuda:0")
+    bufs = {k: torch.tensor(start[k], dtype=torch.float64, device=dev) for k in KEYS}
+    torch.cuda.synchronize()
+    ncol, tout = C.c_int64(), C.c_double()
+    rc = L.edmd_run_noalloc(C.byref(desc), *[C.c_void_p(bufs[k].data_ptr()) for k in KEYS],
+                            2000, float("inf"), C.byref(ncol), C.byref(tout), None)
+    assert rc == edmd.OK, L.edmd_last_error(None)
+    out = {k: bufs[k].cpu().numpy() for k in KEYS}
+    ost = o.state()
+    for k in ("x", "y", "vx", "vy"):
+        np.testing.assert_array_equal(out[k], ost[k])
+    assert ncol.value == 2000 and tout.value == o.t
