@@ -52,6 +52,7 @@ struct edmd_ctx {
   int64_t total_C = 0;
   void* round = nullptr;            // buffers of the round-parallel engine (edmd_round.cu)
   bool round_dirty = false;         // queue order lost: set by the round engine, cleared by a restage
+  bool any_additive = false;        // some system uses additive contact (EDMD_CONTACT_ADDITIVE)
   std::vector<char> ckpt_dirty;     // round_dirty of each checkpoint
   std::string err;
 };

@@ -148,20 +148,38 @@ __device__ __forceinline__ int pbc_cx(const Box& B, int a) { return a < 0 ? a + 
 __device__ __forceinline__ int pbc_cy(const Box& B, int a) { return a < 0 ? a + B.Nyc : (a >= B.Nyc ? a - B.Nyc : a); }
 
 
+// 4 x exactly, on the integer pipe: x's exponent field + 2.  Equal to the
+// FP64 product 4 * x for x = 0 and for normal |x| < 2^1021; disk radii are
+// checked to be one of those when a system is created or loaded.
+__device__ __forceinline__ double times4(double x) {
+  const long long b = __double_as_longlong(x);
+  return __longlong_as_double((b & 0x7ff0000000000000ll) ? b + (2ll << 52) : b);
+}
+
+// radii the engines accept: zero or normal, positive and below 2^1020 (so
+// that times4 is exact)
+__host__ __device__ __forceinline__ bool radius_ok(double r) {
+  return r == 0.0 || (r >= 2.2250738585072014e-308 && r < 0x1p1020);
+}
+
 // Contact distance and its square, DIST / DIST2 (src/EDMD.c:35-43): the
 // reference's default (NONADDITIVE 0) is 2 sqrt(r1 r2); additive contact
-// (NONADDITIVE 1) is r1 + r2.  Same operation order as the macros.  The
-// switch is per system and uniform over a warp's system.
+// (NONADDITIVE 1) is r1 + r2.  Same roundings as the macros (4 r1 r2 is
+// (4 r1) r2 with 4 r1 exact).  The switch is per system, uniform over the
+// lanes that work on one system.
+// ADD = false compiles the reference's default rule only (a kernel
+// specialised for contexts without additive systems).
+template <bool ADD = true>
 __device__ __forceinline__ double contact2(const Box& B, double r1, double r2) {
-  if (B.additive) {
+  if (ADD && B.additive) {
     const double s = r1 + r2;
     return s * s;
   }
-  return 4 * r1 * r2;
+  return times4(r1) * r2;
 }
 __device__ __forceinline__ double contact(const Box& B, double r1, double r2) {
   if (B.additive) return r1 + r2;
-  return sqrt(4 * r1 * r2);
+  return sqrt(times4(r1) * r2);
 }
 
 // collisionTimeNormal src/EDMD.c:2661-2723; p1 is current at t.
@@ -282,6 +300,7 @@ __device__ __forceinline__ void free_fly_i(const Box& B, Disk& p, double t) {
 }
 // collisionTimeNormal (src/EDMD.c:2661-2723), same operations as
 // coll_time_normal with the tests on the integer pipe
+template <bool ADD = true>
 __device__ __forceinline__ double coll_time_normal_i(const Box& B, const Disk& p1, const Disk& p2,
                                                      double t, bool* overlap) {
   double lat2 = t - p2.tl;
@@ -293,11 +312,25 @@ __device__ __forceinline__ double coll_time_normal_i(const Box& B, const Disk& p
   double b = dx * dvx + dy * dvy;
   if (is_pos(b)) return NEVER;
   double v2 = dvx * dvx + dvy * dvy;
-  double d2 = dx * dx + dy * dy - contact2(B, p1.rad, p2.rad);
+  double d2 = dx * dx + dy * dy - contact2<ADD>(B, p1.rad, p2.rad);
   double det = b * b - v2 * d2;
   if (lt_neg(d2, 0.01)) { *overlap = true; return NEVER; }
   if (is_neg(det)) return NEVER;
   return (-b - sqrt(det)) / v2;
+}
+
+// The approach test of collisionTimeNormal (src/EDMD.c:2683-2697): the same
+// operations as coll_time_normal_i up to b = dr.dv; false exactly when that
+// function returns "never" at its first test (b > 0), before any overlap test.
+__device__ __forceinline__ bool approaching_i(const Box& B, const Disk& p1, const Disk& p2, double t) {
+  double lat2 = t - p2.tl;
+  double dvx = p2.vx - p1.vx;
+  double dvy = p2.vy - p1.vy;
+  double dx = (p2.x + lat2 * p2.vx) - p1.x;
+  double dy = (p2.y + lat2 * p2.vy) - p1.y;
+  pbc_i(B, dx, dy);
+  double b = dx * dvx + dy * dvy;
+  return !is_pos(b);
 }
 
 __device__ __forceinline__ bool key_less(uint32_t b1, uint64_t t1, uint64_t k1, int32_t i1,

@@ -288,10 +288,11 @@ __device__ __forceinline__ void grow_fly(const SysDev& S, Disk& p, int i, double
   if (grow) p.rad += dt * S.vr[i];
 }
 
+template <bool ADD>
 __device__ __forceinline__ double pair_time(const SysDev& S, const Disk& A, int a, const Disk& P,
                                             int p, double t, bool grow, bool* ovl) {
   if (grow) return coll_time_grow(S.B, A, S.vr[a], P, S.vr[p], t, ovl);
-  return coll_time_normal_i(S.B, A, P, t, ovl);
+  return coll_time_normal_i<ADD>(S.B, A, P, t, ovl);
 }
 
 // candidate times compared as their order-preserving integer images: the
@@ -313,7 +314,7 @@ __device__ __forceinline__ void best_merge(uint64_t& bk, int& bo, int& bp, uint3
 // t = 0..8 (a0's cells in scan order) and 9..17 (a1's): task t runs on lane
 // t % GW, a lane with two tasks walks both lists at once.  The candidates are
 // then packed over the group in task order and solved GW at a time.
-template <int GW>
+template <int GW, bool ADD>
 __device__ void predict2(const SysDev& S, SysState& R, int a0, int a1, Pred& r0, Pred& r1,
                          const Grp<GW>& G, WarpSmem* sm, bool* ovl, int* ovl_a, int* ovl_b) {
   const Box& B = S.B;
@@ -403,7 +404,7 @@ __device__ void predict2(const SysDev& S, SysState& R, int a0, int a1, Pred& r0,
       Disk P = S.d[p];
       bool g1 = f >= tot0;
       bool ov = false;
-      double d = pair_time(S, g1 ? A1 : A0, g1 ? a1 : a0, P, p, R.t, grow, &ov);
+      double d = pair_time<ADD>(S, g1 ? A1 : A0, g1 ? a1 : a0, P, p, R.t, grow, &ov);
       if (ov) { lovl = true; la = g1 ? a1 : a0; lb = p; }
       if (g1) best_merge(bd1, bo1, bp1, bc1, cand_key(d), o, p, P.coll);
       else best_merge(bd0, bo0, bp0, bc0, cand_key(d), o, p, P.coll);
@@ -426,7 +427,7 @@ __device__ void predict2(const SysDev& S, SysState& R, int a0, int a1, Pred& r0,
         Disk P = S.d[p];
         if (p != own) {
           bool ov = false;
-          double d = pair_time(S, AA, own, P, p, R.t, grow, &ov);
+          double d = pair_time<ADD>(S, AA, own, P, p, R.t, grow, &ov);
           if (ov) { lovl = true; la = own; lb = p; }
           if (g1) best_merge(bd1, bo1, bp1, bc1, cand_key(d), q * 4096 + k, p, P.coll);
           else best_merge(bd0, bo0, bp0, bc0, cand_key(d), q * 4096 + k, p, P.coll);
@@ -538,7 +539,7 @@ __device__ __noinline__ void do_thermo(const SysDev& S, SysState& R, const Grp<G
 }
 
 // stopGrow (src/EDMD.c:4740-4800)
-template <int GW>
+template <int GW, bool ADD>
 __device__ __noinline__ void do_growstop(const SysDev& S, SysState& R, const Grp<GW>& G, WarpSmem* sm,
                             bool* ovl, int* oa, int* ob) {
   const int lane = G.lane;
@@ -577,7 +578,7 @@ __device__ __noinline__ void do_growstop(const SysDev& S, SysState& R, const Grp
     G.sync();
     unqueue(S, R, N + i, G);
     Pred r0, r1;
-    predict2(S, R, i, -1, r0, r1, G, sm, ovl, oa, ob);
+    predict2<GW, ADD>(S, R, i, -1, r0, r1, G, sm, ovl, oa, ob);
     schedule(S, R, N + i, R.t + r0.dt, r0.partner, r0.ca, 2ull, G);
     unqueue(S, R, i, G);
     int dir;
@@ -616,7 +617,9 @@ __device__ __forceinline__ void gather_virial(SysState& R, double ctl, const Grp
   for (int k = 0; k < 4; k++) R.collT[k] = G.shfl(ctl, k);
 }
 
-template <int GW>
+// ADD = false: a context without additive-contact systems (the rule's
+// switch compiled out of the pair solves and the collision rule)
+template <int GW, bool ADD = true>
 __device__ void run_system(const SysDev& S, const RunArgs& A, int64_t max_coll, const Grp<GW>& G,
                            WarpSmem* sm) {
   const int lane = G.lane;
@@ -742,7 +745,7 @@ __device__ void run_system(const SysDev& S, const RunArgs& A, int64_t max_coll, 
           // dx*dvx on even lanes, dy*dvy on odd lanes, then their sum
           const double pm = ((q4 & 1) ? dy : dx) * ((q4 & 1) ? dvy : dvx);
           double collKernel = invMass * (1 + S.res) * (G.shfl(pm, 0) + G.shfl(pm, 1));
-          double distSquared = contact2(B, di.rad, dj.rad);
+          double distSquared = contact2<ADD>(B, di.rad, dj.rad);
           double f = __double_as_longlong(distSquared) == 0x4010000000000000ll ? collKernel * 0.25
                                                                                 : collKernel / distSquared;
           double ct = di.m * dj.m * f;
@@ -843,7 +846,7 @@ __device__ void run_system(const SysDev& S, const RunArgs& A, int64_t max_coll, 
       se0 = e; sT0 = R.t + S.dtimeTh;
       la = N + SP_THERMO;
     } else {
-      do_growstop(S, R, G, sm, &ovl, &oa, &ob);
+      do_growstop<GW, ADD>(S, R, G, sm, &ovl, &oa, &ob);
       if (A.flags & EDMD_F_STOP_AT_GROW) stop = EDMD_STOP_GROW;
     }
     // the tail shared by the handlers: new crossing events of the one or two
@@ -862,7 +865,7 @@ __device__ void run_system(const SysDev& S, const RunArgs& A, int64_t max_coll, 
     }
     if (pa >= 0) {
       Pred r0, r1;
-      predict2(S, R, pa, pb, r0, r1, G, sm, &ovl, &oa, &ob);
+      predict2<GW, ADD>(S, R, pa, pb, r0, r1, G, sm, &ovl, &oa, &ob);
       const double tn = R.t + ((lane & 1) ? r1.dt : r0.dt);
       se0 = N + pa; sT0 = G.shfl(tn, 0); sj0 = r0.partner; sca0 = r0.ca;
       if (pb >= 0) { se1 = N + pb; sT1 = G.shfl(tn, 1); sj1 = r1.partner; sca1 = r1.ca; }
@@ -890,7 +893,7 @@ __device__ void run_system(const SysDev& S, const RunArgs& A, int64_t max_coll, 
 // Persistent launch: lane groups (GW lanes, one system each) pull systems
 // from a counter, in A.order, and record each system's run time
 // (globaltimer) for the next call's order.
-template <int GW>
+template <int GW, bool ADD = true>
 __global__ void __launch_bounds__(32 * WARPS_PER_BLOCK, 4)
 k_run(const SysDev* __restrict__ sys, RunArgs A) {
   __shared__ WarpSmem smem[WARPS_PER_BLOCK * (32 / GW)];
@@ -904,7 +907,7 @@ k_run(const SysDev* __restrict__ sys, RunArgs A) {
     const int s = A.order ? A.order[it] : it;
     unsigned long long t0 = 0, t1 = 0;
     if (A.cost) asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
-    run_system(sys[s], A, A.max_coll, G, sm);
+    run_system<GW, ADD>(sys[s], A, A.max_coll, G, sm);
     if (A.cost && G.lane == 0) {
       asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t1));
       const unsigned long long c = (t1 - t0) >> 10;
@@ -1278,6 +1281,8 @@ static int stage_all(edmd_ctx* ctx, const double* x, const double* y, const doub
       }
       if (!(px >= 0 && px < D.Lx && py >= 0 && py < D.Ly))
         return set_err(ctx, EDMD_ERR_ARG, "position outside the box (system " + std::to_string(s) + ")");
+      if (!radius_ok(rad[g]))
+        return set_err(ctx, EDMD_ERR_ARG, "radius not zero or normal positive (system " + std::to_string(s) + ")");
       Disk& q = hd[g];
       q.x = px; q.y = py; q.vx = vx[g]; q.vy = vy[g]; q.tl = 0; q.rad = rad[g]; q.m = m[g];
       q.coll = 0;
@@ -1348,6 +1353,7 @@ extern "C" int edmd_create(int32_t nsys, const edmd_system_desc* desc, const dou
     Box& B = S.B;
     B.N = D.N; B.Lx = D.Lx; B.Ly = D.Ly;
     B.additive = D.contact == EDMD_CONTACT_ADDITIVE;
+    if (B.additive) ctx->any_additive = true;
     B.hLx = D.Lx / 2; B.hLy = D.Ly / 2;                      // boxConstantHelper 679-714
     B.Nyc = (int)(B.hLy); B.Nxc = (int)(B.hLx);
     if (B.Nxc < 1 || B.Nyc < 1) return set_err(ctx, EDMD_ERR_ARG, "box smaller than one cell");
@@ -1495,7 +1501,8 @@ static int advance_smem_split(edmd_ctx* ctx, RunArgs A, int kgrid_max, int nsm) 
     const int per_block = WARPS_PER_BLOCK;
     int grid = ((int)rest.size() + per_block - 1) / per_block;
     if (grid > kgrid_max) grid = kgrid_max;
-    k_run<32><<<grid, 32 * WARPS_PER_BLOCK, 0, ctx->stream>>>(ctx->ds, B);
+    if (ctx->any_additive) k_run<32><<<grid, 32 * WARPS_PER_BLOCK, 0, ctx->stream>>>(ctx->ds, B);
+    else k_run<32, false><<<grid, 32 * WARPS_PER_BLOCK, 0, ctx->stream>>>(ctx->ds, B);
     CK(cudaGetLastError());
   }
   if (!fit.empty()) CK(cudaStreamWaitEvent(ctx->stream, ctx->e2, 0));
@@ -1558,7 +1565,8 @@ extern "C" int edmd_advance(edmd_ctx* ctx, int64_t max_coll, double t_stop, uint
     if (gw == 4) k_run<4><<<grid, 32 * WARPS_PER_BLOCK, 0, ctx->stream>>>(ctx->ds, A);
     else if (gw == 8) k_run<8><<<grid, 32 * WARPS_PER_BLOCK, 0, ctx->stream>>>(ctx->ds, A);
     else if (gw == 16) k_run<16><<<grid, 32 * WARPS_PER_BLOCK, 0, ctx->stream>>>(ctx->ds, A);
-    else k_run<32><<<grid, 32 * WARPS_PER_BLOCK, 0, ctx->stream>>>(ctx->ds, A);
+    else if (ctx->any_additive) k_run<32><<<grid, 32 * WARPS_PER_BLOCK, 0, ctx->stream>>>(ctx->ds, A);
+    else k_run<32, false><<<grid, 32 * WARPS_PER_BLOCK, 0, ctx->stream>>>(ctx->ds, A);
     }
   }
   CK(cudaGetLastError());
@@ -1758,8 +1766,9 @@ __global__ void k_noalloc_put(SysDev s, SysDev* dst) {
 
 // disk records, cell lists (index order, push-front as addToCell) and the
 // scalar state from the caller's device arrays; one thread, N <= 8192.
-// A position outside [0, Lx) x [0, Ly) (or a NaN) is an argument error, as in
-// edmd_create: the scalar state gets status EDMD_ERR_ARG with the first such
+// A position outside [0, Lx) x [0, Ly) (or a NaN), or a radius that is not
+// zero or normal positive, is an argument error, as in edmd_create: the
+// scalar state gets status EDMD_ERR_ARG with the first such
 // disk in err_a, the event loop then does nothing, and the host reports it.
 // The cell index is still clamped into the grid so that the initial
 // predictions that run before the loop stay inside the arrays.
@@ -1776,7 +1785,7 @@ __global__ void k_noalloc_stage(const SysDev* __restrict__ sys, const double* x,
     Disk q;
     q.x = x[i]; q.y = y[i]; q.vx = vx[i]; q.vy = vy[i]; q.tl = 0; q.rad = rad[i]; q.m = m[i];
     q.coll = 0;
-    if (bad < 0 && !(q.x >= 0 && q.x < B.Lx && q.y >= 0 && q.y < B.Ly)) bad = i;
+    if (bad < 0 && !(q.x >= 0 && q.x < B.Lx && q.y >= 0 && q.y < B.Ly && radius_ok(q.rad))) bad = i;
     int X = (int)(q.x * B.cxf), Y = (int)(q.y * B.cyf);
     if (!(X < B.Nxc)) X = B.Nxc - 1;
     if (!(Y < B.Nyc)) Y = B.Nyc - 1;
@@ -1900,7 +1909,8 @@ extern "C" int edmd_run_noalloc(const edmd_system_desc* desc, double* x, double*
   k_tree_build<<<1, 256, 0, st>>>(dsys, 1);
   if (cudaMemsetAsync(work, 0, sizeof(int32_t), st) != cudaSuccess)
     return noalloc_fail(EDMD_ERR_CUDA, "edmd_run_noalloc: memset failed");
-  k_run<32><<<1, 32 * WARPS_PER_BLOCK, 0, st>>>(dsys, A);
+  if (B.additive) k_run<32><<<1, 32 * WARPS_PER_BLOCK, 0, st>>>(dsys, A);
+  else k_run<32, false><<<1, 32 * WARPS_PER_BLOCK, 0, st>>>(dsys, A);
   k_sync<<<1, 256, 0, st>>>(dsys, 1);
   k_noalloc_out<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(dsys, x, y, vx, vy);
   cudaError_t ce = cudaGetLastError();

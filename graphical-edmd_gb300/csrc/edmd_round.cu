@@ -332,11 +332,20 @@ __global__ void k_round_begin(RoundArgs A) {
 }
 
 __device__ __forceinline__ int wrapi(int v, int n) {
+  if (v >= 0 && v < n) return v;          // inside: the common case, no division
+  if (v < 0 && v + n >= 0) return v + n;  // one period off (tiles of systems wider than a tile)
+  if (v >= n && v - n < n) return v - n;
   v %= n;
   return v < 0 ? v + n : v;
 }
 
-// window minima of one tile in shared memory and selection of its events
+size_t select_smem(int r);
+
+// window minima of one tile in shared memory and selection of its events.
+// RC > 0: the window radius as a compile-time constant (the radii the exact
+// mode uses), so that the tile's index arithmetic has no division and the
+// window loops unroll; RC = 0 reads it from the call.
+template <int RC>
 __global__ void __launch_bounds__(TX * TY) k_select(const SysDev* __restrict__ sys, RoundArgs A) {
   extern __shared__ unsigned char smem[];
   for (int t = blockIdx.x; t < A.ntiles; t += gridDim.x) {
@@ -346,7 +355,7 @@ __global__ void __launch_bounds__(TX * TY) k_select(const SysDev* __restrict__ s
   const Box& B = sys[s].B;
   const int Nxc = B.Nxc, Nyc = B.Nyc;
   const int x0 = A.tx0[t], y0 = A.ty0[t];
-  const int r = A.radius, H = r + 1;
+  const int r = RC > 0 ? RC : A.radius, H = r + 1;
   const int CW = TX + 2 * H, CH = TY + 2 * H;    // cell minima, halo H
   const int HW = TX + 2;                          // horizontal minima: cols -1..TX
   uint64_t* ck = (uint64_t*)smem;
@@ -369,6 +378,7 @@ __global__ void __launch_bounds__(TX * TY) k_select(const SysDev* __restrict__ s
     const int lx = hx - 1 + H;
     uint64_t bk = KINF;
     int32_t bi = IINF;
+#pragma unroll
     for (int d = -r; d <= r; d++) {
       const int o = ly * CW + lx + d;
       if (pair_less(ck[o], ci[o], bk, bi)) { bk = ck[o]; bi = ci[o]; }
@@ -382,6 +392,7 @@ __global__ void __launch_bounds__(TX * TY) k_select(const SysDev* __restrict__ s
     const int ly = wy - 1 + H;
     uint64_t bk = KINF;
     int32_t bi = IINF;
+#pragma unroll
     for (int d = -r; d <= r; d++) {
       const int o = (ly + d) * HW + wx;
       if (pair_less(hk[o], hi[o], bk, bi)) { bk = hk[o]; bi = hi[o]; }
@@ -1218,16 +1229,54 @@ __device__ void recompute_cell(const SysDev& S, const RoundArgs& A, int64_t base
   }
 }
 
-// the cells whose minimum the selected events can have changed, one warp each
+// minimum (key, id) of the events on list q of the 3x3 block around local
+// cell c that are attributed to c (the walk of recompute_cell for one list)
+__device__ __forceinline__ void list_min(const SysDev& S, const RoundArgs& A, int64_t dbase, int c, int q,
+                                         uint64_t& bk, int32_t& bi) {
+  const Box& B = S.B;
+  const int x = c % B.Nxc, y = c / B.Nxc;
+  int p = S.head[pbc_cy(B, y + q / 3 - 1) * B.Nxc + pbc_cx(B, x + q % 3 - 1)];
+  int guard = 0;
+  while (p != NIL && guard++ < B.N) {
+    const int64_t g = dbase + p;
+    const uint64_t k = A.dkey[g];
+    if (k != KINF && (A.fc[2 * g] == c || A.fc[2 * g + 1] == c) && pair_less(k, A.dpk[g], bk, bi)) {
+      bk = k;
+      bi = A.dpk[g];
+    }
+    p = S.d[p].nxt;
+  }
+}
+
+// the cells whose minimum the selected events can have changed: four cells
+// per warp, one 8-lane group each (lane q walks list q of the 3x3 block,
+// lane 0 also list 8), the same minima as recompute_cell
 __global__ void __launch_bounds__(256) k_recompute(const SysDev* __restrict__ sys, RoundArgs A) {
-  const int lane = threadIdx.x & 31;
+  const int lane = threadIdx.x & 31, grp = lane >> 3, q = lane & 7;
   const int64_t total = (int64_t)(*A.nsafe) * MAXDIRTY;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < total; w += nwarps) {
-    const int32_t gc = A.dcell[w];
-    if (gc < 0) continue;
-    const int s = A.dsys[A.safe[w / MAXDIRTY]];
-    recompute_cell(sys[s], A, A.coff[s], A.doff[s], gc, lane);
+  for (int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w * 4 < total; w += nwarps) {
+    const int64_t item = w * 4 + grp;
+    const int32_t gc = item < total ? A.dcell[item] : -1;
+    uint64_t bk = KINF;
+    int32_t bi = IINF;
+    if (gc >= 0) {
+      const int s = A.dsys[A.safe[item / MAXDIRTY]];
+      const SysDev& S = sys[s];
+      const int c = (int)(gc - A.coff[s]);
+      const int64_t dbase = A.doff[s];
+      list_min(S, A, dbase, c, q, bk, bi);
+      if (q == 0) list_min(S, A, dbase, c, 8, bk, bi);
+    }
+    for (int o = 4; o > 0; o >>= 1) {
+      const uint64_t k2 = __shfl_xor_sync(FULLM, bk, o);
+      const int32_t i2 = __shfl_xor_sync(FULLM, bi, o);
+      if (pair_less(k2, i2, bk, bi)) { bk = k2; bi = i2; }
+    }
+    if (gc >= 0 && q == 0) {
+      A.cmt[gc] = bk;
+      A.cmi[gc] = bi;
+    }
   }
 }
 
@@ -1540,6 +1589,14 @@ int round_init(edmd_ctx* ctx) {
   CK(sync_copy(ctx, R->tx0, tx0.data(), R->ntiles * 4, cudaMemcpyHostToDevice));
   CK(sync_copy(ctx, R->ty0, ty0.data(), R->ntiles * 4, cudaMemcpyHostToDevice));
   CK(sync_set(ctx, R->selflag, 0, ctx->nsys * 4));
+  // the selection tile of the widest window (radius 12) needs more than the
+  // default 48 KB of dynamic shared memory
+  const int sbmax = (int)select_smem(RTILE);
+  CK(cudaFuncSetAttribute(k_select<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, sbmax));
+  CK(cudaFuncSetAttribute(k_select<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, sbmax));
+  CK(cudaFuncSetAttribute(k_select<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, sbmax));
+  CK(cudaFuncSetAttribute(k_select<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, sbmax));
+  CK(cudaFuncSetAttribute(k_select<12>, cudaFuncAttributeMaxDynamicSharedMemorySize, sbmax));
   k_round_setup<<<dim3(64, ctx->nsys), 256, 0, ctx->stream>>>(R->doff, ctx->ds, R->dsys);
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(ctx->stream));
@@ -1556,7 +1613,14 @@ cudaError_t enqueue_round(edmd_ctx* ctx, const RoundBufs* R, const RoundArgs& A,
   cudaStream_t st = ctx->stream;
   k_round_begin<<<1, 1, 0, st>>>(A);
   const unsigned tgrid = (unsigned)(R->ntiles < nsm * 8 ? R->ntiles : nsm * 8);
-  k_select<<<tgrid, TX * TY, select_smem(A.radius), st>>>(ctx->ds, A);
+  const size_t sb = select_smem(A.radius);
+  switch (A.radius) {
+    case 3: k_select<3><<<tgrid, TX * TY, sb, st>>>(ctx->ds, A); break;
+    case 4: k_select<4><<<tgrid, TX * TY, sb, st>>>(ctx->ds, A); break;
+    case 8: k_select<8><<<tgrid, TX * TY, sb, st>>>(ctx->ds, A); break;
+    case 12: k_select<12><<<tgrid, TX * TY, sb, st>>>(ctx->ds, A); break;
+    default: k_select<0><<<tgrid, TX * TY, sb, st>>>(ctx->ds, A); break;
+  }
   k_process<<<nsm * 16, 32 * WPB, 0, st>>>(ctx->ds, A);
   k_process_thread<<<nsm * 8, 128, 0, st>>>(ctx->ds, A);
   k_recompute<<<nsm * 8, 256, 0, st>>>(ctx->ds, A);

@@ -13,7 +13,20 @@
  * ending in 'p').  Added: --hex (triangular-lattice start, the reference's
  * Hex = 1 global), --max-coll n (stop after n accepted collisions),
  * --quiet, --additive (contact distance r1 + r2: the reference built with
- * NONADDITIVE 1, src/EDMD.c:35-43).
+ * NONADDITIVE 1, src/EDMD.c:35-43), --engine auto|warp|round.
+ *
+ * Engines.  "warp" runs every phase in the serial-exact engine, which makes
+ * the thermo rows itself.  "round" runs the growth phase there and the
+ * constant-radius phase in the round-parallel engine (edmd_advance_rounds,
+ * exact mode), which stops at each screenshot and thermo time; the rows are
+ * then computed here from the state and the collision virial with the same
+ * operations in the same order.  Positions, velocities, collision counts and
+ * dump files are the same as the serial engine's; the virial sums of a round
+ * are added in another order, so a pressure term can differ in its last
+ * bits (about 1e-16 relative), far below the printed digits.  Past tmax the
+ * round call may process a few more disk events than the serial loop's one
+ * (no file records them; only the final counters printed to stdout see
+ * them).  "auto" takes rounds from ROUND_MIN_N disks.
  */
 #include "../../include/edmd_gpu.h"
 #include "../../include/edmd_host.h"
@@ -30,8 +43,12 @@
 typedef struct {
 	int N; double phi, xs, q, aspect, tmax, dtime, dtimeThermo, Einit, res;
 	unsigned seed; int version; int hex; int load; char loadfile[512];
-	long long max_coll; int quiet; int additive;
+	long long max_coll; int quiet; int additive; int engine;
 } opts;
+
+enum { ENG_AUTO = 0, ENG_WARP = 1, ENG_ROUND = 2 };
+/* --engine auto runs the constant-radius phase in rounds from this many disks */
+#define ROUND_MIN_N 1000
 
 static void die(const char* m, edmd_ctx* c)
 {
@@ -127,16 +144,140 @@ static int load_dump(const char* fn, double** arr, int32_t** type, double* Lx, d
 	return N;
 }
 
+/* one saveThermo row (EDMD.c:5409-5577 with Nthermo = 1) */
+static void put_row(FILE* f, const double* r)
+{
+	fprintf(f, "%lf ", r[0]);
+	fprintf(f, "%ld ", (long)r[1]);
+	fprintf(f, "%lf ", r[2]);
+	fprintf(f, "%lf %lf %lf %.10lf %.10lf ", r[3], r[4], r[5], r[6], r[7]);
+	fprintf(f, "%lf ", r[8]);
+	fprintf(f, "\n");
+}
+
+/* one frame of saveTXT (EDMD.c:5012-5153), as takeAScreenshot writes it */
+static void put_frame(FILE* f, double t, int N, double Lx, double Ly, const int32_t* type, const double* x,
+                      const double* y, const double* vx, const double* vy, const double* rad, const double* m)
+{
+	fprintf(f, "ITEM: TIMESTEP\n%lf\nITEM: NUMBER OF ATOMS\n%d\nITEM: BOX BOUNDS pp pp pp\n"
+	           "0 %lf\n0 %lf\n0 0\nITEM: ATOMS id type x y vx vy radius m coll", t, N, Lx, Ly);
+	fprintf(f, "\n");
+	for (int i = 0; i < N; i++) {
+		fprintf(f, "%d %d %.3lf %lf %lf %lf %lf %lf %d", i, type[i], x[i], y[i], vx[i], vy[i], rad[i], m[i], type[i]);
+		fprintf(f, "\n");
+	}
+	fflush(f);
+}
+
+/* takeAThermo + physicalQ + saveThermo (EDMD.c:4679-4705, 5968-6013,
+ * 5232-5697 with Nthermo = 1) at time t: the operations of the serial
+ * engines' in-kernel rows, in the same order (sums over disks in index
+ * order).  collT holds collTermX, Y, XY, YX since the previous row; *last is
+ * lastScreen, the time of the previous row (0 before the first). */
+static void thermo_row(double* row, double t, double* last, uint64_t ncol, int N, double Lx, double Ly,
+                       const double* vx, const double* vy, const double* m, const double collT[4])
+{
+	double E = 0;
+	for (int i = 0; i < N; i++) {
+		double v = vx[i];
+		E += 0.5 * m[i] * (v * v + vy[i] * vy[i]);
+	}
+	double area = Lx * Ly;
+	double dT = t - *last;
+	*last = t;
+	double e4[4] = {0, 0, 0, 0};
+	for (int i = 0; i < N; i++) {
+		e4[0] += m[i] * vx[i] * vx[i];
+		e4[1] += m[i] * vy[i] * vy[i];
+		e4[2] += m[i] * vx[i] * vy[i];
+		e4[3] += m[i] * vy[i] * vx[i];
+	}
+	row[0] = t;
+	row[1] = (double)ncol;
+	row[2] = E / N;
+	for (int k = 0; k < 4; k++) row[4 + k] = -1 * collT[k] / (area * dT) + e4[k] / area;
+	row[3] = (-1 / (dT)) * (collT[0] + collT[1]) / (2 * area) + E / area;
+	double vxa = 0;
+	for (int i = 0; i < N; i++) vxa += vx[i];
+	vxa /= N;
+	double v2 = 0, v4 = 0;
+	for (int i = 0; i < N; i++) {
+		double dd = vx[i] - vxa;
+		double d2 = dd * dd;
+		v2 += d2;
+		v4 += d2 * d2;
+	}
+	v2 /= N;
+	v4 /= N;
+	row[8] = (v2 > 0.0) ? v4 / (3.0 * v2 * v2) - 1.0 : 0.0;
+}
+
+/* The constant-radius phase in the round-parallel engine: advance to each
+ * screenshot or thermo time in turn (screenshot times firstScreen + k dtime,
+ * thermo times firstThermo + 1e-9 + k dtimeThermo, accumulated by repeated
+ * addition as addEventThermo / takeAScreenshot do) and write the frame or
+ * the row there.  The serial loop ends after the first event later than
+ * tmax; when that event is a screenshot or thermo event, its frame or row
+ * is written here too. */
+static edmd_counters round_phase(edmd_ctx* ctx, const edmd_system_desc* d, const opts* o, int N, double Lx,
+                                 double Ly, const int32_t* type, long long coll_left, uint64_t ncol_seen,
+                                 FILE* dump, FILE* thermo, double* sx, double* sy, double* svx, double* svy,
+                                 double* srad, double* sm)
+{
+	double ts = d->first_screen, tt = d->first_thermo + 0.000000001, last_th = 0;
+	double tend = nextafter(d->tmax, INFINITY);
+	edmd_counters cnt;
+	for (;;) {
+		int th = tt < ts;                               /* the thermo time comes first */
+		double tb = th ? tt : nextafter(ts, INFINITY);  /* a screenshot is passed, then the call stops */
+		int64_t nr = 0, nv = 0;
+		int last = tb > tend;
+		/* after tmax: finish the events at or before it; the first event
+		 * after it is the loop's last (while (t <= tmax), EDMD.c:523) */
+		int rc = edmd_advance_rounds(ctx, coll_left, last ? tend : tb, EDMD_F_EXACT, 4, (int64_t)1 << 60, NULL,
+		                             &nr, &nv);
+		if (rc != EDMD_OK) die("round advance failed", ctx);
+		edmd_get_counters(ctx, 0, &cnt);
+		coll_left -= (long long)(cnt.ncol_total - ncol_seen);
+		ncol_seen = cnt.ncol_total;
+		if (cnt.stop_reason == EDMD_STOP_COLL || coll_left <= 0) break;
+		if (last) {
+			/* is the barrier that first event?  Only if no disk event comes before it */
+			uint64_t ev0 = cnt.ncol + cnt.ncross + cnt.nstale;
+			rc = edmd_advance_rounds(ctx, coll_left, tb, EDMD_F_EXACT, 4, (int64_t)1 << 60, NULL, &nr, &nv);
+			if (rc != EDMD_OK) die("round advance failed", ctx);
+			edmd_get_counters(ctx, 0, &cnt);
+			if (cnt.ncol + cnt.ncross + cnt.nstale != ev0) break;
+		}
+		if (th) {
+			double collT[4], row[9];
+			edmd_get_state(ctx, 0, NULL, NULL, svx, svy, NULL, sm, NULL, NULL);
+			edmd_get_virial(ctx, 0, collT, 1);
+			thermo_row(row, tt, &last_th, cnt.ncol, N, Lx, Ly, svx, svy, sm, collT);
+			put_row(thermo, row);
+			fflush(thermo);
+			tt = tt + o->dtimeThermo;
+		} else {
+			edmd_get_state(ctx, 0, sx, sy, svx, svy, srad, sm, NULL, NULL);
+			put_frame(dump, ts, N, Lx, Ly, type, sx, sy, svx, svy, srad, sm);
+			if (!o->quiet) printf("\rt = %.2e / %.2e  ncol = %.2e", ts, o->tmax, (double)cnt.ncol);
+			ts = ts + o->dtime;
+		}
+		if (last) break;
+	}
+	return cnt;
+}
+
 int main(int argc, char* argv[])
 {
-	opts o = {500, 0.38, 0.3, 0.4, 1.0, 4000, 100, 100, 1, 1, 0, 1, 0, 0, "", -1, 0, 0};
+	opts o = {500, 0.38, 0.3, 0.4, 1.0, 4000, 100, 100, 1, 1, 0, 1, 0, 0, "", -1, 0, 0, ENG_AUTO};
 	int seeded = 0;
 	static struct option lo[] = {
 		{"load", 1, 0, 'l'}, {"number", 1, 0, 'N'}, {"phi", 1, 0, 'p'}, {"res", 1, 0, 'r'},
 		{"time", 1, 0, 't'}, {"dt", 1, 0, 'D'}, {"initial-energy", 1, 0, 'E'}, {"xs", 1, 0, 'x'},
 		{"sizeratio", 1, 0, 'q'}, {"aspect", 1, 0, 'a'}, {"dtimeThermo", 1, 0, 'o'},
 		{"version", 1, 0, 'v'}, {"hex", 0, 0, 1000}, {"max-coll", 1, 0, 1001}, {"quiet", 0, 0, 1002},
-		{"additive", 0, 0, 1003}, {0, 0, 0, 0}};
+		{"additive", 0, 0, 1003}, {"engine", 1, 0, 1004}, {0, 0, 0, 0}};
 	int c;
 	while ((c = getopt_long(argc, argv, "l:N:p:r:t:D:E:x:q:a:o:v:", lo, NULL)) != -1) {
 		switch (c) {
@@ -161,6 +302,12 @@ int main(int argc, char* argv[])
 		case 1001: o.max_coll = atoll(optarg); break;
 		case 1002: o.quiet = 1; break;
 		case 1003: o.additive = 1; break;
+		case 1004:
+			if (strcmp(optarg, "auto") == 0) o.engine = ENG_AUTO;
+			else if (strcmp(optarg, "warp") == 0) o.engine = ENG_WARP;
+			else if (strcmp(optarg, "round") == 0) o.engine = ENG_ROUND;
+			else { fprintf(stderr, "edmd: --engine auto|warp|round\n"); return 1; }
+			break;
 		default: fprintf(stderr, "edmd: unknown option\n"); return 1;
 		}
 	}
@@ -226,53 +373,47 @@ int main(int argc, char* argv[])
 	if (!dump || !thermo) die("cannot open output files", NULL);
 	fprintf(thermo, "t Ncol E p px py pxy pyx a2 \n");    /* initThermo 1220-1290 */
 
-	/* ---- main loop: advance to each screenshot, dump, repeat (EDMD.c:523-618) */
+	/* ---- main loop (EDMD.c:523-618) */
 	double* sx = malloc(N * 8), *sy = malloc(N * 8), *svx = malloc(N * 8), *svy = malloc(N * 8);
 	double* srad = malloc(N * 8), *sm = malloc(N * 8);
 	static double rows[9 * 1024];
-	int32_t rows_done = 0;
 	long long coll_left = o.max_coll < 0 ? (long long)4e18 : o.max_coll;
 	uint64_t ncol_seen = 0;
-	for (;;) {
-		rc = edmd_advance(ctx, coll_left, INFINITY, EDMD_F_STOP_AT_SCREEN, (int64_t)1 << 60, NULL);
+	int rounds = o.engine == ENG_ROUND || (o.engine == ENG_AUTO && N >= ROUND_MIN_N);
+	if ((int)(Lx / 2) < 3 || (int)(Ly / 2) < 3) rounds = 0;  /* the round engine needs 3x3 cells */
+	edmd_counters cnt;
+	memset(&cnt, 0, sizeof cnt);
+	/* serial engine: every phase, or the growth phase before the rounds.
+	 * Each call stops at a screenshot, at the growth stop (before rounds),
+	 * or after at most 1000 thermo periods, so the 1024-row buffer the
+	 * engine keeps per system never overflows between drains. */
+	int growing = vr_base > 0 && !o.load;
+	for (; !rounds || growing;) {
+		double tchunk = o.dtimeThermo > 0 ? cnt.t + 1000 * o.dtimeThermo : INFINITY;
+		uint32_t fl = EDMD_F_STOP_AT_SCREEN | (rounds ? EDMD_F_STOP_AT_GROW : 0);
+		rc = edmd_advance(ctx, coll_left, tchunk, fl, (int64_t)1 << 60, NULL);
 		if (rc != EDMD_OK) die("advance failed", ctx);
-		edmd_counters cnt;
 		edmd_get_counters(ctx, 0, &cnt);
 		coll_left -= (long long)(cnt.ncol_total - ncol_seen);
 		ncol_seen = cnt.ncol_total;
-		/* thermo rows produced so far (saveThermo row format, 5409-5577) */
 		int32_t nr = 0;
-		edmd_get_thermo(ctx, 0, rows, 1024, &nr);
-		if (nr > 1024) nr = 1024;
-		for (; rows_done < nr; rows_done++) {
-			double* r = rows + 9 * rows_done;
-			fprintf(thermo, "%lf ", r[0]);
-			fprintf(thermo, "%ld ", (long)r[1]);
-			fprintf(thermo, "%lf ", r[2]);
-			fprintf(thermo, "%lf %lf %lf %.10lf %.10lf ", r[3], r[4], r[5], r[6], r[7]);
-			fprintf(thermo, "%lf ", r[8]);
-			fprintf(thermo, "\n");
-		}
+		rc = edmd_take_thermo(ctx, 0, rows, 1024, &nr);
+		if (rc != EDMD_OK) die("thermo rows", ctx);
+		for (int k = 0; k < nr; k++) put_row(thermo, rows + 9 * k);
 		fflush(thermo);
-		if (cnt.stop_reason == EDMD_STOP_SCREEN) {          /* takeAScreenshot -> saveTXT */
+		if (cnt.stop_reason == EDMD_STOP_SCREEN) {
 			edmd_get_state(ctx, 0, sx, sy, svx, svy, srad, sm, NULL, NULL);
-			fprintf(dump, "ITEM: TIMESTEP\n%lf\nITEM: NUMBER OF ATOMS\n%d\nITEM: BOX BOUNDS pp pp pp\n"
-			              "0 %lf\n0 %lf\n0 0\nITEM: ATOMS id type x y vx vy radius m coll", cnt.t, N, Lx, Ly);
-			fprintf(dump, "\n");
-			for (int i = 0; i < N; i++) {
-				fprintf(dump, "%d %d %.3lf %lf %lf %lf %lf %lf %d", i, type[i], sx[i], sy[i], svx[i], svy[i],
-				        srad[i], sm[i], type[i]);
-				fprintf(dump, "\n");
-			}
-			fflush(dump);
+			put_frame(dump, cnt.t, N, Lx, Ly, type, sx, sy, svx, svy, srad, sm);
 			if (!o.quiet)
 				printf("\rt = %.2e / %.2e  ncol = %.2e", cnt.t, o.tmax, (double)cnt.ncol);
 			if (coll_left > 0) continue;
 		}
-		break;   /* t > tmax or the collision budget is spent */
+		if (cnt.stop_reason == EDMD_STOP_TIME && coll_left > 0) continue;
+		break;   /* t > tmax, the growth stop (rounds follow) or the collision budget is spent */
 	}
-	edmd_counters cnt;
-	edmd_get_counters(ctx, 0, &cnt);
+	if (rounds && coll_left > 0 && (!growing || cnt.stop_reason == EDMD_STOP_GROW))
+		cnt = round_phase(ctx, &d, &o, N, Lx, Ly, type, coll_left, ncol_seen, dump, thermo,
+		                  sx, sy, svx, svy, srad, sm);
 	if (!o.quiet) printf("\rt = %.2e  ncol = %lu  ncross = %lu\n", cnt.t, (unsigned long)cnt.ncol, (unsigned long)cnt.ncross);
 	fclose(dump);
 	fclose(thermo);

@@ -132,7 +132,8 @@ typedef struct edmd_ctx edmd_ctx;
 /* Create `nsys` systems (replaces particlesInit's hand-off, cellListInit
  * src/EDMD.c:1906 and eventListInit src/EDMD.c:1935).  Arrays hold the sum
  * of desc[k].N entries.  `vr` (growth rate per disk) may be NULL for direct
- * starts.  Positions must lie in [0,L).  trace_cap is the per-system
+ * starts.  Positions must lie in [0,L); radii must be zero or normal
+ * positive below 2^1020 (EDMD_ERR_ARG otherwise).  trace_cap is the per-system
  * capacity of the collision trace (0 disables tracing).  *out is set even when
  * the call fails, so that edmd_last_error can be read; destroy it either way. */
 int edmd_create(int32_t nsys, const edmd_system_desc* desc,
@@ -322,8 +323,9 @@ int edmd_host_free(void* p);
  * entries; the call starts the system from them directly, exactly as
  * edmd_create with vr = NULL does: t = 0, normal phase, first screenshot and
  * thermo events at desc->first_screen and desc->first_thermo, positions used
- * as given (no periodic wrap; a position outside [0, Lx) x [0, Ly) returns
- * EDMD_ERR_ARG naming the disk).  It runs until max_coll accepted
+ * as given (no periodic wrap; a position outside [0, Lx) x [0, Ly), or a
+ * radius that is not zero or normal positive below 2^1020, returns
+ * EDMD_ERR_ARG naming the disk, as edmd_create does).  It runs until max_coll accepted
  * collisions, t_stop or desc->tmax, free-flies every disk to the final time
  * and writes x, y, vx, vy back.  ncol_out / t_out (host, may be NULL) receive
  * the collisions run and the final time.  `stream` is a cudaStream_t (NULL:

@@ -77,3 +77,17 @@ def test_round_budget_of_one(edmd):
     # rounds run in graph-captured groups: the budget stops at the first group
     assert rounds >= 1 and 0 < eng.counters(0)["ncol"] < 10 ** 6
     eng.close()
+
+
+@pytest.mark.parametrize("bad", [-1.0, 1e-310, float("nan"), float("inf")])
+def test_invalid_radius_is_an_argument_error(edmd, bad):
+    """Radii must be zero or normal positive: the contact distance takes 4 r
+    exactly on the integer pipe, which holds for those."""
+    s = edmd.hex_start(256, 0.30, 4)
+    s["desc"] = edmd.default_desc(s["N"], s["Lx"], s["Ly"])
+    s["rad"] = s["rad"].copy()
+    s["rad"][17] = bad
+    with pytest.raises(edmd.EngineError) as ei:
+        edmd.Engine([s])
+    assert ei.value.code == edmd.ERR_ARG
+    assert "radius" in str(ei.value)
