@@ -326,10 +326,6 @@ __global__ void k_limits(const SysDev* __restrict__ sys, RoundArgs A) {
 
 // ---------------------------------------------------------------- per round
 
-__global__ void k_round_begin(RoundArgs A) {
-  *A.nsafe = 0;
-  *A.active = 0;
-}
 
 __device__ __forceinline__ int wrapi(int v, int n) {
   if (v >= 0 && v < n) return v;          // inside: the common case, no division
@@ -339,15 +335,71 @@ __device__ __forceinline__ int wrapi(int v, int n) {
   return v < 0 ? v + n : v;
 }
 
-size_t select_smem(int r);
+// (time key, event id) as one 96-bit value in a 128-bit word: the unsigned
+// order of the word is the lexicographic order pair_less uses (ids are
+// non-negative), so a window minimum is one compare-and-select per element
+typedef unsigned __int128 kid_t;
+__device__ __forceinline__ kid_t kid(uint64_t k, int32_t id) { return ((kid_t)k << 32) | (uint32_t)id; }
+__device__ __forceinline__ kid_t kid_min(kid_t a, kid_t b) { return b < a ? b : a; }
 
-// window minima of one tile in shared memory and selection of its events.
-// RC > 0: the window radius as a compile-time constant (the radii the exact
-// mode uses), so that the tile's index arithmetic has no division and the
-// window loops unroll; RC = 0 reads it from the call.
-template <int RC>
-__global__ void __launch_bounds__(TX * TY) k_select(const SysDev* __restrict__ sys, RoundArgs A) {
-  extern __shared__ unsigned char smem[];
+// Window minima of S consecutive positions: out[k] = min(a[k .. k+W-1]).
+// The W-S+1 middle elements are common to all S windows; each window adds a
+// suffix of the left part and a prefix of the right part (a van Herk /
+// Gil-Werman block): W + 2S - 4 compares instead of S (W - 1).
+template <int S, int W>
+__device__ __forceinline__ void block_window_min(const kid_t (&a)[S + W - 1], kid_t (&out)[S]) {
+  static_assert(W >= S, "window narrower than the block");
+  kid_t c = a[S - 1];
+#pragma unroll
+  for (int j = S; j < W; j++) c = kid_min(c, a[j]);
+  if constexpr (S == 1) {
+    out[0] = c;
+    return;
+  }
+  kid_t rp[S];
+  rp[0] = c;
+#pragma unroll
+  for (int k = 1; k < S; k++) rp[k] = kid_min(rp[k - 1], a[W + k - 1]);
+  out[S - 1] = rp[S - 1];
+  if constexpr (S > 1) {
+    kid_t ls = a[S - 2];
+#pragma unroll
+    for (int k = S - 2; k >= 0; k--) {
+      if (k < S - 2) ls = kid_min(ls, a[k]);
+      out[k] = kid_min(ls, rp[k]);
+    }
+  }
+}
+
+// tile geometry of the selection for window radius R: cell minima with a
+// halo, horizontal minima of rows, window minima (padded so that every block
+// of SB outputs reads in range; the padding's outputs are never used)
+template <int R>
+struct SelGeom {
+  // two outputs per thread: measured best of 1, 2 and 4 (fewer compares per
+  // output against idle threads at the tile's barriers)
+  static constexpr int H = R + 1, W = 2 * R + 1, SB = 2;
+  static constexpr int HW = TX + 2;                    // outputs per row: columns -1..TX
+  static constexpr int NHB = (HW + SB - 1) / SB;
+  static constexpr int CW = NHB * SB + W - 1;          // input columns
+  static constexpr int VR = TY + 2;                    // outputs per column: rows -1..TY
+  static constexpr int NVB = (VR + SB - 1) / SB;
+  static constexpr int CH = NVB * SB + W - 1;          // rows of cell and horizontal minima
+  static constexpr size_t bytes = (size_t)(CH * CW + CH * HW + NVB * SB * HW) * sizeof(kid_t);
+};
+
+// Window minima of one tile in shared memory and selection of its events;
+// the window radius R is a compile-time constant (3..12).
+template <int R>
+__global__ void __launch_bounds__(TX * TY, 4) k_select(const SysDev* __restrict__ sys, RoundArgs A) {
+  using G = SelGeom<R>;
+  constexpr int H = G::H, W = G::W, SB = G::SB, HW = G::HW, CW = G::CW, CH = G::CH;
+  extern __shared__ kid_t sel_smem[];
+  // the round's count of running systems is rebuilt by k_barrier
+  if (blockIdx.x == 0 && threadIdx.x == 0) *A.active = 0;
+  kid_t* ck = sel_smem;                // CH x CW
+  kid_t* hk = ck + CH * CW;            // CH x HW
+  kid_t* wk = hk + CH * HW;            // NVB*SB x HW
   for (int t = blockIdx.x; t < A.ntiles; t += gridDim.x) {
   const int s = A.tsys[t];
   const uint64_t lim = A.lim[s];
@@ -355,50 +407,43 @@ __global__ void __launch_bounds__(TX * TY) k_select(const SysDev* __restrict__ s
   const Box& B = sys[s].B;
   const int Nxc = B.Nxc, Nyc = B.Nyc;
   const int x0 = A.tx0[t], y0 = A.ty0[t];
-  const int r = RC > 0 ? RC : A.radius, H = r + 1;
-  const int CW = TX + 2 * H, CH = TY + 2 * H;    // cell minima, halo H
-  const int HW = TX + 2;                          // horizontal minima: cols -1..TX
-  uint64_t* ck = (uint64_t*)smem;
-  uint64_t* hk = ck + CW * CH;
-  uint64_t* wk = hk + HW * CH;
-  int32_t* ci = (int32_t*)(wk + HW * (TY + 2));
-  int32_t* hi = ci + CW * CH;
-  int32_t* wi = hi + HW * CH;
   const int64_t base = A.coff[s];
-  for (int q = threadIdx.x; q < CW * CH; q += blockDim.x) {
-    const int lx = q % CW, ly = q / CW;
-    const int gx = wrapi(x0 + lx - H, Nxc), gy = wrapi(y0 + ly - H, Nyc);
-    const int64_t c = base + (int64_t)gy * Nxc + gx;
-    ck[q] = A.cmt[c];
-    ci[q] = A.cmi[c];
+  if (x0 >= H && x0 - H + CW <= Nxc && y0 >= H && y0 - H + CH <= Nyc) {
+    // a tile away from the periodic edges: no wrap
+    const int64_t c0 = base + (int64_t)(y0 - H) * Nxc + (x0 - H);
+    for (int q = threadIdx.x; q < CW * CH; q += blockDim.x) {
+      const int lx = q % CW, ly = q / CW;
+      const int64_t c = c0 + (int64_t)ly * Nxc + lx;
+      ck[q] = kid(A.cmt[c], A.cmi[c]);
+    }
+  } else {
+    for (int q = threadIdx.x; q < CW * CH; q += blockDim.x) {
+      const int lx = q % CW, ly = q / CW;
+      const int gx = wrapi(x0 + lx - H, Nxc), gy = wrapi(y0 + ly - H, Nyc);
+      const int64_t c = base + (int64_t)gy * Nxc + gx;
+      ck[q] = kid(A.cmt[c], A.cmi[c]);
+    }
   }
   __syncthreads();
-  for (int q = threadIdx.x; q < HW * CH; q += blockDim.x) {
-    const int hx = q % HW, ly = q / HW;
-    const int lx = hx - 1 + H;
-    uint64_t bk = KINF;
-    int32_t bi = IINF;
+  for (int q = threadIdx.x; q < CH * G::NHB; q += blockDim.x) {
+    const int ly = q / G::NHB, hx0 = (q % G::NHB) * SB;
+    kid_t a[SB + W - 1], o[SB];
 #pragma unroll
-    for (int d = -r; d <= r; d++) {
-      const int o = ly * CW + lx + d;
-      if (pair_less(ck[o], ci[o], bk, bi)) { bk = ck[o]; bi = ci[o]; }
-    }
-    hk[q] = bk;
-    hi[q] = bi;
+    for (int j = 0; j < SB + W - 1; j++) a[j] = ck[ly * CW + hx0 + j];
+    block_window_min<SB, W>(a, o);
+#pragma unroll
+    for (int k = 0; k < SB; k++)
+      if (hx0 + k < HW) hk[ly * HW + hx0 + k] = o[k];
   }
   __syncthreads();
-  for (int q = threadIdx.x; q < HW * (TY + 2); q += blockDim.x) {
-    const int wx = q % HW, wy = q / HW;
-    const int ly = wy - 1 + H;
-    uint64_t bk = KINF;
-    int32_t bi = IINF;
+  for (int q = threadIdx.x; q < HW * G::NVB; q += blockDim.x) {
+    const int wx = q % HW, wy0 = (q / HW) * SB;
+    kid_t a[SB + W - 1], o[SB];
 #pragma unroll
-    for (int d = -r; d <= r; d++) {
-      const int o = (ly + d) * HW + wx;
-      if (pair_less(hk[o], hi[o], bk, bi)) { bk = hk[o]; bi = hi[o]; }
-    }
-    wk[q] = bk;
-    wi[q] = bi;
+    for (int j = 0; j < SB + W - 1; j++) a[j] = hk[(wy0 + j) * HW + wx];
+    block_window_min<SB, W>(a, o);
+#pragma unroll
+    for (int k = 0; k < SB; k++) wk[(wy0 + k) * HW + wx] = o[k];
   }
   __syncthreads();
   const int ix = threadIdx.x % TX, iy = threadIdx.x / TX;
@@ -406,12 +451,12 @@ __global__ void __launch_bounds__(TX * TY) k_select(const SysDev* __restrict__ s
   bool sel = false;
   int32_t g = 0;
   if (cx < Nxc && cy < Nyc) {
-    const int o = (iy + H) * CW + ix + H;
-    const uint64_t k = ck[o];
-    const int32_t id = ci[o];
+    const kid_t v = ck[(iy + H) * CW + ix + H];
+    const uint64_t k = (uint64_t)(v >> 32);
+    const int32_t id = (int32_t)(uint32_t)v;
     g = id & GMASK;
     const int w = (iy + 1) * HW + ix + 1;
-    if (k < lim && wk[w] == k && wi[w] == id) {
+    if (k < lim && wk[w] == v) {
       const int c = cy * Nxc + cx;
       if (A.fc[2 * (int64_t)g] == c) {
         const int c2 = A.fc[2 * (int64_t)g + 1];
@@ -423,10 +468,7 @@ __global__ void __launch_bounds__(TX * TY) k_select(const SysDev* __restrict__ s
           if (dx < -1) dx += Nxc;
           if (dy > 1) dy -= Nyc;
           if (dy < -1) dy += Nyc;
-          if (dx >= -1 && dx <= 1 && dy >= -1 && dy <= 1) {
-            const int w2 = (iy + 1 + dy) * HW + ix + 1 + dx;
-            sel = wk[w2] == k && wi[w2] == id;
-          }
+          if (dx >= -1 && dx <= 1 && dy >= -1 && dy <= 1) sel = wk[(iy + 1 + dy) * HW + ix + 1 + dx] == v;
         }
       }
     }
@@ -1442,6 +1484,9 @@ __global__ void __launch_bounds__(32 * BWPB, 4) k_block_rounds(const SysDev* __r
 // reschedules it; then the eligibility bound of the next round
 __global__ void k_barrier(const SysDev* __restrict__ sys, RoundArgs A) {
   __shared__ int go;
+  // every reader of this round's selection has finished: empty it for the
+  // next round (the call starts with it empty)
+  if (blockIdx.x == 0 && threadIdx.x == 0) *A.nsafe = 0;
   for (int s = blockIdx.x; s < A.nsys; s += gridDim.x) {
     if (A.lim[s] == 0) continue;      // stopped for the rest of the call
     const SysDev& S = sys[s];
@@ -1589,37 +1634,36 @@ int round_init(edmd_ctx* ctx) {
   CK(sync_copy(ctx, R->tx0, tx0.data(), R->ntiles * 4, cudaMemcpyHostToDevice));
   CK(sync_copy(ctx, R->ty0, ty0.data(), R->ntiles * 4, cudaMemcpyHostToDevice));
   CK(sync_set(ctx, R->selflag, 0, ctx->nsys * 4));
-  // the selection tile of the widest window (radius 12) needs more than the
-  // default 48 KB of dynamic shared memory
-  const int sbmax = (int)select_smem(RTILE);
-  CK(cudaFuncSetAttribute(k_select<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, sbmax));
-  CK(cudaFuncSetAttribute(k_select<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, sbmax));
-  CK(cudaFuncSetAttribute(k_select<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, sbmax));
-  CK(cudaFuncSetAttribute(k_select<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, sbmax));
-  CK(cudaFuncSetAttribute(k_select<12>, cudaFuncAttributeMaxDynamicSharedMemorySize, sbmax));
+  // selection tiles of wide windows need more than the default 48 KB of
+  // dynamic shared memory
+  CK(cudaFuncSetAttribute(k_select<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SelGeom<3>::bytes));
+  CK(cudaFuncSetAttribute(k_select<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SelGeom<4>::bytes));
+  CK(cudaFuncSetAttribute(k_select<5>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SelGeom<5>::bytes));
+  CK(cudaFuncSetAttribute(k_select<6>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SelGeom<6>::bytes));
+  CK(cudaFuncSetAttribute(k_select<7>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SelGeom<7>::bytes));
+  CK(cudaFuncSetAttribute(k_select<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SelGeom<8>::bytes));
+  CK(cudaFuncSetAttribute(k_select<9>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SelGeom<9>::bytes));
+  CK(cudaFuncSetAttribute(k_select<10>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SelGeom<10>::bytes));
+  CK(cudaFuncSetAttribute(k_select<11>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SelGeom<11>::bytes));
+  CK(cudaFuncSetAttribute(k_select<12>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SelGeom<12>::bytes));
   k_round_setup<<<dim3(64, ctx->nsys), 256, 0, ctx->stream>>>(R->doff, ctx->ds, R->dsys);
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(ctx->stream));
   return EDMD_OK;
 }
 
-size_t select_smem(int r) {
-  const int H = r + 1, CW = TX + 2 * H, CH = TY + 2 * H, HW = TX + 2;
-  return (size_t)(CW * CH + HW * CH + HW * (TY + 2)) * 12;
-}
 
 // one round: selection, processing, minima, barriers
 cudaError_t enqueue_round(edmd_ctx* ctx, const RoundBufs* R, const RoundArgs& A, int nsm) {
   cudaStream_t st = ctx->stream;
-  k_round_begin<<<1, 1, 0, st>>>(A);
   const unsigned tgrid = (unsigned)(R->ntiles < nsm * 8 ? R->ntiles : nsm * 8);
-  const size_t sb = select_smem(A.radius);
   switch (A.radius) {
-    case 3: k_select<3><<<tgrid, TX * TY, sb, st>>>(ctx->ds, A); break;
-    case 4: k_select<4><<<tgrid, TX * TY, sb, st>>>(ctx->ds, A); break;
-    case 8: k_select<8><<<tgrid, TX * TY, sb, st>>>(ctx->ds, A); break;
-    case 12: k_select<12><<<tgrid, TX * TY, sb, st>>>(ctx->ds, A); break;
-    default: k_select<0><<<tgrid, TX * TY, sb, st>>>(ctx->ds, A); break;
+#define SEL_CASE(R) \
+    case R: k_select<R><<<tgrid, TX * TY, SelGeom<R>::bytes, st>>>(ctx->ds, A); break;
+    SEL_CASE(3) SEL_CASE(4) SEL_CASE(5) SEL_CASE(6) SEL_CASE(7)
+    SEL_CASE(8) SEL_CASE(9) SEL_CASE(10) SEL_CASE(11) SEL_CASE(12)
+#undef SEL_CASE
+    default: break;   // radius is checked to be 3..RTILE before any round
   }
   k_process<<<nsm * 16, 32 * WPB, 0, st>>>(ctx->ds, A);
   k_process_thread<<<nsm * 8, 128, 0, st>>>(ctx->ds, A);
@@ -1741,7 +1785,8 @@ static int run_rounds(edmd_ctx* ctx, const std::vector<uint64_t>& tgt, double t_
   }
   int64_t rounds = 0;
   int32_t active = 1;
-  while (active && rounds < max_rounds) {
+  ce = cudaMemsetAsync(R->nsafe, 0, 4, st);
+  while (ce == cudaSuccess && active && rounds < max_rounds) {
     ce = cudaGraphLaunch(exec, st);
     if (ce == cudaSuccess) ce = cudaMemcpyAsync(active_h, R->active, 4, cudaMemcpyDeviceToHost, st);
     if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
