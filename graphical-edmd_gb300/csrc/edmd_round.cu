@@ -85,6 +85,7 @@ struct RoundArgs {
   uint64_t* cmt; int32_t* cmi;   // attributed minimum (key, id) per cell
   uint64_t* lw; uint64_t* lr;    // causality stamps per cell
   int32_t* safe; int32_t* nsafe; // selected events of the round
+  int32_t* nsafe_next;           // the next round's count (two alternate), emptied in this round
   int32_t* dcell;                // cells to recompute, MAXDIRTY per selected event
   int32_t* selflag;              // some event of the system was selected
   int32_t* active;               // systems still running after the round
@@ -1293,7 +1294,7 @@ __device__ __forceinline__ void list_min(const SysDev& S, const RoundArgs& A, in
 // the cells whose minimum the selected events can have changed: four cells
 // per warp, one 8-lane group each (lane q walks list q of the 3x3 block,
 // lane 0 also list 8), the same minima as recompute_cell
-__global__ void __launch_bounds__(256) k_recompute(const SysDev* __restrict__ sys, RoundArgs A) {
+__device__ void recompute_cells(const SysDev* __restrict__ sys, const RoundArgs& A) {
   const int lane = threadIdx.x & 31, grp = lane >> 3, q = lane & 7;
   const int64_t total = (int64_t)(*A.nsafe) * MAXDIRTY;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -1482,12 +1483,9 @@ __global__ void __launch_bounds__(32 * BWPB, 4) k_block_rounds(const SysDev* __r
 // run); a system with nothing eligible left before its screenshot time
 // free-flies every disk to it (takeAScreenshot, src/EDMD.c:4657-4661) and
 // reschedules it; then the eligibility bound of the next round
-__global__ void k_barrier(const SysDev* __restrict__ sys, RoundArgs A) {
+__device__ void barrier_systems(const SysDev* __restrict__ sys, const RoundArgs& A, int first, int stride) {
   __shared__ int go;
-  // every reader of this round's selection has finished: empty it for the
-  // next round (the call starts with it empty)
-  if (blockIdx.x == 0 && threadIdx.x == 0) *A.nsafe = 0;
-  for (int s = blockIdx.x; s < A.nsys; s += gridDim.x) {
+  for (int s = first; s < A.nsys; s += stride) {
     if (A.lim[s] == 0) continue;      // stopped for the rest of the call
     const SysDev& S = sys[s];
     const int N = S.B.N;
@@ -1526,7 +1524,11 @@ __global__ void k_barrier(const SysDev* __restrict__ sys, RoundArgs A) {
       for (int i = threadIdx.x; i < N; i += blockDim.x) {
         Disk p = S.d[i];
         free_fly_i(S.B, p, tbar);
-        S.d[i] = p;
+        // position and time only: the list links are read concurrently by
+        // the minima recompute of the same kernel
+        S.d[i].x = p.x;
+        S.d[i].y = p.y;
+        S.d[i].tl = p.tl;
         shadow_write(A, A.doff[s] + i, S.B, p, S.cx[i], S.cy[i], A.epoch[s]);
       }
       __syncthreads();
@@ -1538,6 +1540,19 @@ __global__ void k_barrier(const SysDev* __restrict__ sys, RoundArgs A) {
     if (threadIdx.x == 0 && A.lim[s] != 0) A.lim[s] = system_limit(S, A, s);
     __syncthreads();
   }
+}
+
+// After the round: the per-system barrier (blocks 0 .. nbar-1, one system at
+// a time) and the minima of the dirty cells (all blocks) in one launch.  The
+// two are independent: the barrier reads the round's counters and writes
+// each system's limits and, when it passes a screenshot, the disks'
+// positions; the recompute reads event keys, footprints and list links.
+__global__ void __launch_bounds__(256) k_recompute_barrier(const SysDev* __restrict__ sys, RoundArgs A,
+                                                          int nbar) {
+  // the next round's selection count starts empty (this round's is still read)
+  if (blockIdx.x == 0 && threadIdx.x == 0) *A.nsafe_next = 0;
+  if ((int)blockIdx.x < nbar) barrier_systems(sys, A, blockIdx.x, nbar);
+  recompute_cells(sys, A);
 }
 
 // fold the call's counters into each system's state; its time is the last
@@ -1620,7 +1635,7 @@ int round_init(edmd_ctx* ctx) {
   CK(dalloc(&R->drank, TN)); CK(dalloc(&R->drank_bak, TN));
   CK(dalloc(&R->ikb, TN)); CK(dalloc(&R->iktie, TN));
   CK(dalloc(&R->cmi, TC)); CK(dalloc(&R->cmt, TC)); CK(dalloc(&R->lw, TC)); CK(dalloc(&R->lr, TC));
-  CK(dalloc(&R->safe, TN)); CK(dalloc(&R->nsafe, 1)); CK(dalloc(&R->dcell, TN * MAXDIRTY));
+  CK(dalloc(&R->safe, TN)); CK(dalloc(&R->nsafe, 2)); CK(dalloc(&R->dcell, TN * MAXDIRTY));
   CK(dalloc(&R->selflag, ctx->nsys)); CK(dalloc(&R->active, 1)); CK(dalloc(&R->work, 1));
   CK(dalloc(&R->doff, ctx->nsys)); CK(dalloc(&R->coff, ctx->nsys));
   CK(dalloc(&R->lim, ctx->nsys)); CK(dalloc(&R->target, ctx->nsys)); CK(dalloc(&R->freeze, ctx->nsys));
@@ -1654,8 +1669,11 @@ int round_init(edmd_ctx* ctx) {
 
 
 // one round: selection, processing, minima, barriers
-cudaError_t enqueue_round(edmd_ctx* ctx, const RoundBufs* R, const RoundArgs& A, int nsm) {
+cudaError_t enqueue_round(edmd_ctx* ctx, const RoundBufs* R, const RoundArgs& A0, int nsm, int k) {
   cudaStream_t st = ctx->stream;
+  RoundArgs A = A0;                  // round k selects into count k % 2 and empties the other
+  A.nsafe = R->nsafe + (k & 1);
+  A.nsafe_next = R->nsafe + ((k + 1) & 1);
   const unsigned tgrid = (unsigned)(R->ntiles < nsm * 8 ? R->ntiles : nsm * 8);
   switch (A.radius) {
 #define SEL_CASE(R) \
@@ -1667,8 +1685,7 @@ cudaError_t enqueue_round(edmd_ctx* ctx, const RoundBufs* R, const RoundArgs& A,
   }
   k_process<<<nsm * 16, 32 * WPB, 0, st>>>(ctx->ds, A);
   k_process_thread<<<nsm * 8, 128, 0, st>>>(ctx->ds, A);
-  k_recompute<<<nsm * 8, 256, 0, st>>>(ctx->ds, A);
-  k_barrier<<<ctx->nsys < nsm * 8 ? ctx->nsys : nsm * 8, 256, 0, st>>>(ctx->ds, A);
+  k_recompute_barrier<<<nsm * 8, 256, 0, st>>>(ctx->ds, A, ctx->nsys < nsm * 8 ? ctx->nsys : nsm * 8);
   return cudaGetLastError();
 }
 
@@ -1767,7 +1784,7 @@ static int run_rounds(edmd_ctx* ctx, const std::vector<uint64_t>& tgt, double t_
   cudaGraphExec_t exec = nullptr;
   CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
   cudaError_t ce = cudaSuccess;
-  for (int k = 0; k < per_graph && ce == cudaSuccess; k++) ce = enqueue_round(ctx, R, A, nsm);
+  for (int k = 0; k < per_graph && ce == cudaSuccess; k++) ce = enqueue_round(ctx, R, A, nsm, k);
   cudaError_t ee = cudaStreamEndCapture(st, &graph);
   if (ce != cudaSuccess || ee != cudaSuccess) {
     if (graph) cudaGraphDestroy(graph);
@@ -1785,7 +1802,7 @@ static int run_rounds(edmd_ctx* ctx, const std::vector<uint64_t>& tgt, double t_
   }
   int64_t rounds = 0;
   int32_t active = 1;
-  ce = cudaMemsetAsync(R->nsafe, 0, 4, st);
+  ce = cudaMemsetAsync(R->nsafe, 0, 8, st);
   while (ce == cudaSuccess && active && rounds < max_rounds) {
     ce = cudaGraphLaunch(exec, st);
     if (ce == cudaSuccess) ce = cudaMemcpyAsync(active_h, R->active, 4, cudaMemcpyDeviceToHost, st);
