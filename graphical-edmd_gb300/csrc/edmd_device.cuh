@@ -319,20 +319,6 @@ __device__ __forceinline__ double coll_time_normal_i(const Box& B, const Disk& p
   return (-b - sqrt(det)) / v2;
 }
 
-// The approach test of collisionTimeNormal (src/EDMD.c:2683-2697): the same
-// operations as coll_time_normal_i up to b = dr.dv; false exactly when that
-// function returns "never" at its first test (b > 0), before any overlap test.
-__device__ __forceinline__ bool approaching_i(const Box& B, const Disk& p1, const Disk& p2, double t) {
-  double lat2 = t - p2.tl;
-  double dvx = p2.vx - p1.vx;
-  double dvy = p2.vy - p1.vy;
-  double dx = (p2.x + lat2 * p2.vx) - p1.x;
-  double dy = (p2.y + lat2 * p2.vy) - p1.y;
-  pbc_i(B, dx, dy);
-  double b = dx * dvx + dy * dvy;
-  return !is_pos(b);
-}
-
 __device__ __forceinline__ bool key_less(uint32_t b1, uint64_t t1, uint64_t k1, int32_t i1,
                                          uint32_t b2, uint64_t t2, uint64_t k2, int32_t i2) {
   if (b1 != b2) return b1 < b2;
