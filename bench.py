@@ -79,10 +79,10 @@ DIFF_N, DIFF_PHI, DIFF_SEED, DIFF_COLL = 1024, 0.60, 11, 10000
 # configuration (workload, engine, lanes per system)
 PROFILED = {
     ("batched", "warp", 32): dict(
-        kernel="k_run<32>", dram_bytes_per_collision=5744.0, fp64_pipe_active=0.558,
+        kernel="k_run<32, false>", dram_bytes_per_collision=5765.0, fp64_pipe_active=0.543,
         capture="ncu --set full --clock-control none -k regex:k_run -s 4 -c 1 python bench.py --workload batched "
-                "--nsys 4096 --coll 2000 --steps 1 --warmup 3 --no-cpu-baseline --no-secondary "
-                "(dram__bytes_read.sum + dram__bytes_write.sum = 47.05 GB for 8.192e6 collisions)"),
+                "--nsys 4096 --coll 2000 --steps 1 --warmup 3 --no-cpu-baseline --no-secondary --no-tune "
+                "(dram__bytes_read.sum + dram__bytes_write.sum = 47.23 GB for 8.192e6 collisions)"),
 }
 
 
