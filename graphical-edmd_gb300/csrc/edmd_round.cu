@@ -95,6 +95,8 @@ struct RoundArgs {
   uint64_t* tlast;               // per-system largest screenshot key passed
   uint64_t* cnt;                 // [nsys][NSTRIPE][NCNT] counters of this call
   int32_t thr_min;               // rounds of at least this many events run one thread per event
+  int32_t thread_kernel;         // k_process_thread is in this round's graph
+  int32_t* maxsafe;              // largest selection count of the graph launch
   float4* shp;                   // FP32 shadow of each disk: cell-relative x, y and vx, vy
   float* sht;                    // ... and its time relative to the system's epoch
   double* epoch;                 // per-system time origin of the shadows (the call's start)
@@ -1208,7 +1210,8 @@ __global__ void __launch_bounds__(32 * WPB, 2) k_process(const SysDev* __restric
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   WarpScratch* W = &scr[wid];
   const int nsafe = *A.nsafe;
-  if (nsafe >= A.thr_min) return;                 // k_process_thread takes the round
+  if (blockIdx.x == 0 && threadIdx.x == 0) atomicMax(A.maxsafe, nsafe);
+  if (A.thread_kernel && nsafe >= A.thr_min) return;   // k_process_thread takes the round
   const int gw = blockIdx.x * WPB + wid, nw = gridDim.x * WPB;
   const int stripe = gw & (NSTRIPE - 1);
   for (int n = gw; n < nsafe; n += nw) {
@@ -1636,7 +1639,7 @@ int round_init(edmd_ctx* ctx) {
   CK(dalloc(&R->ikb, TN)); CK(dalloc(&R->iktie, TN));
   CK(dalloc(&R->cmi, TC)); CK(dalloc(&R->cmt, TC)); CK(dalloc(&R->lw, TC)); CK(dalloc(&R->lr, TC));
   CK(dalloc(&R->safe, TN)); CK(dalloc(&R->nsafe, 2)); CK(dalloc(&R->dcell, TN * MAXDIRTY));
-  CK(dalloc(&R->selflag, ctx->nsys)); CK(dalloc(&R->active, 1)); CK(dalloc(&R->work, 1));
+  CK(dalloc(&R->selflag, ctx->nsys)); CK(dalloc(&R->active, 2)); CK(dalloc(&R->work, 1));
   CK(dalloc(&R->doff, ctx->nsys)); CK(dalloc(&R->coff, ctx->nsys));
   CK(dalloc(&R->lim, ctx->nsys)); CK(dalloc(&R->target, ctx->nsys)); CK(dalloc(&R->freeze, ctx->nsys));
   CK(dalloc(&R->tlast, ctx->nsys)); CK(dalloc(&R->viol, 1));
@@ -1669,11 +1672,13 @@ int round_init(edmd_ctx* ctx) {
 
 
 // one round: selection, processing, minima, barriers
-cudaError_t enqueue_round(edmd_ctx* ctx, const RoundBufs* R, const RoundArgs& A0, int nsm, int k) {
+cudaError_t enqueue_round(edmd_ctx* ctx, const RoundBufs* R, const RoundArgs& A0, int nsm, int k,
+                          bool with_thread) {
   cudaStream_t st = ctx->stream;
   RoundArgs A = A0;                  // round k selects into count k % 2 and empties the other
   A.nsafe = R->nsafe + (k & 1);
   A.nsafe_next = R->nsafe + ((k + 1) & 1);
+  A.thread_kernel = with_thread ? 1 : 0;
   const unsigned tgrid = (unsigned)(R->ntiles < nsm * 8 ? R->ntiles : nsm * 8);
   switch (A.radius) {
 #define SEL_CASE(R) \
@@ -1684,7 +1689,7 @@ cudaError_t enqueue_round(edmd_ctx* ctx, const RoundBufs* R, const RoundArgs& A0
     default: break;   // radius is checked to be 3..RTILE before any round
   }
   k_process<<<nsm * 16, 32 * WPB, 0, st>>>(ctx->ds, A);
-  k_process_thread<<<nsm * 8, 128, 0, st>>>(ctx->ds, A);
+  if (with_thread) k_process_thread<<<nsm * 8, 128, 0, st>>>(ctx->ds, A);
   k_recompute_barrier<<<nsm * 8, 256, 0, st>>>(ctx->ds, A, ctx->nsys < nsm * 8 ? ctx->nsys : nsm * 8);
   return cudaGetLastError();
 }
@@ -1733,6 +1738,7 @@ static int run_rounds(edmd_ctx* ctx, const std::vector<uint64_t>& tgt, double t_
   A.dkey = R->dkey; A.dpk = R->dpk; A.drank = R->drank; A.ikb = R->ikb; A.iktie = R->iktie; A.fc = R->fc; A.cmt = R->cmt; A.cmi = R->cmi; A.lw = R->lw; A.lr = R->lr;
   A.safe = R->safe; A.nsafe = R->nsafe; A.dcell = R->dcell; A.selflag = R->selflag;
   A.active = R->active; A.lim = R->lim; A.target = R->target; A.freeze = R->freeze;
+  A.maxsafe = R->active + 1; A.thread_kernel = 1;
   // one thread per event needs enough events to keep every SM busy with one
   // lane each: the cells of small systems stay in L2, so 4096 events do; the
   // events of a large system are far apart, each cell list walk misses L2,
@@ -1777,43 +1783,58 @@ static int run_rounds(edmd_ctx* ctx, const std::vector<uint64_t>& tgt, double t_
     *active_out = capped;
     return EDMD_OK;
   }
-  // a block of rounds is captured once into a graph and replayed until every
-  // system has stopped; the host polls the active count between blocks
+  // A block of rounds is captured into a graph and replayed until every
+  // system has stopped; the host polls the active count between blocks.
+  // Two graphs: with the thread-per-event kernel, and without it (k_process
+  // then takes every round).  Both give the same results; the host runs the
+  // second while the rounds stay well below the thread kernel's threshold,
+  // which saves a kernel per round that would return at once.
   const int per_graph = 16;
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t exec = nullptr;
-  CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-  cudaError_t ce = cudaSuccess;
-  for (int k = 0; k < per_graph && ce == cudaSuccess; k++) ce = enqueue_round(ctx, R, A, nsm, k);
-  cudaError_t ee = cudaStreamEndCapture(st, &graph);
-  if (ce != cudaSuccess || ee != cudaSuccess) {
+  cudaGraphExec_t exec[2] = {nullptr, nullptr};
+  auto capture = [&](bool with_thread, cudaGraphExec_t* out) -> cudaError_t {
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return e;
+    cudaError_t ce = cudaSuccess;
+    for (int k = 0; k < per_graph && ce == cudaSuccess; k++) ce = enqueue_round(ctx, R, A, nsm, k, with_thread);
+    cudaError_t ee = cudaStreamEndCapture(st, &graph);
+    if (ce == cudaSuccess) ce = ee;
+    if (ce == cudaSuccess) ce = cudaGraphInstantiate(out, graph, 0);
     if (graph) cudaGraphDestroy(graph);
-    return set_err(ctx, EDMD_ERR_CUDA, std::string("round capture: ") +
-                                           cudaGetErrorString(ce != cudaSuccess ? ce : ee));
-  }
-  ce = cudaGraphInstantiate(&exec, graph, 0);
-  cudaGraphDestroy(graph);
+    return ce;
+  };
+  const bool may_thread = A.thr_min != INT32_MAX;
+  const bool only_thread = A.thr_min == 0;
+  cudaError_t ce = capture(may_thread, &exec[may_thread ? 1 : 0]);
   if (ce != cudaSuccess) return set_err(ctx, EDMD_ERR_CUDA, std::string("round graph: ") + cudaGetErrorString(ce));
   int32_t* active_h = nullptr;
-  ce = cudaMallocHost((void**)&active_h, sizeof(int32_t));
+  ce = cudaMallocHost((void**)&active_h, 2 * sizeof(int32_t));
   if (ce != cudaSuccess) {
-    cudaGraphExecDestroy(exec);
+    for (auto& x : exec) if (x) cudaGraphExecDestroy(x);
     CK(ce);
   }
   int64_t rounds = 0;
   int32_t active = 1;
+  bool with_thread = may_thread;
   ce = cudaMemsetAsync(R->nsafe, 0, 8, st);
   while (ce == cudaSuccess && active && rounds < max_rounds) {
-    ce = cudaGraphLaunch(exec, st);
-    if (ce == cudaSuccess) ce = cudaMemcpyAsync(active_h, R->active, 4, cudaMemcpyDeviceToHost, st);
+    if (!exec[with_thread ? 1 : 0]) {
+      ce = capture(with_thread, &exec[with_thread ? 1 : 0]);
+      if (ce != cudaSuccess) break;
+    }
+    ce = cudaMemsetAsync(A.maxsafe, 0, 4, st);
+    if (ce == cudaSuccess) ce = cudaGraphLaunch(exec[with_thread ? 1 : 0], st);
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(active_h, R->active, 8, cudaMemcpyDeviceToHost, st);
     if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
     if (ce != cudaSuccess) break;
     rounds += per_graph;
-    active = *active_h;
+    active = active_h[0];
+    // the thread kernel's graph while rounds come within 3/4 of its threshold
+    with_thread = may_thread && (only_thread || (int64_t)active_h[1] * 4 >= (int64_t)A.thr_min * 3);
   }
-  cudaGraphExecDestroy(exec);
+  for (auto& x : exec) if (x) cudaGraphExecDestroy(x);
   cudaFreeHost(active_h);
-  CK(ce);
+  if (ce != cudaSuccess) return set_err(ctx, EDMD_ERR_CUDA, std::string("round graph: ") + cudaGetErrorString(ce));
   k_round_finish<<<(ctx->nsys + 127) / 128, 128, 0, st>>>(ctx->ds, A);
   CK(cudaGetLastError());
   CK(cudaMemcpyAsync(viol_out, R->viol, 8, cudaMemcpyDeviceToHost, st));
