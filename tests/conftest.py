@@ -58,9 +58,10 @@ def golden(name):
 
 
 def golden_names():
-    """Trace fixtures (the files_* and load_* fixtures pin output files instead)."""
+    """Trace fixtures (the files_* and load_* fixtures pin output files instead,
+    the abort_* fixtures the reference's overlap abort)."""
     return sorted(f[:-4] for f in os.listdir(GOLDEN)
-                  if f.endswith(".npz") and not f.startswith(("files_", "load_")))
+                  if f.endswith(".npz") and not f.startswith(("files_", "load_", "abort_")))
 
 
 def parse_args(args):

@@ -20,6 +20,7 @@ only these files, never the reference checkout.
 """
 import argparse
 import os
+import re
 import subprocess
 import sys
 
@@ -37,6 +38,22 @@ CASES = {
     "grow256_v7": ("-N 256 --phi 0.5 -x 0.5 -q 0.7142857 -v 7", 20000, True),
     "grow400_v11": ("-N 400 --phi 0.74 -x 0.5 -q 0.7142857 -v 11", 20000, True),
     "grow300_v5": ("-N 300 --phi 0.3 -x 0.5 -q 0.7142857 -v 5", 20000, True),
+}
+
+# boxes of four to five cells a side, where the 3x3 neighbourhood of a cell
+# wraps onto the cells at its other side
+TINY_CASES = {
+    "tiny_hex12": ("--hex -N 12 --phi 0.4 -x 0 -v 3", 3000, True),
+    "tiny_grow10": ("-N 10 --phi 0.3 -x 0.5 -q 0.7 -v 3", 3000, True),
+    "tiny_grow20": ("-N 20 --phi 0.5 -x 0.5 -q 0.7 -v 5", 3000, True),
+}
+
+# runs the reference ends with its overlap abort (collisionTimeNormal,
+# src/EDMD.c:2708-2717, exit(3)): the collisions before it and the pair it
+# names are kept
+ABORT_CASES = {
+    "abort_hex8": "--hex -N 8 --phi 0.2 -x 0 -v 3",
+    "abort_grow6": "-N 6 --phi 0.3 -x 0.5 -q 0.7 -v 4",
 }
 
 # the same kind of runs with additive contact, r1 + r2 (the reference's own
@@ -120,7 +137,8 @@ def main():
     exe = os.path.join(ROOT, "oracle", "_ref", "ref_trace")
     exe_add = os.path.join(ROOT, "oracle", "_ref", "ref_trace_additive")
     tmp = os.path.join(HERE, "_tmp_trace.txt")
-    cases = [(n, c, exe, 0) for n, c in CASES.items()] + [(n, c, exe_add, 1) for n, c in ADDITIVE_CASES.items()]
+    cases = ([(n, c, exe, 0) for n, c in CASES.items()] + [(n, c, exe, 0) for n, c in TINY_CASES.items()]
+             + [(n, c, exe_add, 1) for n, c in ADDITIVE_CASES.items()])
     for name, (args, maxcoll, full), case_exe, contact in cases:
         run_case(case_exe, args, maxcoll, tmp)
         head, init, c, vir, tfin, state = parse_trace(tmp)
@@ -145,6 +163,22 @@ def main():
                        radf=state[:, 4].astype(np.float64))
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
         print(name, "N", head["N"], "collisions", len(c), "t_final", tfin[0])
+    for name, args in ABORT_CASES.items():
+        env = dict(os.environ, MAXCOLL="1000000", TRACE_OUT=tmp)
+        r = subprocess.run([exe] + args.split(), env=env, capture_output=True, text=True)
+        assert r.returncode == 3, (name, r.returncode)
+        m = re.search(r"between particle (\d+) and particle (\d+)", r.stdout + r.stderr)
+        head, init, c, _, _, _ = parse_trace(tmp)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), args=np.array(args), contact=0,
+                            N=head["N"], Lx=head["Lx"], Ly=head["Ly"], Nxc=head["Nxc"], Nyc=head["Nyc"],
+                            x0=init[:, 0].astype(np.float64), y0=init[:, 1].astype(np.float64),
+                            vx0=init[:, 2].astype(np.float64), vy0=init[:, 3].astype(np.float64),
+                            rad0=init[:, 4].astype(np.float64), m0=init[:, 5].astype(np.float64),
+                            type0=init[:, 6].astype(np.int32),
+                            ci=np.array([x[0] for x in c], np.int32), cj=np.array([x[1] for x in c], np.int32),
+                            ct=np.array([x[4] for x in c], np.float64),
+                            pair=np.array([int(m.group(1)), int(m.group(2))], np.int32))
+        print(name, "N", head["N"], "collisions before the abort", len(c), "pair", m.group(1), m.group(2))
     # verbatim dump + thermo files of a short run (ovito/LAMMPS text format pin)
     name, args = FILES_CASE
     dump = os.path.join(HERE, name + ".dump")

@@ -91,3 +91,45 @@ def test_invalid_radius_is_an_argument_error(edmd, bad):
         edmd.Engine([s])
     assert ei.value.code == edmd.ERR_ARG
     assert "radius" in str(ei.value)
+
+
+@pytest.mark.parametrize("engine", ["warp", "lane", "round"])
+@pytest.mark.parametrize("name", ["abort_hex8", "abort_grow6"])
+def test_reference_abort_reproduced(edmd, name, engine):
+    """Boxes of three cells a side where the reference itself stops with its
+    overlap abort (collisionTimeNormal, src/EDMD.c:2708-2717, exit(3)) after a
+    few dozen collisions (tests/golden/make_golden.py).  The engine accepts
+    the same collisions, in the same order at the same times, and then
+    reports EDMD_ERR_OVERLAP naming the pair the reference names.  The round
+    engine runs the constant-radius phase only, so it takes the Hex case, and
+    is held to the status and the pair."""
+    from conftest import golden, parse_args
+    g = golden(name)
+    a = parse_args(g["args"])
+    if engine == "round" and not a["hex"]:
+        pytest.skip("the round engine runs the constant-radius phase only")
+    N = int(g["N"])
+    if a["hex"]:
+        vr, vr_base = None, 0.0
+    else:
+        st = edmd.grow_start(a["N"], a["phi"], a["seed"], xs=a["xs"], q=a["q"])
+        vr, vr_base = st["vr"], st["vr_base"]
+    desc = edmd.default_desc(N, float(g["Lx"]), float(g["Ly"]), vr_base, a["tmax"], a["dtime"], a["dtime_thermo"])
+    s = dict(desc=desc, x=g["x0"], y=g["y0"], vx=g["vx0"], vy=g["vy0"], rad=g["rad0"], m=g["m0"], vr=vr)
+    n = len(g["ct"])
+    eng = edmd.Engine([s], trace_cap=n + 16, engine=edmd.ENGINE_LANE if engine == "lane" else edmd.ENGINE_WARP)
+    if engine == "round":
+        rc = eng.advance_rounds(max_coll=10 ** 6, radius=3, flags=edmd.F_TRACE, check=False)[0]
+    else:
+        rc = eng.advance(max_coll=10 ** 6, flags=edmd.F_TRACE, check=False)[0]
+    msg = eng.last_error()
+    assert rc == edmd.ERR_OVERLAP, msg
+    assert names_pair(msg, int(g["pair"][0]), int(g["pair"][1])), msg
+    if engine != "round":
+        # (a round also runs the events selected beside the failing one)
+        tr = eng.trace(0)
+        assert len(tr) == n
+        np.testing.assert_array_equal(tr["i"], g["ci"])
+        np.testing.assert_array_equal(tr["j"], g["cj"])
+        np.testing.assert_array_equal(tr["t"], g["ct"])
+    eng.close()

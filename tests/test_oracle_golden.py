@@ -87,3 +87,19 @@ def test_oracle_contact_rules(oracle):
         tr, n = o.run(3000)
         grown.append(tr["t"].copy())
     assert not np.array_equal(grown[0], grown[1])
+
+
+@pytest.mark.parametrize("name", ["abort_hex8", "abort_grow6"])
+def test_oracle_reproduces_reference_abort(built, name):
+    """Where the reference stops with its overlap abort (exit(3), EDMD.c:2708-2717),
+    the oracle does too, naming the same pair (it exits, so it runs as a child)."""
+    import os
+    import subprocess
+    from conftest import ROOT
+    g = golden(name)
+    exe = os.path.join(ROOT, "oracle", "oracle_trace")
+    r = subprocess.run([exe] + str(g["args"]).split(), env=dict(os.environ, MAXCOLL="1000000", TRACE_OUT=os.devnull),
+                       capture_output=True, text=True, timeout=60)
+    assert r.returncode == 3
+    a, b = int(g["pair"][0]), int(g["pair"][1])
+    assert f"overlap between {a} and {b}" in r.stderr, r.stderr
