@@ -82,19 +82,19 @@ class Oracle:
 
     def __init__(self, N=None, phi=0.7, seed=1, start=HEX, xs=0.0, q=0.4, aspect=1.0, tmax=4000.0,
                  dtime=100.0, dtime_thermo=100.0, arrays=None, Lx=None, Ly=None, first_thermo=None,
-                 additive=False):
+                 additive=False, res=1.0, Einit=1.0):
         L = load()
         self._L = L
         old = L.orc_set_contact(1 if additive else 0)
         try:
             self._create(L, N, phi, seed, start, xs, q, aspect, tmax, dtime, dtime_thermo, arrays, Lx, Ly,
-                         first_thermo)
+                         first_thermo, res, Einit)
         finally:
             L.orc_set_contact(old)
         self.N = L.orc_N(self.h)
 
     def _create(self, L, N, phi, seed, start, xs, q, aspect, tmax, dtime, dtime_thermo, arrays, Lx, Ly,
-                first_thermo):
+                first_thermo, res, Einit):
         if arrays is not None:
             a = {k: np.ascontiguousarray(v) for k, v in arrays.items()}
             self.h = L.orc_create_from_arrays(len(a["x"]), Lx, Ly, a["x"], a["y"], a["vx"], a["vy"],
@@ -105,6 +105,7 @@ class Oracle:
             L.orc_default_params(C.byref(p))
             p.N, p.phi, p.seed, p.start, p.xs, p.q, p.aspect = N, phi, seed, start, xs, q, aspect
             p.tmax, p.dtime, p.dtimeThermo = tmax, dtime, dtime_thermo
+            p.res, p.Einit = res, Einit
             if first_thermo is not None:
                 p.firstThermo = first_thermo
             self.h = L.orc_create(C.byref(p))

@@ -68,9 +68,10 @@ def parse_args(args):
     """Reference CLI string of a fixture -> start parameters."""
     a = str(args).split()
     out = dict(hex="--hex" in a, N=500, phi=0.38, xs=0.3, q=0.4, seed=1, tmax=4000.0, dtime=100.0,
-               dtime_thermo=100.0)
+               dtime_thermo=100.0, res=1.0, Einit=1.0, aspect=1.0)
     keys = {"-N": ("N", int), "--phi": ("phi", float), "-x": ("xs", float), "-q": ("q", float),
-            "-v": ("seed", int), "-t": ("tmax", float), "-D": ("dtime", float), "-o": ("dtime_thermo", float)}
+            "-v": ("seed", int), "-t": ("tmax", float), "-D": ("dtime", float), "-o": ("dtime_thermo", float),
+            "-r": ("res", float), "-E": ("Einit", float), "-a": ("aspect", float)}
     for k, (name, f) in keys.items():
         if k in a:
             out[name] = f(a[a.index(k) + 1])

@@ -48,6 +48,17 @@ TINY_CASES = {
     "tiny_grow20": ("-N 20 --phi 0.5 -x 0.5 -q 0.7 -v 5", 3000, True),
 }
 
+# the command line's other physical options: restitution (-r), energy per
+# disk (-E, the Hex velocities and the growth stop's normalisation) and box
+# aspect ratio (-a)
+OPTION_CASES = {
+    "opt_res_hex": ("--hex -N 400 --phi 0.6 -x 0 -r 0.9 -v 2", 5000, True),
+    "opt_einit_hex": ("--hex -N 400 --phi 0.6 -x 0 -E 2.5 -v 3", 5000, True),
+    "opt_einit_grow": ("-N 300 --phi 0.6 -x 0.5 -q 0.7142857 -E 2.5 -v 6", 12000, True),
+    "opt_aspect_grow": ("-N 300 --phi 0.55 -x 0.5 -q 0.7142857 -a 2.0 -v 8", 12000, True),
+    "opt_aspect_hex": ("--hex -N 500 --phi 0.6 -x 0 -a 0.5 -v 9", 5000, True),
+}
+
 # runs the reference ends with its overlap abort (collisionTimeNormal,
 # src/EDMD.c:2708-2717, exit(3)): the collisions before it and the pair it
 # names are kept
@@ -138,6 +149,7 @@ def main():
     exe_add = os.path.join(ROOT, "oracle", "_ref", "ref_trace_additive")
     tmp = os.path.join(HERE, "_tmp_trace.txt")
     cases = ([(n, c, exe, 0) for n, c in CASES.items()] + [(n, c, exe, 0) for n, c in TINY_CASES.items()]
+             + [(n, c, exe, 0) for n, c in OPTION_CASES.items()]
              + [(n, c, exe_add, 1) for n, c in ADDITIVE_CASES.items()])
     for name, (args, maxcoll, full), case_exe, contact in cases:
         run_case(case_exe, args, maxcoll, tmp)

@@ -24,10 +24,11 @@ def system_from_golden(edmd, g):
     if a["hex"]:
         vr, vr_base = None, 0.0
     else:
-        s = edmd.grow_start(a["N"], a["phi"], a["seed"], xs=a["xs"], q=a["q"])
+        s = edmd.grow_start(a["N"], a["phi"], a["seed"], xs=a["xs"], q=a["q"], aspect=a["aspect"])
         vr, vr_base = s["vr"], s["vr_base"]
     desc = edmd.default_desc(N, float(g["Lx"]), float(g["Ly"]), vr_base, a["tmax"], a["dtime"],
                              a["dtime_thermo"], contact=int(g["contact"]))
+    desc.res, desc.Einit = a["res"], a["Einit"]
     return dict(desc=desc, x=g["x0"], y=g["y0"], vx=g["vx0"], vy=g["vy0"], rad=g["rad0"], m=g["m0"], vr=vr)
 
 

@@ -13,11 +13,11 @@ violation count.
 import numpy as np
 import pytest
 
-from conftest import golden, golden_names
+from conftest import golden, golden_names, parse_args
 
 pytestmark = pytest.mark.gpu
 
-HEX = [n for n in golden_names() if n.startswith("hex")]
+HEX = [n for n in golden_names() if n.startswith("hex") or (n.startswith(("opt_", "tiny_")) and n.endswith(("_hex", "hex12")))]
 
 
 def canon(i, j, ci, cj, t):
@@ -31,7 +31,9 @@ def canon(i, j, ci, cj, t):
 
 
 def system_from_golden(edmd, g):
+    a = parse_args(g["args"])
     desc = edmd.default_desc(int(g["N"]), float(g["Lx"]), float(g["Ly"]))
+    desc.res, desc.Einit = a["res"], a["Einit"]
     return dict(desc=desc, x=g["x0"], y=g["y0"], vx=g["vx0"], vy=g["vy0"], rad=g["rad0"], m=g["m0"])
 
 

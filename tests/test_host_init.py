@@ -14,9 +14,9 @@ def test_init_matches_reference(edmd, name):
     g = golden(name)
     a = parse_args(g["args"])
     if a["hex"]:
-        s = edmd.hex_start(a["N"], a["phi"], a["seed"])
+        s = edmd.hex_start(a["N"], a["phi"], a["seed"], aspect=a["aspect"], Einit=a["Einit"])
     else:
-        s = edmd.grow_start(a["N"], a["phi"], a["seed"], xs=a["xs"], q=a["q"])
+        s = edmd.grow_start(a["N"], a["phi"], a["seed"], xs=a["xs"], q=a["q"], aspect=a["aspect"])
     assert s["N"] == int(g["N"])
     assert (s["Lx"], s["Ly"]) == (float(g["Lx"]), float(g["Ly"]))
     for k, gk in (("x", "x0"), ("y", "y0"), ("vx", "vx0"), ("vy", "vy0"), ("rad", "rad0"), ("m", "m0")):

@@ -16,7 +16,8 @@ def test_oracle_matches_reference(oracle, name):
     g = golden(name)
     a = parse_args(g["args"])
     o = oracle.Oracle(N=a["N"], phi=a["phi"], seed=a["seed"], start=oracle.HEX if a["hex"] else oracle.GROW,
-                      xs=a["xs"], q=a["q"], tmax=a["tmax"], additive=bool(g["contact"]))
+                      xs=a["xs"], q=a["q"], tmax=a["tmax"], additive=bool(g["contact"]), aspect=a["aspect"],
+                      res=a["res"], Einit=a["Einit"])
     assert o.N == int(g["N"])
     Lx, Ly, nx, ny = o.box()
     assert (Lx, Ly, nx, ny) == (float(g["Lx"]), float(g["Ly"]), int(g["Nxc"]), int(g["Nyc"]))
