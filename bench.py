@@ -83,6 +83,14 @@ PROFILED = {
         capture="ncu --set full --clock-control none -k regex:k_run -s 4 -c 1 python bench.py --workload batched "
                 "--nsys 4096 --coll 2000 --steps 1 --warmup 3 --no-cpu-baseline --no-secondary --no-tune "
                 "(dram__bytes_read.sum + dram__bytes_write.sum = 47.23 GB for 8.192e6 collisions)"),
+    ("single_large", "round", None): dict(
+        kernel="k_select<4> + k_process + k_recompute_barrier", dram_bytes_per_collision=4990.0,
+        fp64_pipe_active=0.606,
+        capture="ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum,gpu__time_duration.sum --cache-control none "
+                "--clock-control none -k regex:'k_select|k_process$|k_recompute_barrier' -s 480 -c 60 python bench.py "
+                "--workload single_large --coll 300000 --steps 1 --warmup 3 --no-cpu-baseline --no-secondary "
+                "(20 rounds in the middle of a call, warm caches: 19.76 MB per round, over the workload's mean "
+                "of 3960 collisions per round; FP64 pipe of k_process from one --set full capture of a round)"),
 }
 
 
@@ -615,7 +623,8 @@ def measure(edmd, a, workload, engine, coll, steps, warmup, rank, world, dist, d
                                     "configuration, scaled to the launch's collisions: %s"
                                     % (prof["kernel"], prof["capture"])),
                     fp64_pipe_active=prof["fp64_pipe_active"],
-                    fp64_pipe_source="sm__pipe_fp64_cycles_active of the same capture")
+                    fp64_pipe_source=("sm__pipe_fp64_cycles_active of the same capture" if engine == "warp" else
+                                      "sm__pipe_fp64_cycles_active of k_process in a --set full capture"))
     else:
         roof["traffic_source"] = "no ncu capture of this configuration"
     if engine == "round":
