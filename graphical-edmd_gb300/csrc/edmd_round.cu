@@ -61,7 +61,8 @@ constexpr int OB_CORRUPT = -2;        // overlap partner marker: a cell list lon
 // are R_NEW, or R_FIRST when the serial queue would pop them before the
 // inherited event of equal time they tie with (new_rank)
 constexpr uint8_t R_FIRST = 0, R_NEW = 3;
-constexpr int WPB = 8;                // warps per block of the processing kernel
+constexpr int WPB = 1;                // warps per block of the processing kernel (measured best:
+                                      // one-warp blocks, 20 per SM, 96 registers)
 constexpr int NSTRIPE = 32;           // copies of each system's counters
 // counters of the round engine, per system and stripe (u64 slots)
 enum { C_CT0, C_CT1, C_CT2, C_CT3, C_NCOL, C_NCROSS, C_NSTALE, C_NPAIR, C_NPRED, C_NEV, C_NSCREEN, C_TLAST, NCNT };
@@ -1147,7 +1148,7 @@ __device__ __forceinline__ uint64_t group_max(unsigned m, uint64_t v) {
 // the selected events of a round, one thread each (rounds of at least
 // A.thr_min events; k_process takes the others); per-system counters are
 // summed over the lanes of a warp that share the system before one atomic
-__global__ void __launch_bounds__(128) k_process_thread(const SysDev* __restrict__ sys, RoundArgs A) {
+__global__ void __launch_bounds__(32, 16) k_process_thread(const SysDev* __restrict__ sys, RoundArgs A) {
   const int nsafe = *A.nsafe;
   if (nsafe < A.thr_min) return;
   const int lane = threadIdx.x & 31;
@@ -1205,7 +1206,7 @@ __global__ void __launch_bounds__(128) k_process_thread(const SysDev* __restrict
 
 // the selected events of a round, one warp each; per-system counters go to
 // one of NSTRIPE stripes to spread the atomics
-__global__ void __launch_bounds__(32 * WPB, 2) k_process(const SysDev* __restrict__ sys, RoundArgs A) {
+__global__ void __launch_bounds__(32 * WPB, 20) k_process(const SysDev* __restrict__ sys, RoundArgs A) {
   __shared__ WarpScratch scr[WPB];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   WarpScratch* W = &scr[wid];
@@ -1688,8 +1689,8 @@ cudaError_t enqueue_round(edmd_ctx* ctx, const RoundBufs* R, const RoundArgs& A0
 #undef SEL_CASE
     default: break;   // radius is checked to be 3..RTILE before any round
   }
-  k_process<<<nsm * 16, 32 * WPB, 0, st>>>(ctx->ds, A);
-  if (with_thread) k_process_thread<<<nsm * 8, 128, 0, st>>>(ctx->ds, A);
+  k_process<<<nsm * 160, 32 * WPB, 0, st>>>(ctx->ds, A);
+  if (with_thread) k_process_thread<<<nsm * 128, 32, 0, st>>>(ctx->ds, A);   // one-warp blocks, 16 per SM: measured best
   k_recompute_barrier<<<nsm * 8, 256, 0, st>>>(ctx->ds, A, ctx->nsys < nsm * 8 ? ctx->nsys : nsm * 8);
   return cudaGetLastError();
 }
