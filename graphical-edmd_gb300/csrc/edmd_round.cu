@@ -51,7 +51,8 @@ constexpr uint64_t KINF = ~0ull;
 constexpr int32_t IINF = 0x7fffffff;
 constexpr int32_t GMASK = 0xffffff;   // disk index inside an event id (rank in the top byte)
 constexpr unsigned FULLM = 0xffffffffu;
-constexpr int TX = 32, TY = 16;       // selection tile (cells): 1.8 halo cells per cell at radius 4
+constexpr int TX = 16, TY = 32;       // selection tile (cells): 2.1 cells loaded per cell at radius 4;
+                                      // measured against 32x16, 32x8 and 64x8 (best by ~1%)
 constexpr int RTILE = 12;             // largest window radius of the tile kernel
 constexpr int MAXDIRTY = 8;           // cells whose minimum one event can change
 constexpr int MAXC = 8;               // candidates buffered per cell list per lane
