@@ -506,12 +506,12 @@ class Stepper:
         if self.engine == "round":
             _, ms, rounds, viol = self.eng.advance_rounds(max_coll=self.coll, radius=self.radius,
                                                           flags=self.edmd.F_EXACT | self.extra_flags)
-            self.launches += 6 * rounds + 4
+            self.launches += self.eng.last_launches()
             self.rounds += rounds
             self.violations += viol
             return ms
         _, ms = self.eng.advance(max_coll=self.coll, flags=self.edmd.F_COUNT_NORMAL | self.extra_flags)
-        self.launches += 1
+        self.launches += self.eng.last_launches()
         return ms
 
 

@@ -18,6 +18,7 @@ struct edmd_ctx {
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   cudaEvent_t c0 = nullptr, c1 = nullptr;  // whole-call timing of the differentiation drivers
   float last_ms = 0;                       // device time of the last timed call (edmd_get_last_ms)
+  int64_t last_launches = 0;               // kernels launched by the last advance or round call
   // shared-memory kernel of the warp engine (EDMD_F_SMEM): its system list,
   // work counter, stream and completion event, made on first use
   int32_t* smem_list = nullptr;

@@ -1492,6 +1492,7 @@ static int advance_smem_split(edmd_ctx* ctx, RunArgs A, int kgrid_max, int nsm) 
     CK(cudaStreamWaitEvent(ctx->stream2, ctx->e0, 0));
     k_run_smem<<<g, 32, need, ctx->stream2>>>(ctx->ds, A, ctx->smem_list, (int)fit.size(), ctx->smem_work);
     CK(cudaGetLastError());
+    ctx->last_launches++;
     CK(cudaEventRecord(ctx->e2, ctx->stream2));
   }
   if (!rest.empty()) {
@@ -1504,6 +1505,7 @@ static int advance_smem_split(edmd_ctx* ctx, RunArgs A, int kgrid_max, int nsm) 
     if (ctx->any_additive) k_run<32><<<grid, 32 * WARPS_PER_BLOCK, 0, ctx->stream>>>(ctx->ds, B);
     else k_run<32, false><<<grid, 32 * WARPS_PER_BLOCK, 0, ctx->stream>>>(ctx->ds, B);
     CK(cudaGetLastError());
+    ctx->last_launches++;
   }
   if (!fit.empty()) CK(cudaStreamWaitEvent(ctx->stream, ctx->e2, 0));
   return EDMD_OK;
@@ -1522,6 +1524,7 @@ extern "C" int edmd_advance(edmd_ctx* ctx, int64_t max_coll, double t_stop, uint
   if (ctx->engine == EDMD_ENGINE_LANE) {
     CK(cudaEventRecord(ctx->e0, ctx->stream));
     CK(lane_run_launch(ctx->ds, A, g_lane_threads, ctx->stream));
+    ctx->last_launches = 1;
   } else {
     CK(cudaMemsetAsync(ctx->work, 0, sizeof(int32_t), ctx->stream));
     int dev = 0, nsm = 0;
@@ -1557,10 +1560,12 @@ extern "C" int edmd_advance(edmd_ctx* ctx, int64_t max_coll, double t_stop, uint
                          ctx->stream));
       A.order = ctx->order;
     }
+    ctx->last_launches = 0;
     if ((flags & EDMD_F_SMEM) && gw == 32) {
       int rc = advance_smem_split(ctx, A, per_sm * nsm, nsm);
       if (rc) return rc;
     } else {
+    ctx->last_launches = 1;
     CK(cudaEventRecord(ctx->e0, ctx->stream));
     if (gw == 4) k_run<4><<<grid, 32 * WARPS_PER_BLOCK, 0, ctx->stream>>>(ctx->ds, A);
     else if (gw == 8) k_run<8><<<grid, 32 * WARPS_PER_BLOCK, 0, ctx->stream>>>(ctx->ds, A);
@@ -1732,6 +1737,12 @@ extern "C" int edmd_get_engine(const edmd_ctx* ctx) {
 extern "C" int edmd_get_last_ms(const edmd_ctx* ctx, float* ms) {
   if (!ctx || !ms) return EDMD_ERR_ARG;
   *ms = ctx->last_ms;
+  return EDMD_OK;
+}
+
+extern "C" int edmd_get_last_launches(const edmd_ctx* ctx, int64_t* n) {
+  if (!ctx || !n) return EDMD_ERR_ARG;
+  *n = ctx->last_launches;
   return EDMD_OK;
 }
 

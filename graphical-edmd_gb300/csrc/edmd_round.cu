@@ -1759,6 +1759,7 @@ static int run_rounds(edmd_ctx* ctx, const std::vector<uint64_t>& tgt, double t_
   k_prep<<<gd, 256, 0, st>>>(ctx->ds, A);
   k_prep_owner<<<gd, 256, 0, st>>>(A);
   k_limits<<<(ctx->nsys + 127) / 128, 128, 0, st>>>(ctx->ds, A);
+  ctx->last_launches += fresh ? 4 : 3;
   CK(cudaGetLastError());
   int dev = 0, nsm = 0;
   CK(cudaGetDevice(&dev));
@@ -1773,6 +1774,7 @@ static int run_rounds(edmd_ctx* ctx, const std::vector<uint64_t>& tgt, double t_
     CK(cudaMemsetAsync(R->active, 0, 4, st));
     k_block_rounds<<<nsm * 4, 32 * BWPB, 0, st>>>(ctx->ds, A, R->work, max_rounds);
     CK(cudaGetLastError());
+    ctx->last_launches += 1;
     std::vector<uint64_t> rs(ctx->nsys);
     int32_t capped = 0;
     CK(cudaMemcpyAsync(rs.data(), R->tlast, ctx->nsys * 8, cudaMemcpyDeviceToHost, st));
@@ -1791,7 +1793,7 @@ static int run_rounds(edmd_ctx* ctx, const std::vector<uint64_t>& tgt, double t_
   // then takes every round).  Both give the same results; the host runs the
   // second while the rounds stay well below the thread kernel's threshold,
   // which saves a kernel per round that would return at once.
-  const int per_graph = 16;
+  const int per_graph = 32;         // measured: 32 rounds 0.2-1.6% faster than 16, 64 about the same as 32
   cudaGraphExec_t exec[2] = {nullptr, nullptr};
   auto capture = [&](bool with_thread, cudaGraphExec_t* out) -> cudaError_t {
     cudaGraph_t graph = nullptr;
@@ -1826,6 +1828,7 @@ static int run_rounds(edmd_ctx* ctx, const std::vector<uint64_t>& tgt, double t_
     }
     ce = cudaMemsetAsync(A.maxsafe, 0, 4, st);
     if (ce == cudaSuccess) ce = cudaGraphLaunch(exec[with_thread ? 1 : 0], st);
+    if (ce == cudaSuccess) ctx->last_launches += (int64_t)per_graph * (with_thread ? 4 : 3);
     if (ce == cudaSuccess) ce = cudaMemcpyAsync(active_h, R->active, 8, cudaMemcpyDeviceToHost, st);
     if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
     if (ce != cudaSuccess) break;
@@ -1839,6 +1842,7 @@ static int run_rounds(edmd_ctx* ctx, const std::vector<uint64_t>& tgt, double t_
   if (ce != cudaSuccess) return set_err(ctx, EDMD_ERR_CUDA, std::string("round graph: ") + cudaGetErrorString(ce));
   k_round_finish<<<(ctx->nsys + 127) / 128, 128, 0, st>>>(ctx->ds, A);
   CK(cudaGetLastError());
+  ctx->last_launches += 1;
   CK(cudaMemcpyAsync(viol_out, R->viol, 8, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   *rounds_out += rounds;
@@ -1871,6 +1875,7 @@ extern "C" int edmd_advance_rounds(edmd_ctx* ctx, int64_t max_coll, double t_sto
     if (!fresh) CK(cudaMemcpyAsync(R->drank_bak, R->drank, ctx->total_N, cudaMemcpyDeviceToDevice, ctx->stream));
   }
   ctx->round_dirty = true;
+  ctx->last_launches = 0;
   CK(cudaEventRecord(ctx->e0, ctx->stream));
   int64_t rounds = 0, viol_total = 0;
   int32_t active = 0;

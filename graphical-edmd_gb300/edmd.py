@@ -65,7 +65,7 @@ EXPORTS = [
     "edmd_get_states", "edmd_get_counters", "edmd_get_all_counters", "edmd_get_virial",
     "edmd_get_thermo", "edmd_take_thermo", "edmd_get_trace", "edmd_set_engine", "edmd_set_lane_threads",
     "edmd_set_warp_group",
-    "edmd_get_engine", "edmd_get_last_ms", "edmd_set_device", "edmd_host_alloc", "edmd_host_free", "edmd_run_noalloc",
+    "edmd_get_engine", "edmd_get_last_ms", "edmd_get_last_launches", "edmd_set_device", "edmd_host_alloc", "edmd_host_free", "edmd_run_noalloc",
     "edmd_set_log_capacity", "edmd_clear_log", "edmd_get_log", "edmd_checkpoint_save",
     "edmd_checkpoint_restore", "edmd_tangent_run", "edmd_msd_gradient", "edmd_tangent_run_batch",
     "edmd_msd_gradient_batch", "edmd_destroy",
@@ -120,6 +120,7 @@ def load(path=LIB_PATH):
     L.edmd_set_warp_group.argtypes = [C.c_int32]
     L.edmd_get_engine.argtypes = [C.c_void_p]
     L.edmd_get_last_ms.argtypes = [C.c_void_p, C.POINTER(C.c_float)]
+    L.edmd_get_last_launches.argtypes = [C.c_void_p, C.POINTER(C.c_int64)]
     L.edmd_sync.argtypes = [C.c_void_p]
     L.edmd_get_state.argtypes = [C.c_void_p, C.c_int32] + [C.c_void_p] * 8
     L.edmd_get_counters.argtypes = [C.c_void_p, C.c_int32, C.POINTER(Counters)]
@@ -252,6 +253,12 @@ class Engine:
         ms = C.c_float()
         self._ck(self._L.edmd_get_last_ms(self.h, C.byref(ms)))
         return ms.value
+
+    def last_launches(self):
+        """Kernels launched by the last advance or round call (edmd_get_last_launches)."""
+        n = C.c_int64()
+        self._ck(self._L.edmd_get_last_launches(self.h, C.byref(n)))
+        return n.value
 
     def _ck(self, rc):
         if rc != OK:

@@ -167,7 +167,7 @@ int edmd_advance(edmd_ctx* ctx, int64_t max_coll, double t_stop, uint32_t flags,
  * finishes the pending events earlier than the latest one it processed, so
  * the call always ends on a state of the serial run (ncol may exceed max_coll
  * by the events of that drain).  At most max_rounds rounds are run (rounded up
- * to a multiple of 16).  Thermo rows are not produced.
+ * to a multiple of 32).  Thermo rows are not produced.
  * Collisions, crossings and the final state are those of the serial algorithm
  * unless *violations_out > 0: events processed before an earlier event of the
  * same region, detected exactly with per-cell time stamps (a larger radius
@@ -249,6 +249,11 @@ int edmd_get_engine(const edmd_ctx* ctx);
  * differentiation calls this includes the stream's idle gaps between their
  * kernels).  No reference counterpart (the reference reports no timings). */
 int edmd_get_last_ms(const edmd_ctx* ctx, float* ms);
+
+/* Number of this library's kernels launched by the last edmd_advance or
+ * edmd_advance_rounds call on ctx (graph-launched rounds counted kernel by
+ * kernel).  No reference counterpart. */
+int edmd_get_last_launches(const edmd_ctx* ctx, int64_t* n);
 
 /* Select the CUDA device used by contexts created afterwards in this thread
  * (one process per GPU). */

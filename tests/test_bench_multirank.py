@@ -70,6 +70,9 @@ class Engine:
             self.ncol += max_coll
         return 0, 1.0
 
+    def last_launches(self):
+        return 1
+
     def all_counters(self):
         z = np.zeros(self.n, np.int64)
         return dict(ncol=self.ncol.copy(), npair=self.ncol * 19, npred=self.ncol * 2, growing=z)

@@ -242,3 +242,18 @@ def test_block_rounds_collision_budget(edmd, oracle):
         assert n == c["ncol"][q]
         np.testing.assert_array_equal(eng.state(q)["x"], o.state()["x"])
     eng.close()
+
+
+def test_launch_counts_are_reported(edmd):
+    """edmd_get_last_launches: one persistent launch per serial call; per round
+    the selection, event and recompute/barrier kernels (and the thread-per-event
+    kernel in the graphs that hold it), plus the call's set-up and finish."""
+    s = edmd.hex_start(20000, 0.70, 3)
+    s["desc"] = edmd.default_desc(s["N"], s["Lx"], s["Ly"])
+    eng = edmd.Engine([s])
+    eng.advance(max_coll=1000)
+    assert eng.last_launches() == 1
+    rc, ms, rounds, viol = eng.advance_rounds(max_coll=20000, radius=4, flags=EXACT)
+    n = eng.last_launches()
+    assert rounds > 0 and 3 * rounds + 4 <= n <= 4 * rounds + 5, (n, rounds)
+    eng.close()
