@@ -104,39 +104,50 @@ __global__ void k_gram_sum(const double* __restrict__ Gp, int nblocks, int K, do
   G[e] = s;
 }
 
-// Cholesky G = R^T R (R upper), logs of diag(R) accumulated, Rinv = R^-1
-__device__ void chol_one(const double* __restrict__ G, int K, double* __restrict__ Rinv,
-                         double* __restrict__ logdiag, int accumulate, int* __restrict__ fail) {
-  double R[32][32];
+// Cholesky G = R^T R (R upper) of one K x K Gram matrix by one warp, logs of
+// diag(R) accumulated, Rinv = R^-1.  Right-looking on the warp's shared copy
+// M: step j takes the square root of the pivot, scales row j, and lane c
+// updates column c of the trailing upper triangle; then lane c solves
+// R x = e_c by back substitution into column c of Q.
+__device__ void chol_warp(const double* __restrict__ G, int K, double* __restrict__ Rinv,
+                          double* __restrict__ logdiag, int accumulate, int* __restrict__ fail,
+                          double (*M)[33], double (*Q)[33], int lane) {
   for (int a = 0; a < K; a++)
-    for (int b = 0; b < K; b++) R[a][b] = 0;
-  for (int jj = 0; jj < K; jj++) {
-    double s = G[jj * K + jj];
-    for (int p = 0; p < jj; p++) s -= R[p][jj] * R[p][jj];
-    if (!(s > 0)) { *fail = 1; return; }
-    R[jj][jj] = sqrt(s);
-    for (int c = jj + 1; c < K; c++) {
-      double u = G[jj * K + c];
-      for (int p = 0; p < jj; p++) u -= R[p][jj] * R[p][c];
-      R[jj][c] = u / R[jj][jj];
+    if (lane < K) M[a][lane] = G[a * K + lane];
+  __syncwarp();
+  for (int j = 0; j < K; j++) {
+    const double s = M[j][j];
+    if (!(s > 0)) {                                 // the same value in every lane
+      if (lane == 0) *fail = 1;
+      return;
     }
-  }
-  if (accumulate)
-    for (int a = 0; a < K; a++) logdiag[a] += log(R[a][a]);
-  // invert the upper-triangular R column by column
-  for (int c = 0; c < K; c++) {
-    for (int a = K - 1; a >= 0; a--) {
-      double s = (a == c) ? 1.0 : 0.0;
-      for (int p = a + 1; p < K; p++) s -= R[a][p] * Rinv[p * K + c];
-      Rinv[a * K + c] = s / R[a][a];
+    const double d = sqrt(s);
+    __syncwarp();
+    if (lane > j && lane < K) M[j][lane] /= d;
+    if (lane == j) M[j][j] = d;
+    __syncwarp();
+    if (lane > j && lane < K) {
+      const double rjc = M[j][lane];
+      for (int a2 = j + 1; a2 <= lane; a2++) M[a2][lane] -= M[j][a2] * rjc;
     }
+    __syncwarp();
   }
+  if (accumulate && lane < K) logdiag[lane] += log(M[lane][lane]);
+  if (lane < K) {
+    for (int a2 = K - 1; a2 >= 0; a2--) {
+      double v = (a2 == lane) ? 1.0 : 0.0;
+      for (int p = a2 + 1; p < K; p++) v -= M[a2][p] * Q[p][lane];
+      Q[a2][lane] = v / M[a2][a2];
+    }
+    for (int a2 = 0; a2 < K; a2++) Rinv[a2 * K + lane] = Q[a2][lane];
+  }
+  __syncwarp();
 }
 
-__global__ void k_chol(const double* __restrict__ G, int K, double* __restrict__ Rinv,
-                       double* __restrict__ logdiag, int accumulate, int* __restrict__ fail) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  chol_one(G, K, Rinv, logdiag, accumulate, fail);
+__global__ void __launch_bounds__(32) k_chol(const double* __restrict__ G, int K, double* __restrict__ Rinv,
+                                             double* __restrict__ logdiag, int accumulate, int* __restrict__ fail) {
+  __shared__ double M[32][33], Q[32][33];
+  chol_warp(G, K, Rinv, logdiag, accumulate, fail, M, Q, threadIdx.x);
 }
 
 // T <- T' Rinv at the common time tq (every disk's tangent clock set to tq)
@@ -270,18 +281,25 @@ __global__ void k_gram_b(const SysDev* __restrict__ sys, const int64_t* __restri
     const int e = e0 + l;
     rows[l][k] = (e < 4 * N && k < K) ? row_at(Ts, tls, e, k, K, tq) : 0.0;
     __syncthreads();
-    if (k < K && l < K)
+    if (k <= l && l < K)                            // the upper triangle; G is symmetric
       for (int r = 0; r < 32; r++) acc += rows[r][k] * rows[r][l];
     __syncthreads();
   }
-  if (k < K && l < K) G[(size_t)blockIdx.x * K * K + k * K + l] = acc;
+  if (k <= l && l < K) {
+    G[(size_t)blockIdx.x * K * K + k * K + l] = acc;
+    G[(size_t)blockIdx.x * K * K + l * K + k] = acc;
+  }
 }
 
-__global__ void k_chol_b(const double* __restrict__ G, int nsys, int K, double* __restrict__ Rinv,
-                         double* __restrict__ logdiag, int accumulate, int* __restrict__ fail) {
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+// one warp per system
+__global__ void __launch_bounds__(32) k_chol_b(const double* __restrict__ G, int nsys, int K,
+                                               double* __restrict__ Rinv, double* __restrict__ logdiag,
+                                               int accumulate, int* __restrict__ fail) {
+  __shared__ double M[32][33], Q[32][33];
+  const int s = blockIdx.x;
   if (s >= nsys) return;
-  chol_one(G + (size_t)s * K * K, K, Rinv + (size_t)s * K * K, logdiag + (size_t)s * K, accumulate, fail + s);
+  chol_warp(G + (size_t)s * K * K, K, Rinv + (size_t)s * K * K, logdiag + (size_t)s * K, accumulate, fail + s,
+            M, Q, threadIdx.x);
 }
 
 __global__ void k_apply_rinv_b(const SysDev* __restrict__ sys, const int64_t* __restrict__ doff,
@@ -529,7 +547,7 @@ static int cholqr(edmd_ctx* ctx, double* T, double* tl, int N, int K, double tq,
     if (blocks > GRAM_BLOCKS) blocks = GRAM_BLOCKS;
     k_gram<<<blocks, 1024, 0, ctx->stream>>>(T, tl, N, K, tq, Gp);
     k_gram_sum<<<1, 1024, 0, ctx->stream>>>(Gp, blocks, K, G);
-    k_chol<<<1, 1, 0, ctx->stream>>>(G, K, Rinv, logdiag, accumulate ? 1 : 0, fail);
+    k_chol<<<1, 32, 0, ctx->stream>>>(G, K, Rinv, logdiag, accumulate ? 1 : 0, fail);
     k_apply_rinv<<<(N + 127) / 128, 128, 0, ctx->stream>>>(T, tl, N, K, tq, Rinv);
     CK(cudaGetLastError());
   }
@@ -746,7 +764,7 @@ int cholqr_b(edmd_ctx* ctx, const BatchIndex& bi, double* T, double* tl, int K, 
   const int64_t TN = ctx->total_N;
   for (int pass = 0; pass < 2; pass++) {    // CholQR2: the second pass restores orthogonality
     k_gram_b<<<ctx->nsys, 1024, 0, ctx->stream>>>(ctx->ds, bi.doff, T, tl, K, G);
-    k_chol_b<<<(ctx->nsys + 63) / 64, 64, 0, ctx->stream>>>(G, ctx->nsys, K, Rinv, logdiag, accumulate ? 1 : 0,
+    k_chol_b<<<ctx->nsys, 32, 0, ctx->stream>>>(G, ctx->nsys, K, Rinv, logdiag, accumulate ? 1 : 0,
                                                             fail);
     k_apply_rinv_b<<<(unsigned)((TN + 127) / 128), 128, 0, ctx->stream>>>(ctx->ds, bi.doff, bi.dsys, TN, T, tl,
                                                                          K, Rinv);
