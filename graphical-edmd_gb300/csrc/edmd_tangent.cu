@@ -267,11 +267,11 @@ __global__ void k_tangent_apply_b(const SysDev* __restrict__ sys, const int64_t*
 // time, rows taken 32 at a time in index order (deterministic)
 __global__ void k_gram_b(const SysDev* __restrict__ sys, const int64_t* __restrict__ doff,
                          const double* __restrict__ T, const double* __restrict__ tl, int K,
-                         double* __restrict__ G) {
+                         const double* __restrict__ tqs, double* __restrict__ G) {
   __shared__ double rows[32][33];
   const SysDev& S = sys[blockIdx.x];
   const int N = S.B.N;
-  const double tq = S.st->t;
+  const double tq = tqs[blockIdx.x];            // the system's time at the end of the chunk
   const int64_t o = doff[blockIdx.x];
   const double* Ts = T + (size_t)4 * o * K;
   const double* tls = tl + o;
@@ -302,14 +302,14 @@ __global__ void __launch_bounds__(32) k_chol_b(const double* __restrict__ G, int
             M, Q, threadIdx.x);
 }
 
-__global__ void k_apply_rinv_b(const SysDev* __restrict__ sys, const int64_t* __restrict__ doff,
-                               const int32_t* __restrict__ dsys, int64_t TN, double* __restrict__ T,
-                               double* __restrict__ tl, int K, const double* __restrict__ Rinv) {
+__global__ void k_apply_rinv_b(const int64_t* __restrict__ doff, const int32_t* __restrict__ dsys, int64_t TN,
+                               double* __restrict__ T, double* __restrict__ tl, int K,
+                               const double* __restrict__ tqs, const double* __restrict__ Rinv) {
   const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= TN) return;
   const int s = dsys[g];
   const int64_t o = doff[s];
-  apply_rinv_disk(T + (size_t)4 * o * K, tl + o, (int)(g - o), K, sys[s].st->t, Rinv + (size_t)s * K * K);
+  apply_rinv_disk(T + (size_t)4 * o * K, tl + o, (int)(g - o), K, tqs[s], Rinv + (size_t)s * K * K);
 }
 
 // one thread per system: the transposed map backwards over its segment log
@@ -759,17 +759,20 @@ int advance_logged_all(edmd_ctx* ctx, int64_t ncoll) {
   return EDMD_OK;
 }
 
+// CholQR2 of every system's tangent block at the times tqs, on stream st
 int cholqr_b(edmd_ctx* ctx, const BatchIndex& bi, double* T, double* tl, int K, double* G, double* Rinv,
-             double* logdiag, int* fail, bool accumulate) {
+             double* logdiag, int* fail, bool accumulate, const double* tqs, cudaStream_t st) {
   const int64_t TN = ctx->total_N;
   for (int pass = 0; pass < 2; pass++) {    // CholQR2: the second pass restores orthogonality
-    k_gram_b<<<ctx->nsys, 1024, 0, ctx->stream>>>(ctx->ds, bi.doff, T, tl, K, G);
-    k_chol_b<<<ctx->nsys, 32, 0, ctx->stream>>>(G, ctx->nsys, K, Rinv, logdiag, accumulate ? 1 : 0,
-                                                            fail);
-    k_apply_rinv_b<<<(unsigned)((TN + 127) / 128), 128, 0, ctx->stream>>>(ctx->ds, bi.doff, bi.dsys, TN, T, tl,
-                                                                         K, Rinv);
+    k_gram_b<<<ctx->nsys, 1024, 0, st>>>(ctx->ds, bi.doff, T, tl, K, tqs, G);
+    k_chol_b<<<ctx->nsys, 32, 0, st>>>(G, ctx->nsys, K, Rinv, logdiag, accumulate ? 1 : 0, fail);
+    k_apply_rinv_b<<<(unsigned)((TN + 127) / 128), 128, 0, st>>>(bi.doff, bi.dsys, TN, T, tl, K, tqs, Rinv);
     CK(cudaGetLastError());
   }
+  return EDMD_OK;
+}
+
+int check_fail(edmd_ctx* ctx, const int* fail) {
   std::vector<int> h(ctx->nsys);
   CK(sync_copy(ctx, h.data(), fail, ctx->nsys * sizeof(int), cudaMemcpyDeviceToHost));
   for (int s = 0; s < ctx->nsys; s++)
@@ -796,7 +799,7 @@ extern "C" int edmd_tangent_run_batch(edmd_ctx* ctx, int32_t K, int64_t n_coll, 
   if (rc) return rc;
   BatchIndex bi;
   if ((rc = batch_index(ctx, bi))) return rc;
-  double *T = nullptr, *tl = nullptr, *G = nullptr, *Rinv = nullptr, *logdiag = nullptr;
+  double *T = nullptr, *tl = nullptr, *G = nullptr, *Rinv = nullptr, *logdiag = nullptr, *tqs = nullptr;
   int* fail = nullptr;
   CK(dalloc(&T, (size_t)4 * TN * K));
   CK(dalloc(&tl, TN));
@@ -804,7 +807,19 @@ extern "C" int edmd_tangent_run_batch(edmd_ctx* ctx, int32_t K, int64_t n_coll, 
   CK(dalloc(&Rinv, (size_t)nsys * K * K));
   CK(dalloc(&logdiag, (size_t)nsys * K));
   CK(dalloc(&fail, nsys));
-  struct Free { void* p[6]; ~Free() { for (void* q : p) if (q) cudaFree(q); } } guard{{T, tl, G, Rinv, logdiag, fail}};
+  CK(dalloc(&tqs, nsys));
+  struct Free { void* p[7]; ~Free() { for (void* q : p) if (q) cudaFree(q); } } guard{{T, tl, G, Rinv, logdiag, fail, tqs}};
+  // the QR of a chunk runs on a second stream beside the next chunk's forward
+  // run (which does not touch the tangent vectors); the next tangent map
+  // waits for it
+  if (!ctx->stream2) CK(cudaStreamCreateWithFlags(&ctx->stream2, cudaStreamNonBlocking));
+  struct Ev {
+    cudaEvent_t e = nullptr;
+    ~Ev() { if (e) cudaEventDestroy(e); }
+  } ea, eq;
+  CK(cudaEventCreateWithFlags(&ea.e, cudaEventDisableTiming));
+  CK(cudaEventCreateWithFlags(&eq.e, cudaEventDisableTiming));
+  const unsigned gs = (unsigned)((nsys + 127) / 128);
   // system s starts from the vectors edmd_tangent_run draws from seed + s
   // (drawn on the host before the timed part of the call)
   std::vector<double> h((size_t)4 * TN * K);
@@ -821,15 +836,26 @@ extern "C" int edmd_tangent_run_batch(edmd_ctx* ctx, int32_t K, int64_t n_coll, 
   k_fill_sys_time<<<(unsigned)((TN + 255) / 256), 256, 0, ctx->stream>>>(ctx->ds, bi.dsys, TN, tl);
   CK(cudaMemsetAsync(logdiag, 0, (size_t)nsys * K * sizeof(double), ctx->stream));
   CK(cudaMemsetAsync(fail, 0, nsys * sizeof(int), ctx->stream));
-  if ((rc = cholqr_b(ctx, bi, T, tl, K, G, Rinv, logdiag, fail, false))) return rc;
+  k_sys_times<<<gs, 128, 0, ctx->stream>>>(ctx->ds, nsys, tqs);
+  if ((rc = cholqr_b(ctx, bi, T, tl, K, G, Rinv, logdiag, fail, false, tqs, ctx->stream))) return rc;
+  CK(cudaEventRecord(eq.e, ctx->stream));
   for (int64_t done = 0; done < n_coll;) {
     const int64_t want = n_coll - done < chunk ? n_coll - done : chunk;
     if ((rc = advance_logged_all(ctx, want))) return rc;
+    CK(cudaStreamWaitEvent(ctx->stream, eq.e, 0));             // the previous QR is done
     k_tangent_apply_b<<<nsys, 32, 0, ctx->stream>>>(ctx->ds, bi.doff, T, tl, K);
     CK(cudaGetLastError());
-    if (qr_every > 0 && (rc = cholqr_b(ctx, bi, T, tl, K, G, Rinv, logdiag, fail, true))) return rc;
+    if (qr_every > 0) {
+      k_sys_times<<<gs, 128, 0, ctx->stream>>>(ctx->ds, nsys, tqs);   // the chunk's end times
+      CK(cudaEventRecord(ea.e, ctx->stream));
+      CK(cudaStreamWaitEvent(ctx->stream2, ea.e, 0));
+      if ((rc = cholqr_b(ctx, bi, T, tl, K, G, Rinv, logdiag, fail, true, tqs, ctx->stream2))) return rc;
+      CK(cudaEventRecord(eq.e, ctx->stream2));
+    }
     done += want;
   }
+  CK(cudaStreamWaitEvent(ctx->stream, eq.e, 0));
+  if ((rc = check_fail(ctx, fail))) return rc;
   if (lyap_out) {
     std::vector<double> ld((size_t)nsys * K);
     CK(sync_copy(ctx, ld.data(), logdiag, ld.size() * 8, cudaMemcpyDeviceToHost));
