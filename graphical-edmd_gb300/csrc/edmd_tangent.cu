@@ -81,7 +81,8 @@ __device__ __forceinline__ double row_at(const double* T, const double* tl, int 
 // over the blocks in a fixed order by k_gram_sum, so the result is
 // reproducible run to run
 __global__ void k_gram(const double* __restrict__ T, const double* __restrict__ tl, int N, int K,
-                       double tq, double* __restrict__ Gp) {
+                       const double* __restrict__ tqp, double* __restrict__ Gp) {
+  const double tq = *tqp;
   __shared__ double rows[32][33];
   const int k = threadIdx.x & 31, l = threadIdx.x >> 5;   // 32 x 32 threads
   double acc = 0;
@@ -165,8 +166,9 @@ __device__ __forceinline__ void apply_rinv_disk(double* __restrict__ T, double* 
   tl[i] = tq;
 }
 
-__global__ void k_apply_rinv(double* __restrict__ T, double* __restrict__ tl, int N, int K, double tq,
-                             const double* __restrict__ Rinv) {
+__global__ void k_apply_rinv(double* __restrict__ T, double* __restrict__ tl, int N, int K,
+                             const double* __restrict__ tqp, const double* __restrict__ Rinv) {
+  const double tq = *tqp;
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= N) return;
   apply_rinv_disk(T, tl, i, K, tq, Rinv);
@@ -540,20 +542,18 @@ static int advance_logged(edmd_ctx* ctx, int s, int64_t ncoll, int64_t* nlog) {
 
 constexpr int GRAM_BLOCKS = 1024;
 
-static int cholqr(edmd_ctx* ctx, double* T, double* tl, int N, int K, double tq, double* G, double* Gp,
-                  double* Rinv, double* logdiag, int* fail, bool accumulate) {
+// CholQR2 of one system's tangent block at the time *tqp, on stream st
+static int cholqr(edmd_ctx* ctx, double* T, double* tl, int N, int K, const double* tqp, double* G, double* Gp,
+                  double* Rinv, double* logdiag, int* fail, bool accumulate, cudaStream_t st) {
   for (int pass = 0; pass < 2; pass++) {    // CholQR2: the second pass restores orthogonality
     int blocks = (4 * N + 31) / 32;
     if (blocks > GRAM_BLOCKS) blocks = GRAM_BLOCKS;
-    k_gram<<<blocks, 1024, 0, ctx->stream>>>(T, tl, N, K, tq, Gp);
-    k_gram_sum<<<1, 1024, 0, ctx->stream>>>(Gp, blocks, K, G);
-    k_chol<<<1, 32, 0, ctx->stream>>>(G, K, Rinv, logdiag, accumulate ? 1 : 0, fail);
-    k_apply_rinv<<<(N + 127) / 128, 128, 0, ctx->stream>>>(T, tl, N, K, tq, Rinv);
+    k_gram<<<blocks, 1024, 0, st>>>(T, tl, N, K, tqp, Gp);
+    k_gram_sum<<<1, 1024, 0, st>>>(Gp, blocks, K, G);
+    k_chol<<<1, 32, 0, st>>>(G, K, Rinv, logdiag, accumulate ? 1 : 0, fail);
+    k_apply_rinv<<<(N + 127) / 128, 128, 0, st>>>(T, tl, N, K, tqp, Rinv);
     CK(cudaGetLastError());
   }
-  int h = 0;
-  CK(sync_copy(ctx, &h, fail, 4, cudaMemcpyDeviceToHost));
-  if (h) return set_err(ctx, EDMD_ERR_ARG, "tangent vectors became linearly dependent");
   return EDMD_OK;
 }
 
@@ -567,6 +567,7 @@ extern "C" int edmd_tangent_run(edmd_ctx* ctx, int32_t s, int32_t K, int64_t n_c
   int rc = edmd_set_log_capacity(ctx, chunk + 16);
   if (rc) return rc;
   double *T = nullptr, *tl = nullptr, *G = nullptr, *Gp = nullptr, *Rinv = nullptr, *logdiag = nullptr;
+  double* tqd = nullptr;
   int* fail = nullptr;
   CK(dalloc(&T, (size_t)4 * N * K));
   CK(dalloc(&tl, N));
@@ -575,7 +576,17 @@ extern "C" int edmd_tangent_run(edmd_ctx* ctx, int32_t s, int32_t K, int64_t n_c
   CK(dalloc(&Rinv, K * K));
   CK(dalloc(&logdiag, K));
   CK(dalloc(&fail, 1));
-  struct Free { void* p[7]; ~Free() { for (void* q : p) if (q) cudaFree(q); } } guard{{T, tl, G, Gp, Rinv, logdiag, fail}};
+  CK(dalloc(&tqd, 1));
+  struct Free { void* p[8]; ~Free() { for (void* q : p) if (q) cudaFree(q); } } guard{{T, tl, G, Gp, Rinv, logdiag, fail, tqd}};
+  // as in the batched form: each chunk's QR on a second stream beside the
+  // next chunk's forward run, at the chunk's end time copied on the device
+  if (!ctx->stream2) CK(cudaStreamCreateWithFlags(&ctx->stream2, cudaStreamNonBlocking));
+  struct Ev {
+    cudaEvent_t e = nullptr;
+    ~Ev() { if (e) cudaEventDestroy(e); }
+  } ea, eq;
+  CK(cudaEventCreateWithFlags(&ea.e, cudaEventDisableTiming));
+  CK(cudaEventCreateWithFlags(&eq.e, cudaEventDisableTiming));
   CK(call_begin(ctx));
   double t0;
   if ((rc = current_time(ctx, s, &t0))) return rc;
@@ -593,20 +604,36 @@ extern "C" int edmd_tangent_run(edmd_ctx* ctx, int32_t s, int32_t K, int64_t n_c
   k_fill<<<(N + 255) / 256, 256, 0, ctx->stream>>>(tl, N, t0);
   CK(cudaMemsetAsync(logdiag, 0, K * sizeof(double), ctx->stream));
   CK(cudaMemsetAsync(fail, 0, 4, ctx->stream));
-  if (!tangent_io && (rc = cholqr(ctx, T, tl, N, K, t0, G, Gp, Rinv, logdiag, fail, false))) return rc;
+  k_sys_times<<<1, 32, 0, ctx->stream>>>(ctx->ds + s, 1, tqd);
+  if (!tangent_io && (rc = cholqr(ctx, T, tl, N, K, tqd, G, Gp, Rinv, logdiag, fail, false, ctx->stream)))
+    return rc;
+  CK(cudaEventRecord(eq.e, ctx->stream));
   int64_t done = 0;
-  double t = t0;
   while (done < n_coll) {
     int64_t want = n_coll - done < chunk ? n_coll - done : chunk;
     int64_t nl = 0;
     if ((rc = advance_logged(ctx, s, want, &nl))) return rc;
+    CK(cudaStreamWaitEvent(ctx->stream, eq.e, 0));             // the previous QR is done
     k_tangent_apply<<<1, 32, 0, ctx->stream>>>((const edmd_log_entry*)ctx->hs[s].log, nl, ctx->hs[s].d, T, tl, K);
     CK(cudaGetLastError());
-    if ((rc = current_time(ctx, s, &t))) return rc;
-    if (qr_every > 0 && (rc = cholqr(ctx, T, tl, N, K, t, G, Gp, Rinv, logdiag, fail, true))) return rc;
+    if (qr_every > 0) {
+      k_sys_times<<<1, 32, 0, ctx->stream>>>(ctx->ds + s, 1, tqd);
+      CK(cudaEventRecord(ea.e, ctx->stream));
+      CK(cudaStreamWaitEvent(ctx->stream2, ea.e, 0));
+      if ((rc = cholqr(ctx, T, tl, N, K, tqd, G, Gp, Rinv, logdiag, fail, true, ctx->stream2))) return rc;
+      CK(cudaEventRecord(eq.e, ctx->stream2));
+    }
     done += want;
     if (nl < want) break;     // the run ended early (tmax or t_stop)
   }
+  CK(cudaStreamWaitEvent(ctx->stream, eq.e, 0));
+  {
+    int hf = 0;
+    CK(sync_copy(ctx, &hf, fail, 4, cudaMemcpyDeviceToHost));
+    if (hf) return set_err(ctx, EDMD_ERR_ARG, "tangent vectors became linearly dependent");
+  }
+  double t = t0;
+  if ((rc = current_time(ctx, s, &t))) return rc;
   if (lyap_out) {
     std::vector<double> ld(K);
     CK(sync_copy(ctx, ld.data(), logdiag, K * 8, cudaMemcpyDeviceToHost));
