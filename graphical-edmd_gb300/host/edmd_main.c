@@ -366,7 +366,7 @@ int main(int argc, char* argv[])
 	d.contact = o.additive ? EDMD_CONTACT_ADDITIVE : EDMD_CONTACT_NONADDITIVE;
 	edmd_ctx* ctx = NULL;
 	int rc = edmd_create(1, &d, a[0], a[1], a[2], a[3], a[4], a[5], vr_base > 0 ? a[6] : NULL, 0, &ctx);
-	if (rc != EDMD_OK) die("engine creation failed", ctx);
+	if (rc != EDMD_OK) die(rc == EDMD_ERR_NODEV ? "no CUDA device" : "engine creation failed", ctx);
 
 	FILE* dump = fopen(fileName, "w");
 	FILE* thermo = fopen(thermoName, "w");
