@@ -88,6 +88,7 @@ struct RoundArgs {
   uint64_t* lw; uint64_t* lr;    // causality stamps per cell
   int32_t* safe; int32_t* nsafe; // selected events of the round
   int32_t* nsafe_next;           // the next round's count (two alternate), emptied in this round
+  int32_t* pnext;                // events taken past the first wave of the event kernel, emptied after the round
   int32_t* dcell;                // cells to recompute, MAXDIRTY per selected event
   int32_t* selflag;              // some event of the system was selected
   int32_t* active;               // systems still running after the round
@@ -1146,6 +1147,16 @@ __device__ __forceinline__ uint64_t group_max(unsigned m, uint64_t v) {
   return acc;
 }
 
+// the next chunk of a round's selected events for a warp of an event kernel:
+// past the first wave (each warp's own index), chunks in the order the
+// warps ask for them; none when the first wave holds the whole selection
+__device__ __forceinline__ int next_chunk(const RoundArgs& A, int lane, int wave, int chunk, int nsafe) {
+  if (nsafe <= wave) return nsafe;
+  int q = 0;
+  if (lane == 0) q = atomicAdd(A.pnext, 1);
+  return wave + chunk * __shfl_sync(FULLM, q, 0);
+}
+
 // the selected events of a round, one thread each (rounds of at least
 // A.thr_min events; k_process takes the others); per-system counters are
 // summed over the lanes of a warp that share the system before one atomic
@@ -1156,7 +1167,9 @@ __global__ void __launch_bounds__(32, 16) k_process_thread(const SysDev* __restr
   const int wstart = (blockIdx.x * blockDim.x + threadIdx.x) - lane;
   const int wstride = gridDim.x * blockDim.x;
   const int stripe = (wstart >> 5) & (NSTRIPE - 1);
-  for (int w = wstart; w < nsafe; w += wstride) {
+  // one resident wave: each warp takes the 32 events at its own index, then
+  // the warps that finish first take the rest, 32 at a time, from a counter
+  for (int w = wstart; w < nsafe; w = next_chunk(A, lane, wstride, 32, nsafe)) {
     const int n = w + lane;
     const bool valid = n < nsafe;
     int s = -1;
@@ -1216,7 +1229,10 @@ __global__ void __launch_bounds__(32 * WPB, 20) k_process(const SysDev* __restri
   if (A.thread_kernel && nsafe >= A.thr_min) return;   // k_process_thread takes the round
   const int gw = blockIdx.x * WPB + wid, nw = gridDim.x * WPB;
   const int stripe = gw & (NSTRIPE - 1);
-  for (int n = gw; n < nsafe; n += nw) {
+  // one resident wave: each warp takes the event at its own index, then the
+  // warps that finish first take the rest from a counter (a grid of one
+  // block per event would mostly launch blocks that find nothing to do)
+  for (int n = gw; n < nsafe; n = next_chunk(A, lane, nw, 1, nsafe)) {
     const int64_t g = A.safe[n];
     const int s = A.dsys[g];
     EvResult r;
@@ -1555,7 +1571,10 @@ __device__ void barrier_systems(const SysDev* __restrict__ sys, const RoundArgs&
 __global__ void __launch_bounds__(256) k_recompute_barrier(const SysDev* __restrict__ sys, RoundArgs A,
                                                           int nbar) {
   // the next round's selection count starts empty (this round's is still read)
-  if (blockIdx.x == 0 && threadIdx.x == 0) *A.nsafe_next = 0;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    *A.nsafe_next = 0;
+    *A.pnext = 0;                    // the event kernels of this round are done with it
+  }
   if ((int)blockIdx.x < nbar) barrier_systems(sys, A, blockIdx.x, nbar);
   recompute_cells(sys, A);
 }
@@ -1640,7 +1659,7 @@ int round_init(edmd_ctx* ctx) {
   CK(dalloc(&R->drank, TN)); CK(dalloc(&R->drank_bak, TN));
   CK(dalloc(&R->ikb, TN)); CK(dalloc(&R->iktie, TN));
   CK(dalloc(&R->cmi, TC)); CK(dalloc(&R->cmt, TC)); CK(dalloc(&R->lw, TC)); CK(dalloc(&R->lr, TC));
-  CK(dalloc(&R->safe, TN)); CK(dalloc(&R->nsafe, 2)); CK(dalloc(&R->dcell, TN * MAXDIRTY));
+  CK(dalloc(&R->safe, TN)); CK(dalloc(&R->nsafe, 3)); CK(dalloc(&R->dcell, TN * MAXDIRTY));
   CK(dalloc(&R->selflag, ctx->nsys)); CK(dalloc(&R->active, 2)); CK(dalloc(&R->work, 1));
   CK(dalloc(&R->doff, ctx->nsys)); CK(dalloc(&R->coff, ctx->nsys));
   CK(dalloc(&R->lim, ctx->nsys)); CK(dalloc(&R->target, ctx->nsys)); CK(dalloc(&R->freeze, ctx->nsys));
@@ -1690,8 +1709,10 @@ cudaError_t enqueue_round(edmd_ctx* ctx, const RoundBufs* R, const RoundArgs& A0
 #undef SEL_CASE
     default: break;   // radius is checked to be 3..RTILE before any round
   }
-  k_process<<<nsm * 160, 32 * WPB, 0, st>>>(ctx->ds, A);
-  if (with_thread) k_process_thread<<<nsm * 128, 32, 0, st>>>(ctx->ds, A);   // one-warp blocks, 16 per SM: measured best
+  // one resident wave of each event kernel: one-warp blocks, 20 per SM (k_process)
+  // and 16 per SM (k_process_thread), measured best
+  k_process<<<nsm * 20 / WPB, 32 * WPB, 0, st>>>(ctx->ds, A);
+  if (with_thread) k_process_thread<<<nsm * 16, 32, 0, st>>>(ctx->ds, A);
   k_recompute_barrier<<<nsm * 8, 256, 0, st>>>(ctx->ds, A, ctx->nsys < nsm * 8 ? ctx->nsys : nsm * 8);
   return cudaGetLastError();
 }
@@ -1739,6 +1760,7 @@ static int run_rounds(edmd_ctx* ctx, const std::vector<uint64_t>& tgt, double t_
   A.dsys = R->dsys; A.doff = R->doff; A.coff = R->coff;
   A.dkey = R->dkey; A.dpk = R->dpk; A.drank = R->drank; A.ikb = R->ikb; A.iktie = R->iktie; A.fc = R->fc; A.cmt = R->cmt; A.cmi = R->cmi; A.lw = R->lw; A.lr = R->lr;
   A.safe = R->safe; A.nsafe = R->nsafe; A.dcell = R->dcell; A.selflag = R->selflag;
+  A.pnext = R->nsafe + 2;
   A.active = R->active; A.lim = R->lim; A.target = R->target; A.freeze = R->freeze;
   A.maxsafe = R->active + 1; A.thread_kernel = 1;
   // one thread per event needs enough events to keep every SM busy with one
@@ -1820,7 +1842,7 @@ static int run_rounds(edmd_ctx* ctx, const std::vector<uint64_t>& tgt, double t_
   int64_t rounds = 0;
   int32_t active = 1;
   bool with_thread = may_thread;
-  ce = cudaMemsetAsync(R->nsafe, 0, 8, st);
+  ce = cudaMemsetAsync(R->nsafe, 0, 12, st);
   while (ce == cudaSuccess && active && rounds < max_rounds) {
     if (!exec[with_thread ? 1 : 0]) {
       ce = capture(with_thread, &exec[with_thread ? 1 : 0]);
