@@ -72,6 +72,11 @@ METRICS = {
 }
 DEFAULT_COLL = {"batched": 100000, "single_large": 20000000, "single_4m": 100000000, "plain_small": 100000}
 DEFAULT_ENGINE = {"batched": "warp", "single_large": "round", "single_4m": "round", "plain_small": "round"}
+# window radius of the round engine: 3 for the small system (~1.5x the
+# collisions a round of 4 gives, no replays), 4 for the large ones (3 gives
+# them no more collisions a round, and its rarer causality violations
+# replay whole calls)
+DEFAULT_RADIUS = {"batched": 4, "single_large": 4, "single_4m": 4, "plain_small": 3}
 LARGE_N, LARGE_PHI, LARGE_EQUIL = 1000000, 0.72, 100000
 SINGLE = {"single_large": (LARGE_N, LARGE_PHI), "single_4m": (4000000, 0.78)}
 DIFF_N, DIFF_PHI, DIFF_SEED, DIFF_COLL = 1024, 0.60, 11, 10000
@@ -561,6 +566,7 @@ class Stepper:
 
 def measure(edmd, a, workload, engine, coll, steps, warmup, rank, world, dist, dev, e2e_steps):
     nsys = a.nsys if a.nsys is not None else (4096 if workload == "batched" else 1)
+    radius = a.radius if a.radius is not None else DEFAULT_RADIUS[workload]
     systems = build_systems(edmd, workload, nsys, a.seed, rank)
     edmd.set_warp_group(a.warp_group)
     eng = edmd.Engine(systems, engine=edmd.ENGINE_LANE if engine == "lane" else edmd.ENGINE_WARP)
@@ -571,7 +577,7 @@ def measure(edmd, a, workload, engine, coll, steps, warmup, rank, world, dist, d
         c = eng.all_counters()
         assert not c["growing"].any(), "growth did not finish"
     elif workload in SINGLE:
-        eng.advance_rounds(max_coll=LARGE_EQUIL, radius=a.radius, flags=edmd.F_EXACT)
+        eng.advance_rounds(max_coll=LARGE_EQUIL, radius=radius, flags=edmd.F_EXACT)
     tuned = None
     extra = edmd.F_SMEM if (getattr(a, "smem", False) and engine == "warp") else 0
     if workload == "batched" and engine == "warp" and getattr(a, "tune", False):
@@ -590,7 +596,7 @@ def measure(edmd, a, workload, engine, coll, steps, warmup, rank, world, dist, d
             eng = edmd.Engine(grown, engine=edmd.ENGINE_LANE if tuned["engine"] == "lane" else edmd.ENGINE_WARP)
             engine = tuned["engine"]
         extra = tuned["flags"]
-    st = Stepper(edmd, eng, engine, coll, a.radius)
+    st = Stepper(edmd, eng, engine, coll, radius)
     if engine == "round" and getattr(a, "round_block", False):
         extra |= edmd.F_ROUND_BLOCK
     st.extra_flags = extra
@@ -621,7 +627,7 @@ def measure(edmd, a, workload, engine, coll, steps, warmup, rank, world, dist, d
     value = coll_all / t_max
     screen = None
     if workload == "single_4m" and getattr(a, "screen_compare", False):
-        screen = compare_screen(edmd, a, systems[0], eng, steps, coll, c1)
+        screen = compare_screen(edmd, a, systems[0], eng, steps, coll, c1, radius)
     # ---- end to end through the C ABI with pinned host buffers
     eng.sync()
     stt = eng.states()
@@ -680,7 +686,7 @@ def measure(edmd, a, workload, engine, coll, steps, warmup, rank, world, dist, d
         roof["fp32_screen"] = screen
     return dict(value=value, ms_per_step=1000 * t_max / steps, wall=wall, clocks=clocks, launches=launches,
                 engine=engine, lanes=(tuned["lanes"] if tuned else a.warp_group) if engine == "warp" else None,
-                l2=flush.describe(),
+                l2=flush.describe(), radius=radius if engine == "round" else None,
                 smem=bool(extra), tuned=tuned,
                 systems=len(systems), TN=TN, e2e=e2e, h2d=h2d, d2h=d2h, roofline=roof)
 
@@ -689,7 +695,7 @@ def _kinetic(st):
     return 0.5 * float(np.sum(st["m"] * (st["vx"] ** 2 + st["vy"] ** 2)))
 
 
-def compare_screen(edmd, a, sysd, eng_fp64, steps, coll, c_fp64):
+def compare_screen(edmd, a, sysd, eng_fp64, steps, coll, c_fp64, radius):
     """The precision configuration: the same system, equilibration and timed
     steps again with the FP32 screen of separating pairs (EDMD_F_SCREEN),
     against the all-FP64 run just measured.  Missed collisions show as a
@@ -699,9 +705,9 @@ def compare_screen(edmd, a, sysd, eng_fp64, steps, coll, c_fp64):
     eng_fp64.sync()
     st64 = eng_fp64.states()
     e2 = edmd.Engine([sysd])
-    e2.advance_rounds(max_coll=LARGE_EQUIL, radius=a.radius, flags=edmd.F_EXACT)
+    e2.advance_rounds(max_coll=LARGE_EQUIL, radius=radius, flags=edmd.F_EXACT)
     for _ in range(a.warmup):
-        e2.advance_rounds(max_coll=coll, radius=a.radius, flags=edmd.F_EXACT | edmd.F_SCREEN)
+        e2.advance_rounds(max_coll=coll, radius=radius, flags=edmd.F_EXACT | edmd.F_SCREEN)
     # velocities only: a free flight of every disk here would change the
     # rounding of the positions and part the two runs
     e_start = _kinetic(e2.states())
@@ -710,7 +716,7 @@ def compare_screen(edmd, a, sysd, eng_fp64, steps, coll, c_fp64):
     c0 = e2.counters(0)
     ms = 0.0
     for _ in range(steps):
-        ms += e2.advance_rounds(max_coll=coll, radius=a.radius, flags=edmd.F_EXACT | edmd.F_SCREEN)[1]
+        ms += e2.advance_rounds(max_coll=coll, radius=radius, flags=edmd.F_EXACT | edmd.F_SCREEN)[1]
     c1 = e2.counters(0)
     e2.sync()
     st32 = e2.states()
@@ -847,7 +853,7 @@ def run_ours(a, rank, world, dist):
         s = measure(edmd, a, "single_large", "round", DEFAULT_COLL["single_large"], 3, 3, rank, world,
                     dist, dev, 1)
         other["single_large"] = {"metric": METRICS["single_large"], "value": s["value"], "unit": UNIT,
-                                 "engine": "round (exact mode, radius %d)" % a.radius, "l2": s["l2"],
+                                 "engine": "round (exact mode, radius %d)" % s["radius"], "l2": s["l2"],
                                  "ms_per_step": s["ms_per_step"], "e2e": s["e2e"],
                                  "roofline": s["roofline"], "clocks": s["clocks"],
                                  "gpu_launches": s["launches"]}
@@ -880,7 +886,8 @@ def run_ours(a, rank, world, dist):
         "metric": METRICS[workload], "value": r["value"], "unit": UNIT, "n_gpus": world,
         "steps": a.steps, "warmup": a.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": workload_desc, "engine": r["engine"], "systems_per_gpu": r["systems"],
+        "config": {"workload": workload_desc, "engine": r["engine"], "window_radius": r["radius"],
+                   "systems_per_gpu": r["systems"],
                    "disks_per_gpu": r["TN"], "collisions_per_system_per_step": coll,
                    "l2": r["l2"],
                    "parallelism": f"replicas x{world}",
@@ -908,7 +915,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="batched", choices=["batched", "single_large", "single_4m", "plain_small"])
     ap.add_argument("--engine", default="auto", choices=["auto", "warp", "lane", "round"])
-    ap.add_argument("--radius", type=int, default=4)
+    ap.add_argument("--radius", type=int, default=None,
+                    help="round engine window radius (default: 3 for plain_small, 4 otherwise)")
     ap.add_argument("--nsys", type=int, default=None)
     ap.add_argument("--coll", type=int, default=None)
     ap.add_argument("--cpu-coll", type=int, default=250000, help="collisions per sampled system (CPU baseline)")
