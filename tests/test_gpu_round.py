@@ -80,11 +80,14 @@ def oracle_run_to(oracle, start, t_stop):
 
 @pytest.mark.parametrize("N,phi,seed,t_stop,mode", [(20000, 0.72, 5, 3.0, 0), (4096, 0.45, 6, 12.0, 0),
                                                      (100000, 0.72, 8, 0.6, 0), (100000, 0.72, 8, 0.6, 1),
-                                                     (640000, 0.72, 9, 0.25, 1), (640000, 0.72, 9, 0.25, 2)])
+                                                     (640000, 0.72, 9, 0.25, 1), (640000, 0.72, 9, 0.25, 2),
+                                                     (640000, 0.72, 9, 0.5, 0)])
 def test_rounds_match_oracle_state(edmd, oracle, N, phi, seed, t_stop, mode):
     """Larger systems against the oracle: counters, final state, screenshot at t = 1.
     mode 1 runs every round one thread per event, mode 2 adds the FP32 screen
-    of separating pairs."""
+    of separating pairs.  The 640,000-disk system in mode 0 has rounds of more
+    events than k_process has resident warps, so warps past their first event
+    take the rest of a round from its counter."""
     s = edmd.hex_start(N, phi, seed)
     o, n = oracle_run_to(oracle, s, t_stop)
     eng = edmd.Engine([dict(desc=edmd.default_desc(s["N"], s["Lx"], s["Ly"]), **s)])
@@ -96,6 +99,10 @@ def test_rounds_match_oracle_state(edmd, oracle, N, phi, seed, t_stop, mode):
     assert (c["ncol"], c["ncross"]) == (oc["ncol"], oc["ncross"]) and c["ncol"] == n
     assert c["t"] == o.t
     assert (c["nscreen"] > 0) == (mode == 2)
+    if mode == 0 and N >= 640000:
+        torch = pytest.importorskip("torch")
+        wave = 20 * torch.cuda.get_device_properties(0).multi_processor_count   # one-warp blocks, 20 per SM
+        assert c["nevents"] / rounds > wave      # rounds counts whole 32-round graphs: an underestimate
     st, ost = eng.state(0), o.state()
     for k in ("x", "y", "vx", "vy"):
         np.testing.assert_array_equal(st[k], ost[k])
