@@ -75,7 +75,7 @@ def build(verbose=False):
     lib = os.path.join(HERE, "libedmd_gpu.so")
     if _newer(lib, objs):
         _run_all([[_nvcc(), "-gencode", "arch=compute_103a,code=sm_103a", "-shared", "-o", lib]
-                  + objs + ["-lcudart", "-lm"]])
+                  + objs + ["-lcudart", "-lpthread", "-lm"]])
     main_src = os.path.join(HOST, "edmd_main.c")
     exe = os.path.join(HERE, "edmd")
     if os.path.exists(main_src) and _newer(exe, [main_src, lib] + headers):

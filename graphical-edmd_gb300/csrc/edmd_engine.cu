@@ -27,6 +27,8 @@
 #include <cstring>
 #include <string>
 #include <algorithm>
+#include <memory>
+#include <thread>
 #include <vector>
 
 using namespace edmd;
@@ -1250,6 +1252,28 @@ extern "C" int edmd_device_info(char* name, int32_t cap, int32_t* sm_count) {
 
 
 
+// host threads for staging n disks: one below 2^16 disks, else up to 16
+static int staging_threads(int64_t n) {
+  if (n < ((int64_t)1 << 16)) return 1;
+  const unsigned hc = std::thread::hardware_concurrency();
+  return (int)std::max(1u, std::min(hc, 16u));
+}
+
+// run f(0) .. f(n-1), on n threads where they can be had (inline otherwise)
+template <class F>
+static void run_threads(int n, F&& f) {
+  std::vector<std::thread> pool;
+  for (int k = 1; k < n; k++) {
+    try {
+      pool.emplace_back(f, k);
+    } catch (...) {
+      f(k);
+    }
+  }
+  f(0);
+  for (auto& th : pool) th.join();
+}
+
 // (Re)initialise every system from host arrays: the cell lists are built on
 // the host in index order (cellListInit src/EDMD.c:1906 -> addToCell 2053,
 // push-front), the event set on the device (eventListInit 1935).
@@ -1262,38 +1286,69 @@ static int stage_all(edmd_ctx* ctx, const double* x, const double* y, const doub
                      bool restart) {
   ctx->round_dirty = false;
   const int64_t TN = ctx->total_N;
-  std::vector<Disk> hd(TN);
-  std::vector<int32_t> hcx(TN), hcy(TN), hprv(TN);
+  const int nsys = ctx->nsys;
+  // every field of every staged record is written below
+  std::unique_ptr<Disk[]> hd(new Disk[TN]);
+  std::unique_ptr<int32_t[]> hcx(new int32_t[TN]), hcy(new int32_t[TN]), hprv(new int32_t[TN]);
   std::vector<int32_t> hhead(ctx->total_C, NIL);
-  std::vector<SysState> hst(ctx->nsys);
-  for (int s = 0; s < ctx->nsys; s++) {
-    const SysDev& S = ctx->hs[s];
-    const Box& B = S.B;
-    const edmd_system_desc& D = ctx->desc[s];
-    const int64_t o = ctx->disk_off[s];
-    int32_t* head = hhead.data() + ctx->cell_off[s];
-    for (int64_t i = 0; i < B.N; i++) {
-      int64_t g = o + i;
+  std::vector<SysState> hst(nsys);
+  const int nth = staging_threads(TN);
+  // records and cells, disk by disk, in contiguous slices of the concatenated
+  // disks; each slice stops at its first bad disk, so the smallest of those is
+  // the first bad disk in index order (2 g: position, 2 g + 1: radius)
+  std::vector<int64_t> bad(nth, INT64_MAX);
+  run_threads(nth, [&](int k) {
+    const int64_t lo = TN * k / nth, hi = TN * (k + 1) / nth;
+    int s = (int)(std::upper_bound(ctx->disk_off.begin(), ctx->disk_off.end(), lo) - ctx->disk_off.begin()) - 1;
+    for (int64_t g = lo; g < hi; g++) {
+      while (s + 1 < nsys && g >= ctx->disk_off[s + 1]) s++;
+      const Box& B = ctx->hs[s].B;
+      const edmd_system_desc& D = ctx->desc[s];
       double px = x[g], py = y[g];
       if (restart) {                     // PBCpostX/Y on loaded positions (src/EDMD.c:1405-1406)
         if (px < 0) px += D.Lx; else if (px >= D.Lx) px -= D.Lx;
         if (py < 0) py += D.Ly; else if (py >= D.Ly) py -= D.Ly;
       }
-      if (!(px >= 0 && px < D.Lx && py >= 0 && py < D.Ly))
-        return set_err(ctx, EDMD_ERR_ARG, "position outside the box (system " + std::to_string(s) + ")");
-      if (!radius_ok(rad[g]))
-        return set_err(ctx, EDMD_ERR_ARG, "radius not zero or normal positive (system " + std::to_string(s) + ")");
+      if (!(px >= 0 && px < D.Lx && py >= 0 && py < D.Ly)) { bad[k] = 2 * g; return; }
+      if (!radius_ok(rad[g])) { bad[k] = 2 * g + 1; return; }
       Disk& q = hd[g];
       q.x = px; q.y = py; q.vx = vx[g]; q.vy = vy[g]; q.tl = 0; q.rad = rad[g]; q.m = m[g];
       q.coll = 0;
       int X = (int)(q.x * B.cxf), Y = (int)(q.y * B.cyf);
       if (X >= B.Nxc) X = B.Nxc - 1;
       if (Y >= B.Nyc) Y = B.Nyc - 1;
-      hcx[g] = X; hcy[g] = Y; hprv[g] = NIL;
-      q.nxt = head[Y * B.Nxc + X];
-      head[Y * B.Nxc + X] = (int32_t)i;
-      if (q.nxt != NIL) hprv[o + q.nxt] = (int32_t)i;
+      hcx[g] = X; hcy[g] = Y;
     }
+  });
+  const int64_t first_bad = *std::min_element(bad.begin(), bad.end());
+  if (first_bad != INT64_MAX) {
+    const int64_t g = first_bad / 2;
+    const int s = (int)(std::upper_bound(ctx->disk_off.begin(), ctx->disk_off.end(), g) - ctx->disk_off.begin()) - 1;
+    return set_err(ctx, EDMD_ERR_ARG, std::string(first_bad % 2 ? "radius not zero or normal positive"
+                                                                  : "position outside the box") +
+                                          " (system " + std::to_string(s) + ")");
+  }
+  // cell lists, system by system: push-front in index order (cellListInit
+  // src/EDMD.c:1906 -> addToCell 2053)
+  run_threads(std::min(nth, nsys), [&](int k) {
+    for (int s = k; s < nsys; s += std::min(nth, nsys)) {
+      const Box& B = ctx->hs[s].B;
+      const int64_t o = ctx->disk_off[s];
+      int32_t* head = hhead.data() + ctx->cell_off[s];
+      for (int64_t i = 0; i < B.N; i++) {
+        const int64_t g = o + i;
+        const int c = hcy[g] * B.Nxc + hcx[g];
+        hprv[g] = NIL;
+        hd[g].nxt = head[c];
+        head[c] = (int32_t)i;
+        if (hd[g].nxt != NIL) hprv[o + hd[g].nxt] = (int32_t)i;
+      }
+    }
+  });
+  for (int s = 0; s < nsys; s++) {
+    const SysDev& S = ctx->hs[s];
+    const Box& B = S.B;
+    const edmd_system_desc& D = ctx->desc[s];
     SysState& st = hst[s];
     memset(&st, 0, sizeof(st));
     st.k = 0; st.next_wrap = (uint64_t)B.N; st.ovf = NIL;
@@ -1305,12 +1360,12 @@ static int stage_all(edmd_ctx* ctx, const double* x, const double* y, const doub
   }
   cudaStream_t sm = ctx->stream;
   CK(cudaMemcpyAsync(ctx->st, hst.data(), ctx->nsys * sizeof(SysState), cudaMemcpyHostToDevice, sm));
-  CK(cudaMemcpyAsync(ctx->d, hd.data(), TN * sizeof(Disk), cudaMemcpyHostToDevice, sm));
+  CK(cudaMemcpyAsync(ctx->d, hd.get(), TN * sizeof(Disk), cudaMemcpyHostToDevice, sm));
   if (vr && !restart) CK(cudaMemcpyAsync(ctx->vr, vr, TN * 8, cudaMemcpyHostToDevice, sm));
   else if (!vr && !restart) CK(cudaMemsetAsync(ctx->vr, 0, TN * 8, sm));
-  CK(cudaMemcpyAsync(ctx->cx, hcx.data(), TN * 4, cudaMemcpyHostToDevice, sm));
-  CK(cudaMemcpyAsync(ctx->cy, hcy.data(), TN * 4, cudaMemcpyHostToDevice, sm));
-  CK(cudaMemcpyAsync(ctx->prv, hprv.data(), TN * 4, cudaMemcpyHostToDevice, sm));
+  CK(cudaMemcpyAsync(ctx->cx, hcx.get(), TN * 4, cudaMemcpyHostToDevice, sm));
+  CK(cudaMemcpyAsync(ctx->cy, hcy.get(), TN * 4, cudaMemcpyHostToDevice, sm));
+  CK(cudaMemcpyAsync(ctx->prv, hprv.get(), TN * 4, cudaMemcpyHostToDevice, sm));
   CK(cudaMemsetAsync(ctx->crossX, 0, TN * 4, sm));
   CK(cudaMemsetAsync(ctx->crossY, 0, TN * 4, sm));
   CK(cudaMemcpyAsync(ctx->head, hhead.data(), ctx->total_C * 4, cudaMemcpyHostToDevice, sm));
