@@ -399,17 +399,21 @@ class L2Flusher:
         self.buf = None
         self.k = 0
         self.l2_mb = None
+        self.why = "no CUDA device to torch"
         try:
             import torch
             if torch.cuda.is_available():
                 l2 = int(getattr(torch.cuda.get_device_properties(dev), "L2_cache_size", 0) or 0)
+                self.why = "torch gives no L2 size"
                 if l2 > 0:
                     self.l2_mb = l2 / 1e6
                     if state_bytes < 2 * l2:
                         self.torch = torch
                         self.buf = torch.empty(2 * l2, dtype=torch.uint8, device="cuda:%d" % dev)
-        except Exception:                                  # no CUDA torch: nothing to flush with
+        except Exception as e:                             # no CUDA torch: nothing to flush with
             self.buf = None
+            self.l2_mb = None
+            self.why = "flush buffer unavailable: %s" % repr(e)[:80]
 
     def __call__(self):
         if self.buf is None:
@@ -424,7 +428,7 @@ class L2Flusher:
                     "(a %.0f MB device write outside the timed calls)"
                     % (self.state_mb, self.l2_mb, self.buf.numel() / 1e6))
         if self.l2_mb is None:
-            return "state (~%.1f MB/GPU); L2 size unknown (no CUDA device to torch), no flush" % self.state_mb
+            return "state (~%.1f MB/GPU); L2 size unknown (%s), no flush" % (self.state_mb, self.why)
         return "state (~%.0f MB/GPU) larger than twice L2 (%.0f MB), no flush" % (self.state_mb, self.l2_mb)
 
 

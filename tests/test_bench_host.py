@@ -78,3 +78,18 @@ def test_flusher_without_a_device_says_so(monkeypatch):
     f = bench.L2Flusher(0, 1980 * 160)
     f()
     assert "no flush" in f.describe()
+
+
+def test_failed_flush_buffer_is_reported(monkeypatch):
+    made = []
+    fake = _fake_torch(made)
+
+    def no_memory(n, dtype=None, device=None):
+        raise RuntimeError("CUDA out of memory")
+
+    fake.empty = no_memory
+    monkeypatch.setitem(sys.modules, "torch", fake)
+    f = bench.L2Flusher(0, 1980 * 160)
+    f()
+    d = f.describe()
+    assert "no flush" in d and "out of memory" in d
